@@ -1,0 +1,293 @@
+"""GB300 path tracer: a drop-in for the render call of 1neskk/Ataraxia.
+
+Python mirror of the reference's Renderer / Scene / Camera interface
+(Engine/include/Renderer.h, Scene.h, Camera.h) over the C ABI in
+include/atx.h.  The reference's method names are kept as aliases
+(onResize, Render, getSettings, setSettings, resetFrameIndex, getImage).
+All rendering runs in libatx.so on the GPU; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Sequence
+
+import numpy as np
+
+from . import _native as N
+from ._native import AtxError, LIGHT_DTYPE, MATERIAL_DTYPE, SPHERE_DTYPE
+
+__all__ = [
+    "AtxError", "Camera", "Light", "Material", "Renderer", "Scene", "Settings", "Sphere",
+    "SPHERE_DTYPE", "MATERIAL_DTYPE", "LIGHT_DTYPE", "camera_matrices", "device_count",
+]
+
+
+@dataclass
+class Sphere:
+    """SceneNode.h:11-21."""
+    center: Sequence[float] = (0.0, 0.0, 0.0)
+    radius: float = 1.0
+    id: int = 0
+
+
+@dataclass
+class Material:
+    """Scene.h:28-47 (constructor argument order of Scene.h:44)."""
+    albedo: Sequence[float] = (1.0, 1.0, 1.0)
+    roughness: float = 0.0
+    metallic: float = 0.0
+    emissionColor: Sequence[float] = (0.0, 0.0, 0.0)
+    emissionIntensity: float = 0.0
+    id: int = 0
+    F0: Sequence[float] = (0.04, 0.04, 0.04)
+
+
+@dataclass
+class Light:
+    """Scene.h:17-26."""
+    position: Sequence[float] = (0.0, 0.0, 0.0)
+    color: Sequence[float] = (1.0, 1.0, 1.0)
+    intensity: float = 1.0
+
+
+@dataclass
+class Settings:
+    """Scene.h:49-56."""
+    accumulation: bool = True
+    skyLight: bool = False
+    maxBounces: int = 15
+
+
+@dataclass
+class Camera:
+    """Camera.h / Camera.cpp:14-21 defaults: fov 45, near 0.1, far 100, at (0, 0, 3) looking -Z."""
+    fov: float = 45.0
+    nearClip: float = 0.1
+    farClip: float = 100.0
+    position: Sequence[float] = (0.0, 0.0, 3.0)
+    direction: Sequence[float] = (0.0, 0.0, -1.0)
+
+    def desc(self) -> N.CameraDesc:
+        d = N.CameraDesc()
+        d.position[:] = [float(x) for x in self.position]
+        d.direction[:] = [float(x) for x in self.direction]
+        d.fov_deg, d.near_clip, d.far_clip = float(self.fov), float(self.nearClip), float(self.farClip)
+        return d
+
+
+@dataclass
+class Scene:
+    """Flat scene (the caller flattens the reference's node hierarchy, Renderer.cu:67-96).
+    spheres/materials/lights may be lists of the dataclasses above or structured numpy arrays
+    with SPHERE_DTYPE / MATERIAL_DTYPE / LIGHT_DTYPE."""
+    spheres: object = field(default_factory=list)
+    materials: object = field(default_factory=list)
+    lights: object = field(default_factory=list)
+    settings: Settings = field(default_factory=Settings)
+    camera: Camera = field(default_factory=Camera)
+
+    def arrays(self):
+        return _as_spheres(self.spheres), _as_materials(self.materials), _as_lights(self.lights)
+
+
+def _as_spheres(x) -> np.ndarray:
+    if isinstance(x, np.ndarray):
+        return np.ascontiguousarray(x, dtype=SPHERE_DTYPE)
+    a = np.zeros(len(x), dtype=SPHERE_DTYPE)
+    for i, s in enumerate(x):
+        a[i] = (tuple(s.center), s.radius, s.id)
+    return a
+
+
+def _as_materials(x) -> np.ndarray:
+    if isinstance(x, np.ndarray):
+        return np.ascontiguousarray(x, dtype=MATERIAL_DTYPE)
+    a = np.zeros(len(x), dtype=MATERIAL_DTYPE)
+    for i, m in enumerate(x):
+        a[i] = (tuple(m.albedo), m.roughness, m.metallic, tuple(m.F0), tuple(m.emissionColor),
+                m.emissionIntensity, m.id)
+    return a
+
+
+def _as_lights(x) -> np.ndarray:
+    if isinstance(x, np.ndarray):
+        return np.ascontiguousarray(x, dtype=LIGHT_DTYPE)
+    a = np.zeros(len(x), dtype=LIGHT_DTYPE)
+    for i, l in enumerate(x):
+        a[i] = (tuple(l.position), tuple(l.color), l.intensity)
+    return a
+
+
+def device_count() -> int:
+    n = C.c_int32(0)
+    N.check(N.lib().atx_device_count(C.byref(n)))
+    return n.value
+
+
+def measure_fp32_peak(device: int = 0) -> float:
+    """FP32 FFMA throughput of the device in TFLOP/s (atx_measure_fp32_peak)."""
+    t = C.c_double(0.0)
+    N.check(N.lib().atx_measure_fp32_peak(device, C.byref(t)))
+    return t.value
+
+
+def camera_matrices(camera: Camera, width: int, height: int):
+    """Camera.cpp:134-159 on the host: (view, inv_view, proj, inv_proj) as 4x4 column-major float32
+    arrays (element [c, r] = column c, row r, as glm stores them).  Needs no GPU."""
+    out = [np.zeros(16, dtype=np.float32) for _ in range(4)]
+    d = camera.desc()
+    N.check(N.lib().atx_camera_matrices(C.byref(d), width, height, *[N.ptr(o) for o in out]))
+    return tuple(o.reshape(4, 4) for o in out)
+
+
+class Renderer:
+    """Renderer.h:19-86 over libatx.so.
+
+    Render(camera, scene, spp) follows Renderer.cu:173-249: the scene is uploaded when a different
+    Scene object is passed or the frame index is 1, spp consecutive frames are traced, and the frame
+    index advances (accumulation on) or stays 1 (off)."""
+
+    def __init__(self, device: int = 0, wave_paths: int = 0, threads: int = 0, bvh_threshold: int = 0,
+                 bvh_leaf_size: int = 0, hbm_budget_bytes: int = 0, flags: int = 0):
+        cfg = N.Config(device, wave_paths, threads, bvh_threshold, bvh_leaf_size, flags, hbm_budget_bytes)
+        h = C.c_void_p()
+        N.check(N.lib().atx_renderer_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self._scene_id = None
+        self.width = 0
+        self.height = 0
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().atx_renderer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- reference interface
+    def on_resize(self, width: int, height: int):
+        N.check(N.lib().atx_resize(self._h, width, height))
+        self.width, self.height = width, height
+
+    onResize = on_resize
+
+    def get_settings(self) -> Settings:
+        s = N.Settings()
+        N.check(N.lib().atx_get_settings(self._h, C.byref(s)))
+        return Settings(bool(s.accumulation), bool(s.sky_light), int(s.max_bounces))
+
+    getSettings = get_settings
+
+    def set_settings(self, settings: Settings):
+        s = N.Settings(int(bool(settings.accumulation)), int(bool(settings.skyLight)), (C.c_uint8 * 2)(),
+                       int(settings.maxBounces))
+        N.check(N.lib().atx_set_settings(self._h, C.byref(s)))
+
+    setSettings = set_settings
+
+    def reset_frame_index(self):
+        N.check(N.lib().atx_reset_frame_index(self._h))
+
+    resetFrameIndex = reset_frame_index
+
+    @property
+    def frame_index(self) -> int:
+        f = C.c_uint32()
+        N.check(N.lib().atx_get_frame_index(self._h, C.byref(f)))
+        return f.value
+
+    def render(self, camera: Camera, scene: Scene, spp: int = 1):
+        if self._scene_id != id(scene) or self.frame_index == 1:
+            self.set_scene(*scene.arrays())
+            self._scene_id = id(scene)
+        self.set_camera(camera)
+        self.render_frames(spp)
+
+    Render = render
+
+    def get_image(self) -> np.ndarray:
+        """RGBA8 image as (H, W) uint32, A<<24 | B<<16 | G<<8 | R (Renderer.h:70-78)."""
+        out = np.empty(self.width * self.height, dtype=np.uint32)
+        N.check(N.lib().atx_read_image(self._h, N.ptr(out), out.size))
+        return out.reshape(self.height, self.width)
+
+    getImage = get_image
+
+    # -- explicit API
+    def set_scene(self, spheres: np.ndarray, materials: np.ndarray, lights: np.ndarray):
+        s, m, l = _as_spheres(spheres), _as_materials(materials), _as_lights(lights)
+        N.check(N.lib().atx_set_scene(self._h, N.ptr(s) if len(s) else None, len(s), N.ptr(m) if len(m) else None,
+                                      len(m), N.ptr(l) if len(l) else None, len(l)))
+
+    def set_camera(self, camera: Camera):
+        d = camera.desc()
+        N.check(N.lib().atx_set_camera(self._h, C.byref(d)))
+
+    def set_camera_matrices(self, inv_view: np.ndarray, inv_proj: np.ndarray, position):
+        iv = np.ascontiguousarray(inv_view, dtype=np.float32).reshape(16)
+        ip = np.ascontiguousarray(inv_proj, dtype=np.float32).reshape(16)
+        p = np.ascontiguousarray(position, dtype=np.float32).reshape(3)
+        N.check(N.lib().atx_set_camera_matrices(self._h, N.ptr(iv), N.ptr(ip), N.ptr(p)))
+
+    def render_frames(self, spp: int = 1):
+        N.check(N.lib().atx_render(self._h, spp))
+
+    def synchronize(self):
+        N.check(N.lib().atx_synchronize(self._h))
+
+    def get_accumulation(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Float4 accumulator as (H, W, 4) float32."""
+        if out is None:
+            out = np.empty((self.height, self.width, 4), dtype=np.float32)
+        N.check(N.lib().atx_read_accumulation(self._h, N.ptr(out), self.width * self.height))
+        return out
+
+    def stats(self) -> dict:
+        s = N.Stats()
+        N.check(N.lib().atx_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in N.Stats._fields_ if k != "reserved"}
+
+    def kernel_times(self) -> dict:
+        t = N.KernelTimes()
+        N.check(N.lib().atx_get_kernel_times(self._h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in N.KernelTimes._fields_}
+
+    def reset_kernel_times(self):
+        N.check(N.lib().atx_reset_kernel_times(self._h))
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        N.check(N.lib().atx_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def trace_nearest(self, origins: np.ndarray, dirs: np.ndarray):
+        o = np.ascontiguousarray(origins, dtype=np.float32).reshape(-1, 3)
+        d = np.ascontiguousarray(dirs, dtype=np.float32).reshape(-1, 3)
+        n = len(o)
+        t = np.empty(n, dtype=np.float32)
+        ids = np.empty(n, dtype=np.int32)
+        N.check(N.lib().atx_trace_nearest(self._h, N.ptr(o), N.ptr(d), n, N.ptr(t), N.ptr(ids)))
+        return t, ids
+
+    def primary_directions(self) -> np.ndarray:
+        out = np.empty((self.height * self.width, 3), dtype=np.float32)
+        N.check(N.lib().atx_primary_directions(self._h, N.ptr(out), self.width * self.height))
+        return out
+
+    def device_buffers(self):
+        a, i = C.c_void_p(), C.c_void_p()
+        N.check(N.lib().atx_device_buffers(self._h, C.byref(a), C.byref(i)))
+        return a.value, i.value

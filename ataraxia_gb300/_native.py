@@ -1,0 +1,140 @@
+"""ctypes binding of libatx.so (include/atx.h).
+
+The library must have been built (``python -m ataraxia_gb300.build``); there
+is no fallback: loading fails with an error that says so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libatx.so"
+
+# Same layout as atx_sphere / atx_material / atx_light (and the reference's
+# Sphere 20 B, Material 52 B, Light 28 B).
+SPHERE_DTYPE = np.dtype([("center", "<f4", (3,)), ("radius", "<f4"), ("material", "<i4")])
+MATERIAL_DTYPE = np.dtype([
+    ("albedo", "<f4", (3,)), ("roughness", "<f4"), ("metallic", "<f4"), ("f0", "<f4", (3,)),
+    ("emission_color", "<f4", (3,)), ("emission_intensity", "<f4"), ("id", "<i4"),
+])
+LIGHT_DTYPE = np.dtype([("position", "<f4", (3,)), ("color", "<f4", (3,)), ("intensity", "<f4")])
+assert SPHERE_DTYPE.itemsize == 20 and MATERIAL_DTYPE.itemsize == 52 and LIGHT_DTYPE.itemsize == 28
+
+STATUS = {
+    0: "ATX_OK", 1: "ATX_ERR_INVALID_ARG", 2: "ATX_ERR_OUT_OF_MEMORY", 3: "ATX_ERR_CUDA",
+    4: "ATX_ERR_TIMEOUT", 5: "ATX_ERR_BUSY", 6: "ATX_ERR_NOT_FOUND", 7: "ATX_ERR_CANCELLED",
+    8: "ATX_ERR_NO_DEVICE", 9: "ATX_ERR_PARSE",
+}
+
+
+class AtxError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+        self.message = message
+
+
+class Settings(C.Structure):
+    _fields_ = [("accumulation", C.c_uint8), ("sky_light", C.c_uint8), ("reserved", C.c_uint8 * 2),
+                ("max_bounces", C.c_int32)]
+
+
+class CameraDesc(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("direction", C.c_float * 3), ("fov_deg", C.c_float),
+                ("near_clip", C.c_float), ("far_clip", C.c_float)]
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("wave_paths", C.c_uint32), ("threads", C.c_uint32),
+                ("bvh_threshold", C.c_uint32), ("bvh_leaf_size", C.c_uint32), ("flags", C.c_uint32),
+                ("hbm_budget_bytes", C.c_uint64)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("frames", C.c_uint64), ("paths", C.c_uint64), ("extension_rays", C.c_uint64),
+                ("shadow_rays", C.c_uint64), ("kernel_launches", C.c_uint64), ("device_bytes", C.c_uint64),
+                ("last_render_ms", C.c_double), ("bvh_in_use", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class KernelTimes(C.Structure):
+    _fields_ = [("extend_ms", C.c_double), ("shadow_ms", C.c_double), ("accumulate_ms", C.c_double),
+                ("other_ms", C.c_double), ("extend_launches", C.c_uint64), ("shadow_launches", C.c_uint64),
+                ("accumulate_launches", C.c_uint64), ("other_launches", C.c_uint64)]
+
+
+FLAG_NO_GRAPHS = 1
+FLAG_PROFILE_KERNELS = 2
+
+assert C.sizeof(Settings) == 8 and C.sizeof(CameraDesc) == 36
+
+_P = C.c_void_p
+_F = C.POINTER(C.c_float)
+_U32 = C.c_uint32
+_U64 = C.c_uint64
+_ST = C.c_int
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "atx_abi_version": (C.c_int, []),
+    "atx_status_string": (C.c_char_p, [C.c_int]),
+    "atx_last_error": (C.c_char_p, []),
+    "atx_device_count": (_ST, [C.POINTER(C.c_int32)]),
+    "atx_renderer_create": (_ST, [C.POINTER(Config), C.POINTER(_P)]),
+    "atx_renderer_destroy": (_ST, [_P]),
+    "atx_resize": (_ST, [_P, _U32, _U32]),
+    "atx_set_scene": (_ST, [_P, _P, _U32, _P, _U32, _P, _U32]),
+    "atx_set_settings": (_ST, [_P, C.POINTER(Settings)]),
+    "atx_get_settings": (_ST, [_P, C.POINTER(Settings)]),
+    "atx_reset_frame_index": (_ST, [_P]),
+    "atx_get_frame_index": (_ST, [_P, C.POINTER(C.c_uint32)]),
+    "atx_set_camera": (_ST, [_P, C.POINTER(CameraDesc)]),
+    "atx_set_camera_matrices": (_ST, [_P, _P, _P, _P]),
+    "atx_render": (_ST, [_P, _U32]),
+    "atx_synchronize": (_ST, [_P]),
+    "atx_read_accumulation": (_ST, [_P, _P, _U64]),
+    "atx_read_image": (_ST, [_P, _P, _U64]),
+    "atx_device_buffers": (_ST, [_P, C.POINTER(_P), C.POINTER(_P)]),
+    "atx_get_stats": (_ST, [_P, C.POINTER(Stats)]),
+    "atx_get_kernel_times": (_ST, [_P, C.POINTER(KernelTimes)]),
+    "atx_reset_kernel_times": (_ST, [_P]),
+    "atx_get_stream": (_ST, [_P, C.POINTER(_P)]),
+    "atx_measure_fp32_peak": (_ST, [C.c_int32, C.POINTER(C.c_double)]),
+    "atx_host_alloc": (_ST, [_U64, C.POINTER(_P)]),
+    "atx_host_free": (_ST, [_P]),
+    "atx_camera_matrices": (_ST, [C.POINTER(CameraDesc), _U32, _U32, _P, _P, _P, _P]),
+    "atx_trace_nearest": (_ST, [_P, _P, _P, _U64, _P, _P]),
+    "atx_primary_directions": (_ST, [_P, _P, _U64]),
+}
+
+_lib = None
+
+
+def lib():
+    """Loads libatx.so once and declares every entry point's signature."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is not built; run `python -m ataraxia_gb300.build` "
+                               "(there is no CPU fallback)")
+        h = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(h, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = h
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != 0:
+        msg = lib().atx_last_error()
+        raise AtxError(status, msg.decode() if msg else "")
+
+
+def ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "arrays passed to libatx must be C-contiguous"
+    return C.c_void_p(a.ctypes.data)

@@ -1,0 +1,282 @@
+// extern "C" entry points of libatx.so (declared in include/atx.h).  Each
+// wrapper checks its handle, clears the thread's last error and converts C++
+// exceptions into status codes so nothing unwinds across the C boundary.
+#include <new>
+
+#include "atx.h"
+#include "host_common.h"
+#include "renderer.h"
+
+struct atx_renderer {
+    atx::Renderer impl;
+    explicit atx_renderer(const atx_config& c) : impl(c) {}
+};
+
+namespace {
+
+template <class F>
+atx_status guarded(F&& f)
+{
+    atx::clear_error();
+    try {
+        return f();
+    } catch (const std::bad_alloc&) {
+        return atx::fail(ATX_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (...) {
+        return atx::fail(ATX_ERR_CUDA, "unexpected exception");
+    }
+}
+
+#define NEED(r) \
+    if (!(r)) return atx::fail(ATX_ERR_INVALID_ARG, "%s: null renderer", __func__)
+
+}  // namespace
+
+extern "C" {
+
+ATX_API int atx_abi_version(void) { return ATX_ABI_VERSION; }
+
+ATX_API const char* atx_status_string(atx_status s)
+{
+    switch (s) {
+    case ATX_OK: return "ok";
+    case ATX_ERR_INVALID_ARG: return "invalid argument";
+    case ATX_ERR_OUT_OF_MEMORY: return "out of memory";
+    case ATX_ERR_CUDA: return "CUDA error";
+    case ATX_ERR_TIMEOUT: return "timeout";
+    case ATX_ERR_BUSY: return "busy";
+    case ATX_ERR_NOT_FOUND: return "not found";
+    case ATX_ERR_CANCELLED: return "cancelled";
+    case ATX_ERR_NO_DEVICE: return "no CUDA device";
+    case ATX_ERR_PARSE: return "parse error";
+    }
+    return "unknown status";
+}
+
+ATX_API const char* atx_last_error(void) { return atx::last_error_message(); }
+
+ATX_API atx_status atx_device_count(int32_t* count)
+{
+    return guarded([&]() -> atx_status {
+        if (!count) return atx::fail(ATX_ERR_INVALID_ARG, "atx_device_count: null pointer");
+        int n = 0;
+        cudaError_t e = cudaGetDeviceCount(&n);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            *count = 0;
+            return ATX_OK;
+        }
+        *count = n;
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_renderer_create(const atx_config* config, atx_renderer** out)
+{
+    return guarded([&]() -> atx_status {
+        if (!out) return atx::fail(ATX_ERR_INVALID_ARG, "atx_renderer_create: null out");
+        *out = nullptr;
+        atx_config c{};
+        if (config) c = *config;
+        atx_renderer* r = new atx_renderer(c);
+        atx_status st = r->impl.init();
+        if (st != ATX_OK) {
+            delete r;
+            return st;
+        }
+        *out = r;
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_renderer_destroy(atx_renderer* r)
+{
+    return guarded([&]() -> atx_status {
+        delete r;
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_resize(atx_renderer* r, uint32_t w, uint32_t h)
+{
+    return guarded([&]() -> atx_status { NEED(r); return r->impl.resize(w, h); });
+}
+
+ATX_API atx_status atx_set_scene(atx_renderer* r, const atx_sphere* s, uint32_t n, const atx_material* m,
+                                 uint32_t nm, const atx_light* l, uint32_t nl)
+{
+    return guarded([&]() -> atx_status { NEED(r); return r->impl.set_scene(s, n, m, nm, l, nl); });
+}
+
+ATX_API atx_status atx_set_settings(atx_renderer* r, const atx_settings* s)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        if (!s) return atx::fail(ATX_ERR_INVALID_ARG, "atx_set_settings: null settings");
+        return r->impl.set_settings(*s);
+    });
+}
+
+ATX_API atx_status atx_get_settings(const atx_renderer* r, atx_settings* s)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        if (!s) return atx::fail(ATX_ERR_INVALID_ARG, "atx_get_settings: null settings");
+        *s = r->impl.settings();
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_reset_frame_index(atx_renderer* r)
+{
+    return guarded([&]() -> atx_status { NEED(r); r->impl.reset_frame_index(); return ATX_OK; });
+}
+
+ATX_API atx_status atx_get_frame_index(const atx_renderer* r, uint32_t* f)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        if (!f) return atx::fail(ATX_ERR_INVALID_ARG, "atx_get_frame_index: null pointer");
+        *f = r->impl.frame_index();
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_set_camera(atx_renderer* r, const atx_camera* c)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        if (!c) return atx::fail(ATX_ERR_INVALID_ARG, "atx_set_camera: null camera");
+        return r->impl.set_camera(*c);
+    });
+}
+
+ATX_API atx_status atx_set_camera_matrices(atx_renderer* r, const float inv_view[16], const float inv_proj[16],
+                                           const float position[3])
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        if (!inv_view || !inv_proj || !position) return atx::fail(ATX_ERR_INVALID_ARG, "atx_set_camera_matrices: null");
+        return r->impl.set_camera_matrices(inv_view, inv_proj, position);
+    });
+}
+
+ATX_API atx_status atx_render(atx_renderer* r, uint32_t spp)
+{
+    return guarded([&]() -> atx_status { NEED(r); return r->impl.render(spp); });
+}
+
+ATX_API atx_status atx_synchronize(atx_renderer* r)
+{
+    return guarded([&]() -> atx_status { NEED(r); return r->impl.synchronize(); });
+}
+
+ATX_API atx_status atx_read_accumulation(atx_renderer* r, float* host_rgba, uint64_t n)
+{
+    return guarded([&]() -> atx_status { NEED(r); return r->impl.read_accumulation(host_rgba, n); });
+}
+
+ATX_API atx_status atx_read_image(atx_renderer* r, uint32_t* host_rgba8, uint64_t n)
+{
+    return guarded([&]() -> atx_status { NEED(r); return r->impl.read_image(host_rgba8, n); });
+}
+
+ATX_API atx_status atx_device_buffers(atx_renderer* r, void** accumulation, void** image)
+{
+    return guarded([&]() -> atx_status { NEED(r); return r->impl.device_buffers(accumulation, image); });
+}
+
+ATX_API atx_status atx_get_stats(const atx_renderer* r, atx_stats* s)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        if (!s) return atx::fail(ATX_ERR_INVALID_ARG, "atx_get_stats: null pointer");
+        return const_cast<atx_renderer*>(r)->impl.stats(s);
+    });
+}
+
+ATX_API atx_status atx_get_kernel_times(atx_renderer* r, atx_kernel_times* t)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        if (!t) return atx::fail(ATX_ERR_INVALID_ARG, "atx_get_kernel_times: null pointer");
+        return r->impl.kernel_times(t);
+    });
+}
+
+ATX_API atx_status atx_reset_kernel_times(atx_renderer* r)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        atx_kernel_times drop{};
+        ATX_TRY(r->impl.kernel_times(&drop));
+        r->impl.reset_kernel_times();
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_get_stream(atx_renderer* r, void** stream)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        if (!stream) return atx::fail(ATX_ERR_INVALID_ARG, "atx_get_stream: null pointer");
+        *stream = static_cast<void*>(r->impl.stream());
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_measure_fp32_peak(int32_t device, double* tflops)
+{
+    return guarded([&]() -> atx_status {
+        if (!tflops) return atx::fail(ATX_ERR_INVALID_ARG, "atx_measure_fp32_peak: null pointer");
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+            (void)cudaGetLastError();
+            return atx::fail(ATX_ERR_NO_DEVICE, "no CUDA device visible");
+        }
+        ATX_CUDA(atx::measure_fp32_peak(device, tflops));
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_host_alloc(uint64_t bytes, void** out)
+{
+    return guarded([&]() -> atx_status {
+        if (!out) return atx::fail(ATX_ERR_INVALID_ARG, "atx_host_alloc: null out");
+        *out = nullptr;
+        ATX_CUDA(cudaMallocHost(out, bytes ? bytes : 1));
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_host_free(void* p)
+{
+    return guarded([&]() -> atx_status {
+        if (p) ATX_CUDA(cudaFreeHost(p));
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_camera_matrices(const atx_camera* c, uint32_t w, uint32_t h, float view[16],
+                                       float inv_view[16], float proj[16], float inv_proj[16])
+{
+    return guarded([&]() -> atx_status {
+        if (!c) return atx::fail(ATX_ERR_INVALID_ARG, "atx_camera_matrices: null camera");
+        if (w == 0 || h == 0) return atx::fail(ATX_ERR_INVALID_ARG, "atx_camera_matrices: zero viewport");
+        atx::camera_matrices(*c, w, h, view, inv_view, proj, inv_proj);
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_trace_nearest(atx_renderer* r, const float* origins, const float* dirs, uint64_t n,
+                                     float* t_out, int32_t* id_out)
+{
+    return guarded([&]() -> atx_status { NEED(r); return r->impl.trace_nearest(origins, dirs, n, t_out, id_out); });
+}
+
+ATX_API atx_status atx_primary_directions(atx_renderer* r, float* host_dirs, uint64_t n_pixels)
+{
+    return guarded([&]() -> atx_status { NEED(r); return r->impl.primary_directions(host_dirs, n_pixels); });
+}
+
+}  // extern "C"

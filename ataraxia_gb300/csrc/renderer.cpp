@@ -1,0 +1,489 @@
+// Renderer: the reference's Renderer::onResize / Render state machine
+// (Renderer.cu:98-249) over the wavefront kernels, with explicit scene upload,
+// device-side ray generation and status codes instead of exit()/stderr.
+#include "renderer.h"
+
+#include <algorithm>
+#include <cstring>
+
+#include "lbvh.h"
+
+namespace atx {
+
+namespace {
+constexpr uint32_t kDefaultWavePaths = 4u << 20;   // 4 Mi paths, ~480 MB of state
+constexpr uint32_t kDefaultBvhThreshold = 1024;
+constexpr uint32_t kDefaultBvhLeaf = 2;
+constexpr uint32_t kMaxBounces = 4096;
+}  // namespace
+
+// ------------------------------------------------------------------ scene
+
+atx_status SceneStore::upload(const atx_sphere* s, uint32_t n, const atx_material* m, uint32_t nm,
+                              const atx_light* l, uint32_t nl, Budget* budget, cudaStream_t stream)
+{
+    if ((n && !s) || (nm && !m) || (nl && !l)) return fail(ATX_ERR_INVALID_ARG, "set_scene: null array");
+    if (n > 0 && nm == 0) return fail(ATX_ERR_INVALID_ARG, "set_scene: spheres need at least one material");
+
+    std::vector<float4> sph(n);
+    std::vector<int32_t> smat(n);
+    std::vector<float> srad(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float r = s[i].radius;
+        sph[i] = make_float4(s[i].center[0], s[i].center[1], s[i].center[2], r * r);
+        // Renderer.cu:30-37: ids outside [0, materials) render with material 0
+        smat[i] = ((uint32_t)s[i].material >= nm) ? 0 : s[i].material;
+        srad[i] = r;
+    }
+    std::vector<DevMaterial> mats(nm);
+    for (uint32_t i = 0; i < nm; ++i) {
+        DevMaterial& d = mats[i];
+        for (int k = 0; k < 3; ++k) {
+            d.albedo[k] = m[i].albedo[k];
+            d.f0[k] = m[i].f0[k];
+            d.emission[k] = m[i].emission_color[k] * m[i].emission_intensity;  // Scene.h:41
+        }
+        d.roughness = m[i].roughness;
+        d.metallic = m[i].metallic;
+        d.emission_intensity = m[i].emission_intensity;
+    }
+    std::vector<DevLight> lts(nl);
+    for (uint32_t i = 0; i < nl; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            lts[i].pos[k] = l[i].position[k];
+            lts[i].le[k] = l[i].color[k] * l[i].intensity;  // Renderer.cu:362
+        }
+        lts[i].pad0 = lts[i].pad1 = 0.0f;
+    }
+
+    ATX_TRY(sph.empty() ? ATX_OK : this->sph.ensure(n * sizeof(float4), budget, "sphere table"));
+    ATX_TRY(smat.empty() ? ATX_OK : sph_mat.ensure(n * sizeof(int32_t), budget, "sphere materials"));
+    ATX_TRY(srad.empty() ? ATX_OK : sph_rad.ensure(n * sizeof(float), budget, "sphere radii"));
+    ATX_TRY(mats.empty() ? ATX_OK : mat.ensure(nm * sizeof(DevMaterial), budget, "materials"));
+    ATX_TRY(lts.empty() ? ATX_OK : lights.ensure(nl * sizeof(DevLight), budget, "lights"));
+    // The host vectors die at return: copy synchronously with respect to them.
+    if (n) {
+        ATX_CUDA(cudaMemcpyAsync(this->sph.get(), sph.data(), n * sizeof(float4), cudaMemcpyHostToDevice, stream));
+        ATX_CUDA(cudaMemcpyAsync(sph_mat.get(), smat.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+        ATX_CUDA(cudaMemcpyAsync(sph_rad.get(), srad.data(), n * sizeof(float), cudaMemcpyHostToDevice, stream));
+    }
+    if (nm) ATX_CUDA(cudaMemcpyAsync(mat.get(), mats.data(), nm * sizeof(DevMaterial), cudaMemcpyHostToDevice, stream));
+    if (nl) ATX_CUDA(cudaMemcpyAsync(lights.get(), lts.data(), nl * sizeof(DevLight), cudaMemcpyHostToDevice, stream));
+
+    view = SceneView{};
+    view.sph = n ? this->sph.as<float4>() : nullptr;
+    view.sph_mat = n ? sph_mat.as<int32_t>() : nullptr;
+    view.mat = nm ? mat.as<DevMaterial>() : nullptr;
+    view.lights = nl ? lights.as<DevLight>() : nullptr;
+    view.n_sph = n;
+    view.n_mat = nm;
+    view.n_lights = nl;
+
+    const uint32_t thr = bvh_threshold ? bvh_threshold : kDefaultBvhThreshold;
+    if (n >= thr && n > 1) {
+        const uint64_t need = lbvh_bytes(n);
+        ATX_TRY(bvh.ensure(need, budget, "lbvh"));
+        BvhView bv{};
+        ATX_CUDA(lbvh_build(view.sph, sph_rad.as<float>(), n, bvh_leaf ? bvh_leaf : kDefaultBvhLeaf, bvh.get(),
+                            bvh.bytes(), &bv, stream));
+        view.bvh = bv;
+        view.use_bvh = 1;
+    } else {
+        bvh.reset();
+    }
+    ATX_CUDA(cudaStreamSynchronize(stream));
+    return ATX_OK;
+}
+
+// ------------------------------------------------------------------ waves
+
+uint64_t WaveStore::bytes_for(uint32_t capacity, uint32_t max_bounces)
+{
+    const uint64_t c = capacity;
+    return c * (7 * sizeof(float4) + 2 * sizeof(uint32_t)) + 2ull * (max_bounces + 1) * sizeof(uint32_t) + 16 +
+           10 * 256;
+}
+
+atx_status WaveStore::ensure(uint32_t capacity, uint32_t max_bounces, Budget* budget)
+{
+    if (view.capacity >= capacity && bounces >= max_bounces && buf.get()) return ATX_OK;
+    const uint32_t cap = std::max(capacity, view.capacity);
+    const uint32_t b = std::max(max_bounces, bounces);
+    buf.reset();
+    ATX_TRY(buf.ensure(bytes_for(cap, b), budget, "path state"));
+    char* p = buf.as<char>();
+    auto take = [&](uint64_t bytes) {
+        char* r = p;
+        p += (bytes + 255) & ~uint64_t(255);
+        return r;
+    };
+    const uint64_t c = cap;
+    view.ray_o = reinterpret_cast<float4*>(take(c * sizeof(float4)));
+    view.ray_d = reinterpret_cast<float4*>(take(c * sizeof(float4)));
+    view.thr = reinterpret_cast<float4*>(take(c * sizeof(float4)));
+    view.col = reinterpret_cast<float4*>(take(c * sizeof(float4)));
+    view.sh_o = reinterpret_cast<float4*>(take(c * sizeof(float4)));
+    view.sh_d = reinterpret_cast<float4*>(take(c * sizeof(float4)));
+    view.sh_c = reinterpret_cast<float4*>(take(c * sizeof(float4)));
+    view.q[0] = reinterpret_cast<uint32_t*>(take(c * sizeof(uint32_t)));
+    view.q[1] = reinterpret_cast<uint32_t*>(take(c * sizeof(uint32_t)));
+    view.counters = reinterpret_cast<uint32_t*>(take(2ull * (b + 1) * sizeof(uint32_t)));
+    view.capacity = cap;
+    bounces = b;
+    return ATX_OK;
+}
+
+WavePlan plan_waves(uint64_t pixels, uint32_t spp, uint32_t capacity)
+{
+    WavePlan p;
+    // keep at least 256 pixels per wave so the first bounce fills the GPU
+    const uint32_t max_spp = std::max<uint32_t>(1, capacity / 256);
+    p.spp_per_wave = std::min(spp, max_spp);
+    uint64_t ppw = capacity / p.spp_per_wave;
+    if (ppw < 1) ppw = 1;
+    if (ppw > pixels) ppw = pixels;
+    p.pixels_per_wave = (uint32_t)ppw;
+    return p;
+}
+
+EventTimer::~EventTimer()
+{
+    for (auto& r : recs_) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (cudaEvent_t e : pool_) cudaEventDestroy(e);
+}
+
+cudaEvent_t EventTimer::take()
+{
+    if (!pool_.empty()) {
+        cudaEvent_t e = pool_.back();
+        pool_.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    return e;
+}
+
+void EventTimer::begin(int, cudaStream_t stream)
+{
+    open_ = take();
+    if (open_) cudaEventRecord(open_, stream);
+}
+
+void EventTimer::end(int family, cudaStream_t stream)
+{
+    if (!open_) return;
+    cudaEvent_t b = take();
+    if (!b) {
+        pool_.push_back(open_);
+        open_ = nullptr;
+        return;
+    }
+    cudaEventRecord(b, stream);
+    recs_.push_back(Rec{family, open_, b});
+    open_ = nullptr;
+}
+
+atx_status EventTimer::collect(atx_kernel_times* t)
+{
+    for (auto& r : recs_) {
+        ATX_CUDA(cudaEventSynchronize(r.b));
+        float ms = 0.0f;
+        ATX_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+        double* dst[4] = {&t->extend_ms, &t->shadow_ms, &t->accumulate_ms, &t->other_ms};
+        uint64_t* cnt[4] = {&t->extend_launches, &t->shadow_launches, &t->accumulate_launches, &t->other_launches};
+        *dst[r.family] += ms;
+        *cnt[r.family] += 1;
+        pool_.push_back(r.a);
+        pool_.push_back(r.b);
+    }
+    recs_.clear();
+    return ATX_OK;
+}
+
+atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore& ws, const LaunchShape& shape,
+                          uint32_t frame0, uint32_t spp, int32_t max_bounces, int32_t sky, float4* accum,
+                          uint32_t* image, uint32_t capacity, cudaStream_t stream, uint32_t* launches,
+                          KernelTimer* timer)
+{
+    const uint64_t pixels = (uint64_t)cam.width * cam.height;
+    const WavePlan plan = plan_waves(pixels, spp, capacity);
+    const uint32_t last_frame = frame0 + spp - 1;
+    for (uint64_t p0 = 0; p0 < pixels; p0 += plan.pixels_per_wave) {
+        const uint32_t np = (uint32_t)std::min<uint64_t>(plan.pixels_per_wave, pixels - p0);
+        for (uint32_t s0 = 0; s0 < spp; s0 += plan.spp_per_wave) {
+            WaveJob job;
+            job.pixel0 = (uint32_t)p0;
+            job.n_pixels = np;
+            job.spp = std::min(plan.spp_per_wave, spp - s0);
+            job.frame0 = frame0 + s0;
+            job.max_bounces = max_bounces;
+            job.sky = sky;
+            job.pack_frame = (s0 + job.spp >= spp && image) ? last_frame : 0u;
+            ATX_CUDA(enqueue_wave(sc, cam, ws.view, job, shape, accum, image, stream, launches, timer));
+        }
+    }
+    return ATX_OK;
+}
+
+// ---------------------------------------------------------------- renderer
+
+Renderer::Renderer(const atx_config& cfg) : cfg_(cfg), budget_(cfg.hbm_budget_bytes) {}
+
+Renderer::~Renderer()
+{
+    if (cudaSetDevice(cfg_.device) == cudaSuccess) {
+        if (stream_) cudaStreamSynchronize(stream_);
+        scene_ = SceneStore();
+        wave_.buf.reset();
+        accum_.reset();
+        image_.reset();
+        totals_.reset();
+        if (ev_start_) cudaEventDestroy(ev_start_);
+        if (ev_stop_) cudaEventDestroy(ev_stop_);
+        if (stream_) cudaStreamDestroy(stream_);
+    }
+}
+
+atx_status Renderer::activate() const
+{
+    ATX_CUDA(cudaSetDevice(cfg_.device));
+    return ATX_OK;
+}
+
+atx_status Renderer::init()
+{
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        (void)cudaGetLastError();
+        return fail(ATX_ERR_NO_DEVICE, "no CUDA device visible (%s)", cudaGetErrorString(e));
+    }
+    if (cfg_.device < 0 || cfg_.device >= count)
+        return fail(ATX_ERR_INVALID_ARG, "device %d out of range (%d visible)", cfg_.device, count);
+    ATX_TRY(activate());
+    ATX_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    ATX_CUDA(cudaEventCreate(&ev_start_));
+    ATX_CUDA(cudaEventCreate(&ev_stop_));
+    ATX_TRY(totals_.ensure(2 * sizeof(unsigned long long), &budget_, "ray totals"));
+    ATX_CUDA(cudaMemsetAsync(totals_.get(), 0, 2 * sizeof(unsigned long long), stream_));
+    scene_.bvh_threshold = cfg_.bvh_threshold;
+    scene_.bvh_leaf = cfg_.bvh_leaf_size;
+    // empty scene until set_scene
+    ATX_TRY(scene_.upload(nullptr, 0, nullptr, 0, nullptr, 0, &budget_, stream_));
+    return ATX_OK;
+}
+
+atx_status Renderer::resize(uint32_t w, uint32_t h)
+{
+    if (w == 0 || h == 0) return fail(ATX_ERR_INVALID_ARG, "resize: width and height must be non-zero");
+    if ((uint64_t)w * h > 0xffffffffull) return fail(ATX_ERR_INVALID_ARG, "resize: more than 2^32 pixels");
+    if (w == width_ && h == height_ && accum_.get()) return ATX_OK;  // Renderer.cu:100-101
+    ATX_TRY(activate());
+    ATX_CUDA(cudaStreamSynchronize(stream_));
+    const uint64_t px = (uint64_t)w * h;
+    accum_.reset();
+    image_.reset();
+    ATX_TRY(accum_.ensure(px * sizeof(float4), &budget_, "accumulation buffer"));
+    ATX_TRY(image_.ensure(px * sizeof(uint32_t), &budget_, "image buffer"));
+    width_ = w;
+    height_ = h;
+    frame_ = 1;  // Renderer.cu:145
+    cam_dirty_ = true;
+    return ATX_OK;
+}
+
+atx_status Renderer::set_scene(const atx_sphere* s, uint32_t n, const atx_material* m, uint32_t nm,
+                               const atx_light* l, uint32_t nl)
+{
+    ATX_TRY(activate());
+    ATX_CUDA(cudaStreamSynchronize(stream_));
+    shape_valid_ = false;
+    return scene_.upload(s, n, m, nm, l, nl, &budget_, stream_);
+}
+
+atx_status Renderer::set_settings(const atx_settings& s)
+{
+    if (s.max_bounces > (int32_t)kMaxBounces)
+        return fail(ATX_ERR_INVALID_ARG, "max_bounces %d above the supported %u", s.max_bounces, kMaxBounces);
+    settings_ = s;
+    return ATX_OK;
+}
+
+atx_status Renderer::set_camera(const atx_camera& c)
+{
+    cam_desc_ = c;
+    cam_from_desc_ = true;
+    cam_dirty_ = true;
+    return ATX_OK;
+}
+
+atx_status Renderer::set_camera_matrices(const float inv_view[16], const float inv_proj[16], const float pos[3])
+{
+    std::memcpy(camv_.inv_view, inv_view, sizeof(camv_.inv_view));
+    std::memcpy(camv_.inv_proj, inv_proj, sizeof(camv_.inv_proj));
+    std::memcpy(camv_.pos, pos, sizeof(camv_.pos));
+    cam_from_desc_ = false;
+    cam_dirty_ = false;
+    return ATX_OK;
+}
+
+atx_status Renderer::refresh_camera()
+{
+    camv_.width = width_;
+    camv_.height = height_;
+    if (cam_from_desc_ && (cam_dirty_ || cam_w_ != width_ || cam_h_ != height_)) {
+        camera_matrices(cam_desc_, width_, height_, nullptr, camv_.inv_view, nullptr, camv_.inv_proj);
+        std::memcpy(camv_.pos, cam_desc_.position, sizeof(camv_.pos));
+        cam_w_ = width_;
+        cam_h_ = height_;
+        cam_dirty_ = false;
+    }
+    return ATX_OK;
+}
+
+atx_status Renderer::ensure_shape()
+{
+    if (shape_valid_) return ATX_OK;
+    ATX_CUDA(plan_launch(scene_.view, cfg_.device, (int)cfg_.threads, &shape_));
+    shape_valid_ = true;
+    return ATX_OK;
+}
+
+atx_status Renderer::render(uint32_t spp)
+{
+    if (!width_ || !height_ || !accum_.get()) return fail(ATX_ERR_INVALID_ARG, "render: call atx_resize first");
+    if (spp == 0) return ATX_OK;
+    ATX_TRY(activate());
+    ATX_TRY(refresh_camera());
+    ATX_TRY(ensure_shape());
+    const uint32_t capacity = cfg_.wave_paths ? cfg_.wave_paths : kDefaultWavePaths;
+    const int32_t bounces = settings_.max_bounces;
+    ATX_TRY(wave_.ensure(capacity, bounces > 0 ? (uint32_t)bounces : 0u, &budget_));
+    wave_.view.totals = totals_.as<unsigned long long>();
+
+    if (!settings_.accumulation) frame_ = 1;
+    const uint32_t f0 = frame_;
+    uint32_t launches = 0;
+    KernelTimer* timer = (cfg_.flags & ATX_FLAG_PROFILE_KERNELS) ? &timer_ : nullptr;
+    ATX_CUDA(cudaEventRecord(ev_start_, stream_));
+    if (f0 == 1) {  // Renderer.cu:181-182
+        if (timer) timer->begin(kFamOther, stream_);
+        ATX_CUDA(enqueue_clear_accum(accum_.as<float4>(), (uint64_t)width_ * height_, stream_));
+        if (timer) timer->end(kFamOther, stream_);
+        ++launches;
+    }
+    ATX_TRY(enqueue_frames(scene_.view, camv_, wave_, shape_, f0, spp, bounces, settings_.sky_light ? 1 : 0,
+                           accum_.as<float4>(), image_.as<uint32_t>(), capacity, stream_, &launches, timer));
+    ATX_CUDA(cudaEventRecord(ev_stop_, stream_));
+    timed_ = true;
+    frame_ = settings_.accumulation ? f0 + spp : 1u;  // Renderer.cu:245-248
+    st_.frames += spp;
+    st_.paths += (uint64_t)width_ * height_ * spp;
+    st_.kernel_launches += launches;
+    if (bounces > 0) totals_host_[0] += (uint64_t)width_ * height_ * spp;  // bounce-0 rays
+    return ATX_OK;
+}
+
+atx_status Renderer::synchronize()
+{
+    ATX_TRY(activate());
+    ATX_CUDA(cudaStreamSynchronize(stream_));
+    return ATX_OK;
+}
+
+atx_status Renderer::read_accumulation(float* host, uint64_t n)
+{
+    if (!host) return fail(ATX_ERR_INVALID_ARG, "read_accumulation: null buffer");
+    if (n > (uint64_t)width_ * height_) return fail(ATX_ERR_INVALID_ARG, "read_accumulation: %llu pixels > image",
+                                                    (unsigned long long)n);
+    ATX_TRY(activate());
+    ATX_CUDA(cudaMemcpyAsync(host, accum_.get(), n * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
+    ATX_CUDA(cudaStreamSynchronize(stream_));
+    return ATX_OK;
+}
+
+atx_status Renderer::read_image(uint32_t* host, uint64_t n)
+{
+    if (!host) return fail(ATX_ERR_INVALID_ARG, "read_image: null buffer");
+    if (n > (uint64_t)width_ * height_) return fail(ATX_ERR_INVALID_ARG, "read_image: %llu pixels > image",
+                                                    (unsigned long long)n);
+    ATX_TRY(activate());
+    ATX_CUDA(cudaMemcpyAsync(host, image_.get(), n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+    ATX_CUDA(cudaStreamSynchronize(stream_));
+    return ATX_OK;
+}
+
+atx_status Renderer::device_buffers(void** accum, void** image)
+{
+    if (accum) *accum = accum_.get();
+    if (image) *image = image_.get();
+    return ATX_OK;
+}
+
+atx_status Renderer::stats(atx_stats* out)
+{
+    ATX_TRY(activate());
+    ATX_CUDA(cudaStreamSynchronize(stream_));
+    unsigned long long dev[2] = {0, 0};
+    ATX_CUDA(cudaMemcpy(dev, totals_.get(), sizeof(dev), cudaMemcpyDeviceToHost));
+    if (timed_) {
+        float ms = 0.0f;
+        ATX_CUDA(cudaEventElapsedTime(&ms, ev_start_, ev_stop_));
+        st_.last_render_ms = ms;
+    }
+    *out = st_;
+    out->extension_rays = totals_host_[0] + dev[0];
+    out->shadow_rays = dev[1];
+    out->device_bytes = budget_.used();
+    out->bvh_in_use = scene_.view.use_bvh;
+    return ATX_OK;
+}
+
+atx_status Renderer::kernel_times(atx_kernel_times* out)
+{
+    ATX_TRY(activate());
+    ATX_TRY(timer_.collect(&ktimes_));
+    *out = ktimes_;
+    return ATX_OK;
+}
+
+atx_status Renderer::trace_nearest(const float* o, const float* d, uint64_t n, float* t, int32_t* id)
+{
+    if (n == 0) return ATX_OK;
+    if (!o || !d || !t || !id) return fail(ATX_ERR_INVALID_ARG, "trace_nearest: null array");
+    ATX_TRY(activate());
+    DeviceBuffer buf;
+    ATX_TRY(buf.ensure(n * 8 * sizeof(float) + 1024, &budget_, "trace scratch"));
+    float* dorg = buf.as<float>();
+    float* ddir = dorg + 3 * n;
+    float* dt = ddir + 3 * n;
+    int32_t* did = reinterpret_cast<int32_t*>(dt + n);
+    ATX_CUDA(cudaMemcpyAsync(dorg, o, 3 * n * sizeof(float), cudaMemcpyHostToDevice, stream_));
+    ATX_CUDA(cudaMemcpyAsync(ddir, d, 3 * n * sizeof(float), cudaMemcpyHostToDevice, stream_));
+    ATX_CUDA(enqueue_trace_nearest(scene_.view, dorg, ddir, n, dt, did, stream_));
+    ATX_CUDA(cudaMemcpyAsync(t, dt, n * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+    ATX_CUDA(cudaMemcpyAsync(id, did, n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
+    ATX_CUDA(cudaStreamSynchronize(stream_));
+    return ATX_OK;
+}
+
+atx_status Renderer::primary_directions(float* host, uint64_t n)
+{
+    if (!width_ || !height_) return fail(ATX_ERR_INVALID_ARG, "primary_directions: call atx_resize first");
+    const uint64_t px = (uint64_t)width_ * height_;
+    if (!host || n < px) return fail(ATX_ERR_INVALID_ARG, "primary_directions: buffer smaller than W*H");
+    ATX_TRY(activate());
+    ATX_TRY(refresh_camera());
+    DeviceBuffer buf;
+    ATX_TRY(buf.ensure(px * 3 * sizeof(float), &budget_, "direction scratch"));
+    ATX_CUDA(enqueue_primary_dirs(camv_, buf.as<float>(), stream_));
+    ATX_CUDA(cudaMemcpyAsync(host, buf.get(), px * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+    ATX_CUDA(cudaStreamSynchronize(stream_));
+    return ATX_OK;
+}
+
+}  // namespace atx

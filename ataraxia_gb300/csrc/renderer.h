@@ -1,0 +1,133 @@
+// Host orchestration of one progressive render target: the GB300 counterpart
+// of the reference's Renderer (Engine/include/Renderer.h, Renderer.cu:13-249).
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "atx.h"
+#include "host_common.h"
+#include "wavefront.h"
+
+namespace atx {
+
+// Device-resident scene: sphere table (float4 centre + radius^2), clamped
+// material ids, radii (for BVH boxes), shading tables and the optional LBVH.
+struct SceneStore {
+    DeviceBuffer sph, sph_mat, sph_rad, mat, lights, bvh;
+    SceneView view{};
+    uint32_t bvh_threshold = 0;
+    uint32_t bvh_leaf = 0;
+
+    // Validates, converts and uploads on stream (Renderer.cu:25-57).
+    atx_status upload(const atx_sphere* s, uint32_t n, const atx_material* m, uint32_t nm, const atx_light* l,
+                      uint32_t nl, Budget* budget, cudaStream_t stream);
+    uint64_t device_bytes() const
+    {
+        return sph.bytes() + sph_mat.bytes() + sph_rad.bytes() + mat.bytes() + lights.bytes() + bvh.bytes();
+    }
+};
+
+// Path state for up to `capacity` paths (wavefront.h WaveState) in one block.
+struct WaveStore {
+    DeviceBuffer buf;
+    WaveState view{};
+    uint32_t bounces = 0;
+    atx_status ensure(uint32_t capacity, uint32_t max_bounces, Budget* budget);
+    static uint64_t bytes_for(uint32_t capacity, uint32_t max_bounces);
+};
+
+// Splits pixels x samples into waves of at most `capacity` paths: pixel-major
+// ranges, each covering a chunk of consecutive samples; chunks of one pixel
+// range are issued in frame order so the accumulator adds frames in order.
+struct WavePlan {
+    uint32_t pixels_per_wave;
+    uint32_t spp_per_wave;
+};
+WavePlan plan_waves(uint64_t pixels, uint32_t spp, uint32_t capacity);
+
+// Enqueues frames [frame0, frame0 + spp) for all pixels of the view.
+atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore& ws, const LaunchShape& shape,
+                          uint32_t frame0, uint32_t spp, int32_t max_bounces, int32_t sky, float4* accum,
+                          uint32_t* image, uint32_t capacity, cudaStream_t stream, uint32_t* launches,
+                          KernelTimer* timer = nullptr);
+
+// Records a pair of CUDA events around each kernel and sums their durations
+// per kernel family when collected.
+class EventTimer : public KernelTimer {
+public:
+    ~EventTimer() override;
+    void begin(int family, cudaStream_t stream) override;
+    void end(int family, cudaStream_t stream) override;
+    // Synchronises the recorded events and adds their durations to times.
+    atx_status collect(atx_kernel_times* times);
+
+private:
+    cudaEvent_t take();
+    struct Rec { int family; cudaEvent_t a, b; };
+    std::vector<Rec> recs_;
+    std::vector<cudaEvent_t> pool_;
+    cudaEvent_t open_ = nullptr;
+};
+
+class Renderer {
+public:
+    explicit Renderer(const atx_config& cfg);
+    ~Renderer();
+    atx_status init();
+
+    atx_status resize(uint32_t w, uint32_t h);
+    atx_status set_scene(const atx_sphere* s, uint32_t n, const atx_material* m, uint32_t nm, const atx_light* l,
+                         uint32_t nl);
+    atx_status set_settings(const atx_settings& s);
+    atx_settings settings() const { return settings_; }
+    void reset_frame_index() { frame_ = 1; }
+    uint32_t frame_index() const { return frame_; }
+    atx_status set_camera(const atx_camera& c);
+    atx_status set_camera_matrices(const float inv_view[16], const float inv_proj[16], const float pos[3]);
+    atx_status render(uint32_t spp);
+    atx_status synchronize();
+    atx_status read_accumulation(float* host, uint64_t n);
+    atx_status read_image(uint32_t* host, uint64_t n);
+    atx_status device_buffers(void** accum, void** image);
+    atx_status stats(atx_stats* out);
+    atx_status trace_nearest(const float* o, const float* d, uint64_t n, float* t, int32_t* id);
+    atx_status primary_directions(float* host, uint64_t n);
+    atx_status kernel_times(atx_kernel_times* out);
+    void reset_kernel_times() { ktimes_ = atx_kernel_times{}; }
+    cudaStream_t stream() const { return stream_; }
+
+private:
+    atx_status activate() const;
+    atx_status refresh_camera();
+    atx_status ensure_shape();
+
+    atx_config cfg_;
+    Budget budget_;
+    cudaStream_t stream_ = nullptr;
+    cudaEvent_t ev_start_ = nullptr, ev_stop_ = nullptr;
+    bool timed_ = false;
+
+    uint32_t width_ = 0, height_ = 0;
+    uint32_t frame_ = 1;
+    atx_settings settings_{1, 0, {0, 0}, 15};
+
+    bool cam_from_desc_ = true;
+    atx_camera cam_desc_{{0.0f, 0.0f, 3.0f}, {0.0f, 0.0f, -1.0f}, 45.0f, 0.1f, 100.0f};
+    CameraView camv_{};
+    uint32_t cam_w_ = 0, cam_h_ = 0;
+    bool cam_dirty_ = true;
+
+    SceneStore scene_;
+    WaveStore wave_;
+    DeviceBuffer accum_, image_, totals_;
+    LaunchShape shape_{};
+    bool shape_valid_ = false;
+
+    atx_stats st_{};
+    uint64_t totals_host_[2] = {0, 0};
+    EventTimer timer_;
+    atx_kernel_times ktimes_{};
+};
+
+}  // namespace atx

@@ -1,0 +1,483 @@
+// Wavefront path tracer for sm_103a: the reference's per-pixel loop
+// (Renderer.cu:287-387) split into queue-driven stages.
+//
+//   k_extend<FIRST>  bounce b: (FIRST: generate the primary ray, Camera.cpp:
+//                    161-195) nearest hit over the sphere table staged in
+//                    shared memory, shading, light pick and the shadow ray,
+//                    Russian roulette and the next direction.  Survivors go to
+//                    the next extension queue, shadow rays to the shadow
+//                    queue, both through warp-aggregated atomics.
+//   k_shadow         any-hit over the shadow queue of bounce b; unoccluded
+//                    rays add their contribution to the path colour.
+//   k_accumulate     adds the wave's per-sample colours to the float4
+//                    accumulator in frame order (Renderer.cu:165) and packs
+//                    the RGBA8 image (Renderer.cu:166-168).
+//
+// Order of the colour sums is the reference's: emission of bounce b (extend b),
+// light of bounce b (shadow b), then bounce b+1.  Each path owns its colour
+// row, so no float atomics are needed and results do not depend on queue
+// order.  The random stream is consumed per path exactly as the reference
+// does: seed += b at the top of the bounce, PcgHash(seed) (no advance) for the
+// light, one PcgFloat for roulette and two for the new direction.
+#include "wavefront.h"
+#include "device_math.cuh"
+#include "bvh_traverse.cuh"
+
+namespace atx {
+namespace {
+
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// One atomicAdd per warp; pushing lanes receive consecutive slots in lane order.
+// Must be reached by all 32 lanes of the warp.
+__device__ __forceinline__ uint32_t warp_push(uint32_t* counter, bool pred)
+{
+    const unsigned mask = __ballot_sync(kFull, pred);
+    if (mask == 0u) return 0u;
+    const uint32_t lane = lane_id();
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0u;
+    if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(kFull, base, leader);
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+// Camera.cpp:173-187 for pixel (x, y): NDC without a pixel-centre offset, y = 0
+// the bottom row; target = invProj * (cx, cy, 1, 1); direction =
+// normalize(invView * (normalize(target.xyz / target.w), 0)).
+__device__ __forceinline__ float3 primary_dir(const CameraView& cam, uint32_t x, uint32_t y)
+{
+    const float qx = __uint2float_rn(x) / __uint2float_rn(cam.width);
+    const float qy = __uint2float_rn(y) / __uint2float_rn(cam.height);
+    const float cx = qx * 2.0f - 1.0f;
+    const float cy = qy * 2.0f - 1.0f;
+    float t[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+        t[r] = (cam.inv_proj[r] * cx + cam.inv_proj[4 + r] * cy) + (cam.inv_proj[8 + r] + cam.inv_proj[12 + r]);
+    const float3 tv = normalize3(mk3(t[0] / t[3], t[1] / t[3], t[2] / t[3]));
+    float dv[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+        dv[r] = (cam.inv_view[r] * tv.x + cam.inv_view[4 + r] * tv.y) + cam.inv_view[8 + r] * tv.z;
+    return normalize3(mk3(dv[0], dv[1], dv[2]));
+}
+
+// Renderer.cu:256-279: brute-force nearest hit, lowest index on equal t.
+template <bool SMEM>
+__device__ __forceinline__ int32_t nearest_brute(const float4* __restrict__ sph, uint32_t n, float3 o, float3 d,
+                                                 float& tmin)
+{
+    const float a = dot3(d, d);
+    int32_t best = -1;
+    float tm = kFltMax;
+#pragma unroll 4
+    for (uint32_t i = 0; i < n; ++i) {
+        const float4 s = SMEM ? sph[i] : __ldg(&sph[i]);
+        float t;
+        if (sphere_t(s, o, d, a, t) && t > 0.0f && t < tm) {
+            tm = t;
+            best = (int32_t)i;
+        }
+    }
+    tmin = tm;
+    return best;
+}
+
+// Renderer.cu:351-352 as an any-hit query.  The reference takes the nearest
+// hit and tests t > 0 && t*t < dist2; since the nearest accepted t is <= every
+// accepted t and squaring is monotone, that equals "some sphere has t > 0 and
+// t*t < dist2", so the loop can stop at the first such sphere.
+template <bool SMEM>
+__device__ __forceinline__ bool occluded_brute(const float4* __restrict__ sph, uint32_t n, float3 o, float3 d,
+                                               float dist2)
+{
+    const float a = dot3(d, d);
+#pragma unroll 4
+    for (uint32_t i = 0; i < n; ++i) {
+        const float4 s = SMEM ? sph[i] : __ldg(&sph[i]);
+        float t;
+        if (sphere_t(s, o, d, a, t) && t > 0.0f && t * t < dist2) return true;
+    }
+    return false;
+}
+
+template <bool SMEM>
+__device__ __forceinline__ int32_t scene_nearest(const SceneView& sc, const float4* sph, float3 o, float3 d,
+                                                 float& tmin)
+{
+    if (sc.use_bvh) return bvh_nearest(sc, o, d, tmin);
+    return nearest_brute<SMEM>(sph, sc.n_sph, o, d, tmin);
+}
+
+template <bool SMEM>
+__device__ __forceinline__ bool scene_occluded(const SceneView& sc, const float4* sph, float3 o, float3 d,
+                                               float dist2)
+{
+    if (sc.use_bvh) return bvh_occluded(sc, o, d, dist2);
+    return occluded_brute<SMEM>(sph, sc.n_sph, o, d, dist2);
+}
+
+__device__ __forceinline__ void stage_spheres(const SceneView& sc, float4* s_sph)
+{
+    for (uint32_t i = threadIdx.x; i < sc.n_sph; i += blockDim.x) s_sph[i] = __ldg(&sc.sph[i]);
+    __syncthreads();
+}
+
+template <bool FIRST, bool SMEM>
+__global__ void __launch_bounds__(kThreads) k_extend(SceneView sc, CameraView cam, WaveState ws, WaveJob job,
+                                                     int bounce)
+{
+    extern __shared__ float4 s_sph[];
+    const uint32_t n = FIRST ? job.n_pixels * job.spp : ws.counters[2 * bounce];
+    if (blockIdx.x * blockDim.x >= n) return;
+    if (SMEM) stage_spheres(sc, s_sph);
+    const float4* sph = SMEM ? s_sph : sc.sph;
+
+    const uint32_t* qin = ws.q[bounce & 1];
+    uint32_t* qout = ws.q[(bounce + 1) & 1];
+    const bool last = bounce + 1 >= job.max_bounces;
+    const uint32_t stride = gridDim.x * blockDim.x;
+
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t idx = base + threadIdx.x;
+        bool push_next = false, push_sh = false;
+        uint32_t pid = 0u, seed = 0u;
+        float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o;
+        float4 sho = make_float4(0.f, 0.f, 0.f, 0.f), shd = sho, shc = sho;
+
+        if (idx < n) {
+            if (FIRST) {
+                pid = idx;
+                const uint32_t p = job.pixel0 + idx / job.spp;
+                const uint32_t s = idx % job.spp;
+                o = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
+                d = primary_dir(cam, p % cam.width, p / cam.width);
+                thr = mk3(1.f, 1.f, 1.f);
+                seed = p * (job.frame0 + s);
+            } else {
+                pid = qin[idx];
+                const float4 ro = ws.ray_o[pid];
+                const float4 rd = ws.ray_d[pid];
+                const float4 tt = ws.thr[pid];
+                o = mk3(ro.x, ro.y, ro.z);
+                seed = __float_as_uint(ro.w);
+                d = mk3(rd.x, rd.y, rd.z);
+                thr = mk3(tt.x, tt.y, tt.z);
+            }
+            seed += (uint32_t)bounce;
+
+            float tmin;
+            const int32_t hit = scene_nearest<SMEM>(sc, sph, o, d, tmin);
+            bool touch = false;
+            float3 add = mk3(0.f, 0.f, 0.f);
+            if (hit < 0) {
+                if (job.sky) {  // Renderer.cu:311-316
+                    add = mul3(mk3(0.6f, 0.7f, 0.9f), thr);
+                    touch = true;
+                }
+            } else {
+                const float4 s = SMEM ? sph[hit] : __ldg(&sc.sph[hit]);
+                float3 pos, nrm;
+                ray_hit(s, o, d, tmin, pos, nrm);
+                const int32_t mi = __ldg(&sc.sph_mat[hit]);
+                const float4* mrow = reinterpret_cast<const float4*>(sc.mat + mi);
+                const float4 m0 = __ldg(mrow), m1 = __ldg(mrow + 1), m2 = __ldg(mrow + 2);
+                const float3 albedo = mk3(m0.x, m0.y, m0.z);
+                const float rough = m0.w;
+                const float3 f0 = mk3(m1.x, m1.y, m1.z);
+                const float metallic = m1.w;
+
+                if (m2.w > 0.0f) {  // Renderer.cu:329-333
+                    add = mul3(mk3(m2.x, m2.y, m2.z), thr);
+                    touch = true;
+                }
+                // glm::mix(F0, albedo, metallic), Renderer.cu:335
+                const float3 base = add3(muls3(f0, 1.0f - metallic), muls3(albedo, metallic));
+
+                if (sc.n_lights > 0u) {  // Renderer.cu:338-369
+                    const uint32_t li = pcg_hash(seed) % sc.n_lights;
+                    const float4* lrow = reinterpret_cast<const float4*>(sc.lights + li);
+                    const float4 l0 = __ldg(lrow), l1 = __ldg(lrow + 1);
+                    float3 L = sub3(mk3(l0.x, l0.y, l0.z), pos);
+                    const float dist2 = dot3(L, L);
+                    L = muls3(L, 1.0f / sqrtf(dist2));
+                    const float3 so = add3(pos, muls3(nrm, kOffset));
+                    const float3 f = cook_torrance(albedo, base, metallic, rough, nrm, neg3(d), L);
+                    const float3 c = mul3(mul3(mk3(l1.x, l1.y, l1.z), f), thr);
+                    sho = make_float4(so.x, so.y, so.z, dist2);
+                    shd = make_float4(L.x, L.y, L.z, __uint_as_float(pid));
+                    shc = make_float4(c.x, c.y, c.z, 0.0f);
+                    push_sh = true;
+                }
+
+                if (!last) {  // Renderer.cu:371-384
+                    thr = mul3(thr, albedo);
+                    o = add3(pos, muls3(nrm, kOffset));
+                    const float p = gmax(0.1f, gmin(1.0f, length3(thr)));
+                    if (!(pcg_float(seed) > p)) {
+                        thr = divs3(thr, p);
+                        d = (metallic > 0.0f) ? sample_ggx(nrm, rough, seed) : sample_cosine(nrm, seed);
+                        push_next = true;
+                    }
+                }
+            }
+            if (FIRST) {
+                const float3 c = add3(mk3(0.f, 0.f, 0.f), add);
+                ws.col[pid] = make_float4(c.x, c.y, c.z, 0.0f);
+            } else if (touch) {
+                float4 c = ws.col[pid];
+                c.x = c.x + add.x;
+                c.y = c.y + add.y;
+                c.z = c.z + add.z;
+                ws.col[pid] = c;
+            }
+        }
+
+        const uint32_t ss = warp_push(&ws.counters[2 * bounce + 1], push_sh);
+        if (push_sh) {
+            ws.sh_o[ss] = sho;
+            ws.sh_d[ss] = shd;
+            ws.sh_c[ss] = shc;
+        }
+        const uint32_t sn = warp_push(&ws.counters[2 * (bounce + 1)], push_next);
+        if (push_next) {
+            qout[sn] = pid;
+            ws.ray_o[pid] = make_float4(o.x, o.y, o.z, __uint_as_float(seed));
+            ws.ray_d[pid] = make_float4(d.x, d.y, d.z, 0.0f);
+            ws.thr[pid] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+        }
+    }
+}
+
+template <bool SMEM>
+__global__ void __launch_bounds__(kThreads) k_shadow(SceneView sc, WaveState ws, int bounce)
+{
+    extern __shared__ float4 s_sph[];
+    const uint32_t n = ws.counters[2 * bounce + 1];
+    if (blockIdx.x * blockDim.x >= n) return;
+    if (SMEM) stage_spheres(sc, s_sph);
+    const float4* sph = SMEM ? s_sph : sc.sph;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += stride) {
+        const float4 so = ws.sh_o[idx];
+        const float4 sd = ws.sh_d[idx];
+        if (!scene_occluded<SMEM>(sc, sph, mk3(so.x, so.y, so.z), mk3(sd.x, sd.y, sd.z), so.w)) {
+            const float4 c = ws.sh_c[idx];
+            const uint32_t pid = __float_as_uint(sd.w);
+            float4 col = ws.col[pid];
+            col.x = col.x + c.x;
+            col.y = col.y + c.y;
+            col.z = col.z + c.z;
+            ws.col[pid] = col;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_accumulate(WaveState ws, WaveJob job, float4* accum, uint32_t* image)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const float fpack = __uint2float_rn(job.pack_frame);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && ws.totals) {
+        unsigned long long ext = 0, sh = 0;
+        for (int b = 0; b < job.max_bounces; ++b) {
+            if (b > 0) ext += ws.counters[2 * b];
+            sh += ws.counters[2 * b + 1];
+        }
+        atomicAdd(&ws.totals[0], ext);
+        atomicAdd(&ws.totals[1], sh);
+    }
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < job.n_pixels; j += stride) {
+        const uint32_t p = job.pixel0 + j;
+        float4 a = accum[p];
+        for (uint32_t s = 0; s < job.spp; ++s) {
+            float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (job.max_bounces > 0) c = ws.col[(uint64_t)j * job.spp + s];
+            a.x = a.x + c.x;
+            a.y = a.y + c.y;
+            a.z = a.z + c.z;
+            a.w = a.w + 1.0f;
+        }
+        accum[p] = a;
+        if (job.pack_frame) image[p] = pack_rgba8(a, fpack);
+    }
+}
+
+__global__ void k_clear(float4* p, uint64_t n)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+template <bool SMEM>
+__global__ void __launch_bounds__(kThreads) k_trace(SceneView sc, const float* __restrict__ org,
+                                                    const float* __restrict__ dir, uint64_t n, float* t_out,
+                                                    int32_t* id_out)
+{
+    extern __shared__ float4 s_sph[];
+    if (SMEM) stage_spheres(sc, s_sph);
+    const float4* sph = SMEM ? s_sph : sc.sph;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float3 o = mk3(org[3 * i], org[3 * i + 1], org[3 * i + 2]);
+        const float3 d = mk3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
+        float t;
+        const int32_t id = scene_nearest<SMEM>(sc, sph, o, d, t);
+        t_out[i] = id < 0 ? -1.0f : t;
+        id_out[i] = id;
+    }
+}
+
+__global__ void k_primary_dirs(CameraView cam, float* out)
+{
+    const uint64_t n = (uint64_t)cam.width * cam.height;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float3 d = primary_dir(cam, (uint32_t)(i % cam.width), (uint32_t)(i / cam.width));
+        out[3 * i] = d.x;
+        out[3 * i + 1] = d.y;
+        out[3 * i + 2] = d.z;
+    }
+}
+
+constexpr size_t kSmemSphereCap = 96 * 1024;  // 6144 spheres staged per CTA
+
+bool use_smem(const SceneView& sc)
+{
+    return !sc.use_bvh && (size_t)sc.n_sph * sizeof(float4) <= kSmemSphereCap && sc.n_sph > 0;
+}
+
+int grid_for(uint64_t n, int threads, int cap)
+{
+    uint64_t b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    return (int)(b < (uint64_t)cap ? b : (uint64_t)cap);
+}
+
+}  // namespace
+
+cudaError_t plan_launch(const SceneView& sc, int device, int threads, LaunchShape* out)
+{
+    if (threads <= 0) threads = kThreads;
+    if (threads > kThreads) threads = kThreads;
+    cudaDeviceProp prop;
+    cudaError_t e = cudaGetDeviceProperties(&prop, device);
+    if (e != cudaSuccess) return e;
+    const bool smem = use_smem(sc);
+    const size_t bytes = smem ? (size_t)sc.n_sph * sizeof(float4) : 0;
+    int per_sm_ext = 0, per_sm_sh = 0;
+    if (smem) {
+        if (bytes > 48 * 1024) {
+            e = cudaFuncSetAttribute(k_extend<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_extend<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_shadow<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_trace<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            if (e != cudaSuccess) return e;
+        }
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, true>, threads, bytes);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<true>, threads, bytes);
+    } else {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, false>, threads, 0);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<false>, threads, 0);
+    }
+    if (e != cudaSuccess) return e;
+    if (per_sm_ext < 1) per_sm_ext = 1;
+    if (per_sm_sh < 1) per_sm_sh = 1;
+    out->threads = threads;
+    out->blocks_extend = prop.multiProcessorCount * per_sm_ext;
+    out->blocks_shadow = prop.multiProcessorCount * per_sm_sh;
+    out->smem_spheres = bytes;
+    return cudaSuccess;
+}
+
+cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveState& ws, const WaveJob& job,
+                         const LaunchShape& shape, float4* accum, uint32_t* image, cudaStream_t stream,
+                         uint32_t* launches, KernelTimer* timer)
+{
+    uint32_t nl = 0;
+    const bool smem = shape.smem_spheres > 0;
+    const size_t sm = shape.smem_spheres;
+    const int bounces = job.max_bounces;
+    const uint64_t paths = (uint64_t)job.n_pixels * job.spp;
+    auto begin = [&](int fam) { if (timer) timer->begin(fam, stream); };
+    auto end = [&](int fam) { if (timer) timer->end(fam, stream); };
+    if (bounces > 0) {
+        cudaError_t e = cudaMemsetAsync(ws.counters, 0, sizeof(uint32_t) * 2 * ((size_t)bounces + 1), stream);
+        if (e != cudaSuccess) return e;
+        const int g0 = grid_for(paths, shape.threads, shape.blocks_extend);
+        begin(kFamExtend);
+        if (smem)
+            k_extend<true, true><<<g0, shape.threads, sm, stream>>>(sc, cam, ws, job, 0);
+        else
+            k_extend<true, false><<<g0, shape.threads, 0, stream>>>(sc, cam, ws, job, 0);
+        end(kFamExtend);
+        ++nl;
+        for (int b = 0; b < bounces; ++b) {
+            if (b > 0) {
+                begin(kFamExtend);
+                if (smem)
+                    k_extend<false, true><<<shape.blocks_extend, shape.threads, sm, stream>>>(sc, cam, ws, job, b);
+                else
+                    k_extend<false, false><<<shape.blocks_extend, shape.threads, 0, stream>>>(sc, cam, ws, job, b);
+                end(kFamExtend);
+                ++nl;
+            }
+            begin(kFamShadow);
+            if (smem)
+                k_shadow<true><<<shape.blocks_shadow, shape.threads, sm, stream>>>(sc, ws, b);
+            else
+                k_shadow<false><<<shape.blocks_shadow, shape.threads, 0, stream>>>(sc, ws, b);
+            end(kFamShadow);
+            ++nl;
+        }
+    }
+    begin(kFamAccumulate);
+    k_accumulate<<<grid_for(job.n_pixels, kThreads, 4096), kThreads, 0, stream>>>(ws, job, accum, image);
+    end(kFamAccumulate);
+    ++nl;
+    if (launches) *launches += nl;
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_clear_accum(float4* accum, uint64_t n, cudaStream_t stream)
+{
+    k_clear<<<grid_for(n, kThreads, 4096), kThreads, 0, stream>>>(accum, n);
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_trace_nearest(const SceneView& sc, const float* origins, const float* dirs, uint64_t n,
+                                  float* t_out, int32_t* id_out, cudaStream_t stream)
+{
+    if (n == 0) return cudaSuccess;
+    const int g = grid_for(n, kThreads, 4096);
+    if (use_smem(sc)) {
+        const size_t bytes = (size_t)sc.n_sph * sizeof(float4);
+        if (bytes > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(k_trace<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            if (e != cudaSuccess) return e;
+        }
+        k_trace<true><<<g, kThreads, bytes, stream>>>(sc, origins, dirs, n, t_out, id_out);
+    } else {
+        k_trace<false><<<g, kThreads, 0, stream>>>(sc, origins, dirs, n, t_out, id_out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_primary_dirs(const CameraView& cam, float* out, cudaStream_t stream)
+{
+    const uint64_t n = (uint64_t)cam.width * cam.height;
+    if (n == 0) return cudaSuccess;
+    k_primary_dirs<<<grid_for(n, kThreads, 4096), kThreads, 0, stream>>>(cam, out);
+    return cudaGetLastError();
+}
+
+}  // namespace atx

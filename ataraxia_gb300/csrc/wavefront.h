@@ -1,0 +1,150 @@
+// Shared host/device layout of the wavefront renderer: scene tables in HBM,
+// per-wave path state and the launch entry points implemented in
+// wavefront.cu.  Plain structs only, so host C++ compiled by the system
+// compiler can include it.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace atx {
+
+// Material as the shading code reads it: three float4 rows.  emission holds
+// emissionColor * emissionIntensity (Scene.h:41, one IEEE product done on the
+// host, the same bits the reference's getEmission() gives).
+struct alignas(16) DevMaterial {
+    float albedo[3];
+    float roughness;
+    float f0[3];
+    float metallic;
+    float emission[3];
+    float emission_intensity;
+};
+static_assert(sizeof(DevMaterial) == 48, "DevMaterial is three float4 rows");
+
+// Point light: position and color * intensity (Renderer.cu:362, one product).
+struct alignas(16) DevLight {
+    float pos[3];
+    float pad0;
+    float le[3];
+    float pad1;
+};
+static_assert(sizeof(DevLight) == 32, "DevLight is two float4 rows");
+
+// Linear BVH over the spheres (built on the device by lbvh.cu, Karras' binary
+// radix tree over 30-bit Morton codes).  Nodes [0, n-1) are internal with
+// node 0 the root; node n-1+k is the leaf holding sorted sphere k.  Boxes are
+// stored as centre and half extent.  An internal node whose sorted range holds
+// at most leaf_size spheres is treated as a leaf and its range tested
+// directly.
+struct BvhView {
+    const float4* node_ctr;       // [2n-1] box centre xyz, w = bit-cast left child (internal nodes)
+    const float4* node_half;      // [2n-1] half extent xyz, w = bit-cast right child (internal nodes)
+    const uint2* node_range;      // [n-1] first, last sorted sphere under an internal node
+    const float4* leaf_sph;       // [n] spheres in Morton order (cx, cy, cz, r*r)
+    const uint32_t* leaf_id;      // [n] original sphere index of each sorted slot
+    uint32_t n_leaves;
+    uint32_t leaf_size;
+    uint32_t root;
+};
+
+// Scene tables, all in device memory.
+struct SceneView {
+    const float4* sph;        // (cx, cy, cz, radius*radius), n_sph entries
+    const int32_t* sph_mat;   // material index, already clamped to [0, n_mat)
+    const DevMaterial* mat;
+    const DevLight* lights;
+    uint32_t n_sph;
+    uint32_t n_mat;
+    uint32_t n_lights;
+    uint32_t use_bvh;         // 1: traverse bvh instead of the brute-force loop
+    BvhView bvh;
+};
+
+// Camera as the ray generator needs it (Camera.cpp:161-195): column-major
+// inverse projection and inverse view, the eye position and the viewport.
+struct CameraView {
+    float inv_proj[16];
+    float inv_view[16];
+    float pos[3];
+    uint32_t width;
+    uint32_t height;
+};
+
+// Per-wave path state, structure of arrays of float4 rows.
+//   ray_o  (ox, oy, oz, seed bits)     ray_d (dx, dy, dz, -)
+//   thr    (throughput rgb, -)         col   (path colour rgb, -)
+//   q[2]   ping-pong extension queues of path ids
+//   sh_o   (shadow origin xyz, distance^2)   sh_d (direction xyz, path id bits)
+//   sh_c   (unoccluded contribution rgb, -)
+//   counters[2*b] extension rays queued for bounce b, [2*b+1] shadow rays of bounce b
+struct WaveState {
+    float4* ray_o;
+    float4* ray_d;
+    float4* thr;
+    float4* col;
+    uint32_t* q[2];
+    float4* sh_o;
+    float4* sh_d;
+    float4* sh_c;
+    uint32_t* counters;
+    unsigned long long* totals;   // [0] extension rays after bounce 0, [1] shadow rays (running sums)
+    uint32_t capacity;
+};
+
+// One wave: pixels [pixel0, pixel0 + n_pixels) x samples [0, spp) with the
+// sample s of pixel p at path id (p - pixel0) * spp + s, traced as the
+// reference's frame frame0 + s.
+struct WaveJob {
+    uint32_t pixel0;
+    uint32_t n_pixels;
+    uint32_t spp;
+    uint32_t frame0;
+    int32_t max_bounces;
+    int32_t sky;
+    uint32_t pack_frame;      // when non-zero, pack the RGBA8 image at this frame index after accumulating
+};
+
+// Kernel families timed by KernelTimer.
+enum KernelFamily { kFamExtend = 0, kFamShadow = 1, kFamAccumulate = 2, kFamOther = 3, kFamCount = 4 };
+
+// Optional hook around each kernel launch (records CUDA events on the stream).
+class KernelTimer {
+public:
+    virtual ~KernelTimer() = default;
+    virtual void begin(int family, cudaStream_t stream) = 0;
+    virtual void end(int family, cudaStream_t stream) = 0;
+};
+
+struct LaunchShape {
+    int blocks_extend;
+    int blocks_shadow;
+    int threads;
+    size_t smem_spheres;      // dynamic shared memory for the sphere table (0: read from global)
+};
+
+// Fills in grid sizes for this device and scene (occupancy-derived).
+cudaError_t plan_launch(const SceneView& sc, int device, int threads, LaunchShape* out);
+
+// Enqueues one wave on stream: 2*max_bounces + 1 kernels plus a counter reset.
+// accum is W*H float4, image W*H uint32 (may be null when pack_frame == 0).
+// Returns the number of kernels launched through *launches.
+cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveState& ws, const WaveJob& job,
+                         const LaunchShape& shape, float4* accum, uint32_t* image, cudaStream_t stream,
+                         uint32_t* launches, KernelTimer* timer = nullptr);
+
+// Zeroes n float4 on stream.
+cudaError_t enqueue_clear_accum(float4* accum, uint64_t n, cudaStream_t stream);
+
+// FP32 FFMA throughput of the device in TFLOP/s (probe.cu).
+cudaError_t measure_fp32_peak(int device, double* tflops);
+
+// Debug / parity hook: nearest hit for n rays through the same device code the
+// renderer uses.  origins/dirs are 3 floats per ray in device memory.
+cudaError_t enqueue_trace_nearest(const SceneView& sc, const float* origins, const float* dirs, uint64_t n,
+                                  float* t_out, int32_t* id_out, cudaStream_t stream);
+
+// Writes W*H*3 primary directions (debug / parity hook).
+cudaError_t enqueue_primary_dirs(const CameraView& cam, float* out, cudaStream_t stream);
+
+}  // namespace atx

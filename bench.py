@@ -1,0 +1,375 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 path tracer on the medium-scene workload.
+
+Workload (one step = one render launch): 256 spheres, 64 materials, 8 point
+lights, 1920x1080, 8 bounces, 16 samples per pixel per launch = 33,177,600
+paths (one path = one pixel-sample).  Synthetic seeded scene (scenes.config1);
+the camera is set through the public API (atx_set_camera) as a caller would.
+
+Metric: Mpaths/s, whole job (N replicas on N GPUs, one process per GPU,
+`scaling: weak`).  The path state of one wave (4 Mi paths x 120 B) is larger
+than L2, so every step streams its working set through HBM; no explicit flush.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the reference's per-pixel path restated on the CPU
+(the oracle's literal-order build, OpenMP over all host cores) on a bounded
+sample of the same workload; the reference's own code cannot be built here.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+FLOP_PER_TEST = 20       # FP32 FLOP per ray-sphere test, FMA counted as 2
+FLOP_PER_SHADE = 120     # FP32 FLOP per shaded hit (BRDF + sampler + roulette)
+METRIC = "Mpaths/s per GB300"
+UNIT = "Mpaths/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# --------------------------------------------------------------- dist utils
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = False
+        if self.world > 1:
+            import torch.distributed as dist
+            backend = os.environ.get("ATX_BENCH_BACKEND", "nccl")
+            if backend == "nccl":
+                import torch
+                torch.cuda.set_device(self.local_rank)
+            dist.init_process_group(backend=backend)
+            self.pg = True
+
+    def barrier(self):
+        if self.pg:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        import torch.distributed as dist
+        dev = f"cuda:{self.local_rank}" if dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------ clocks
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.15)
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        rows = [l.split(",") for l in out.strip().splitlines() if l.strip()]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[4:8]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ CPU baseline
+
+def cpu_reference(sc, target_s: float, threads: int = 0):
+    """Times the literal-order oracle (reference expressions, OpenMP) on the first rows of the image,
+    all samples of one launch, sized to about target_s seconds.  Returns (Mpaths/s, sample text,
+    threads, Mrays/s)."""
+    import numpy as np
+
+    from oracle import pyoracle as po
+
+    po.build()
+    view = po.view_for(sc)
+    nthreads = threads or po.max_threads()
+
+    def rows(nrows):
+        ys = (np.arange(nrows, dtype=np.int64) * sc.height) // nrows       # evenly spaced rows
+        return (ys[:, None] * sc.width + np.arange(sc.width)[None, :]).reshape(-1).astype(np.uint32)
+
+    def run(nrows):
+        px = rows(nrows)
+        t0 = time.perf_counter()
+        _, _, st = po.render(sc.spheres, sc.materials, sc.lights, view, max_bounces=sc.max_bounces, spp=sc.spp,
+                             pixels=px, mode=po.LITERAL, threads=nthreads)
+        return time.perf_counter() - t0, st, len(px)
+
+    nrows = 4
+    dt, _, _ = run(nrows)
+    nrows = int(min(sc.height, max(2, nrows * target_s / max(dt, 1e-3))))
+    dt, st, npx = run(nrows)
+    paths = npx * sc.spp
+    rays = st["ext_rays"] + st["shadow_rays"]
+    sample = (f"{nrows} evenly spaced rows ({npx} pixels) x {sc.spp} spp of the {sc.width}x{sc.height} frame "
+              f"= {paths} paths, {dt:.1f} s")
+    return paths / dt / 1e6, sample, nthreads, rays / dt / 1e6
+
+
+# -------------------------------------------------------------- our arm
+
+def run_ours(args, dist: Dist):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import ataraxia_gb300 as atx
+    from ataraxia_gb300 import _native as N
+    from ataraxia_gb300 import scenes
+
+    dev = dist.local_rank
+    torch.cuda.set_device(dev)
+    sc = scenes.config1()
+    cam = atx.Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction)
+    settings = atx.Settings(accumulation=True, skyLight=False, maxBounces=sc.max_bounces)
+    paths_step = sc.pixels * sc.spp
+
+    def make(flags=0):
+        r = atx.Renderer(device=dev, flags=flags)
+        r.on_resize(sc.width, sc.height)
+        r.set_scene(sc.spheres, sc.materials, sc.lights)
+        r.set_camera(cam)
+        r.set_settings(settings)
+        return r
+
+    # ---- device-timed throughput (inputs resident in HBM)
+    r = make()
+    for _ in range(args.warmup):
+        r.render_frames(sc.spp)
+    r.synchronize()
+    stream = torch.cuda.ExternalStream(r.stream, device=dev)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    s0 = r.stats()
+    clocks = Clocks(dev)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        r.render_frames(sc.spp)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dist.barrier()
+    s1 = r.stats()
+    ms_local = ev0.elapsed_time(ev1)
+    ms = dist.max(ms_local)
+    launches = s1["kernel_launches"] - s0["kernel_launches"]
+    rays = (s1["extension_rays"] - s0["extension_rays"]) + (s1["shadow_rays"] - s0["shadow_rays"])
+    value = dist.world * args.steps * paths_step / (ms * 1e-3) / 1e6
+    mrays = dist.world * rays / (ms_local * 1e-3) / 1e6
+    r.close()
+
+    # ---- end to end through the public API with host buffers (pinned)
+    img_bytes = sc.pixels * 4
+    hbuf = C.c_void_p()
+    N.check(N.lib().atx_host_alloc(img_bytes, C.byref(hbuf)))
+    host_img = np.ctypeslib.as_array((C.c_uint32 * sc.pixels).from_address(hbuf.value))
+    sph = np.ascontiguousarray(sc.spheres)
+    mats = np.ascontiguousarray(sc.materials)
+    lts = np.ascontiguousarray(sc.lights)
+    r = atx.Renderer(device=dev)
+    r.on_resize(sc.width, sc.height)
+    r.set_settings(settings)
+
+    def e2e_step():
+        r.set_scene(sph, mats, lts)                 # H2D of the step's scene
+        r.set_camera(cam)
+        r.render_frames(sc.spp)
+        N.check(N.lib().atx_read_image(r._h, C.c_void_p(hbuf.value), sc.pixels))   # D2H of the result
+    for _ in range(args.warmup):
+        e2e_step()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    r.close()
+    N.check(N.lib().atx_host_free(hbuf))
+    h2d = len(sph) * 24 + len(mats) * 48 + len(lts) * 32      # device layout copied by atx_set_scene
+    e2e = {"value": round(dist.world * args.steps * paths_step / e2e_s / 1e6, 2), "unit": UNIT,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": img_bytes,
+           "ms_per_step": round(e2e_s * 1e3 / args.steps, 3)}
+    _ = host_img
+
+    # ---- roofline of the dominant kernel (extension: nearest hit + shading) from per-kernel events
+    rp = make(N.FLAG_PROFILE_KERNELS)
+    for _ in range(max(1, args.warmup)):
+        rp.render_frames(sc.spp)
+    rp.synchronize()
+    rp.reset_kernel_times()
+    p0 = rp.stats()
+    prof_steps = max(2, min(args.steps, 8))
+    for _ in range(prof_steps):
+        rp.render_frames(sc.spp)
+    kt = rp.kernel_times()
+    p1 = rp.stats()
+    rp.close()
+    ext_rays = p1["extension_rays"] - p0["extension_rays"]
+    sh_rays = p1["shadow_rays"] - p0["shadow_rays"]
+    n_sph = len(sc.spheres)
+    ext_flops = ext_rays * n_sph * FLOP_PER_TEST + sh_rays * FLOP_PER_SHADE
+    total_kernel_ms = kt["extend_ms"] + kt["shadow_ms"] + kt["accumulate_ms"] + kt["other_ms"]
+    peak = atx.measure_fp32_peak(dev)
+    achieved = ext_flops / (kt["extend_ms"] * 1e-3) / 1e12
+    roofline = {
+        "kernel": "k_extend (nearest hit over shared-memory sphere table + shading)",
+        "bound": "fp32", "achieved": round(achieved, 2), "peak": round(peak, 2), "unit": "TFLOP/s",
+        "frac": round(achieved / peak, 4) if peak else None,
+        "peak_source": "measured FFMA throughput (atx_measure_fp32_peak, this process); MEASURED_PEAKS.json "
+                       "has no FP32 figure",
+        "traffic": None,
+        "flop_per_launch": round(ext_flops / max(1, kt["extend_launches"])),
+        "avg_launch_ms": round(kt["extend_ms"] / max(1, kt["extend_launches"]), 4),
+        "share_of_kernel_time": round(kt["extend_ms"] / total_kernel_ms, 4) if total_kernel_ms else None,
+        "kernel_ms_per_step": {k: round(kt[k] / prof_steps, 3) for k in
+                               ("extend_ms", "shadow_ms", "accumulate_ms", "other_ms")},
+    }
+    traffic_file = ROOT / "profiles" / "k_extend_config1_traffic.json"
+    if traffic_file.exists():
+        try:
+            roofline["traffic"] = json.loads(traffic_file.read_text()).get("bytes_per_launch")
+        except ValueError:
+            pass
+
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes.config1)",
+        "config": {"workload": "medium scene: 256 spheres, 64 materials, 8 lights, 1920x1080, 8 bounces, "
+                               "16 spp per launch (one step = one launch)",
+                   "paths_per_step": paths_step, "parallelism": f"replicas x{dist.world}",
+                   "l2": "working set > L2: 4 Mi-path wave state (480 MB) streamed per wave"},
+        "mrays_per_s": round(mrays, 1),
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "roofline": roofline,
+        "e2e": e2e,
+    }
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        v, sample, cores, mr = cpu_reference(sc, args.cpu_seconds)
+        out["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": sample, "mrays_per_s": round(mr, 3),
+                               "what": "reference per-pixel path restated in C (literal expression order), "
+                                       "OpenMP over rows"}
+    return out
+
+
+# -------------------------------------------------------- reference arm
+
+def run_reference(args, dist: Dist):
+    from ataraxia_gb300 import scenes
+
+    sc = scenes.config1()
+    vals = []
+    sample = ""
+    cores = 0
+    mrays = []
+    for i in range(args.warmup + args.steps):
+        v, sample, cores, mr = cpu_reference(sc, args.ref_step_seconds)
+        if i >= args.warmup:
+            vals.append(v)
+            mrays.append(mr)
+    value = statistics.mean(vals)
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes.config1)",
+        "config": {"workload": "medium scene: 256 spheres, 64 materials, 8 lights, 1920x1080, 8 bounces, "
+                               "16 spp per launch", "parallelism": "host cores (OpenMP)"},
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample + " per step"},
+        "mrays_per_s": round(statistics.mean(mrays), 3),
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own render path needs glm, Vulkan and GLFW, absent here; this arm runs its "
+                "per-pixel path restated in C on the host cores",
+    }
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=3.0)
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        log("warmup raised to 3 (minimum)")
+        args.warmup = 3
+
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            if dist.rank != 0:
+                return 0
+            out = run_reference(args, dist)
+        else:
+            out = run_ours(args, dist)
+        if dist.rank == 0:
+            print(json.dumps(out), flush=True)
+    finally:
+        dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,240 @@
+/*
+ * atx.h - C ABI of the GB300 path tracer (libatx.so).
+ *
+ * Drop-in boundary for the render call of 1neskk/Ataraxia.  Each entry point
+ * names the reference interface it replaces (paths relative to the Ataraxia
+ * tree).  Plain pointers and sizes only; every call returns an atx_status and
+ * never exits the process (the reference's CUDA_CHECK calls exit(),
+ * Engine/include/DeviceMemory.h:7-16).
+ *
+ * Threading: calls on one atx_renderer must be serialised by the caller;
+ * different renderers may be used from different threads.  Work is enqueued on
+ * the renderer's own CUDA stream; functions that return data to the host
+ * synchronise that stream first.
+ */
+#ifndef ATX_H
+#define ATX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define ATX_API __declspec(dllexport)
+#else
+#define ATX_API __attribute__((visibility("default")))
+#endif
+
+#define ATX_ABI_VERSION 1
+
+typedef enum atx_status {
+    ATX_OK = 0,
+    ATX_ERR_INVALID_ARG = 1,   /* bad pointer, size, index or state */
+    ATX_ERR_OUT_OF_MEMORY = 2, /* device allocation failed or the HBM budget is exceeded */
+    ATX_ERR_CUDA = 3,          /* a CUDA runtime call failed; see atx_last_error() */
+    ATX_ERR_TIMEOUT = 4,       /* a bounded wait ran out */
+    ATX_ERR_BUSY = 5,          /* admission refused for now (queue full) */
+    ATX_ERR_NOT_FOUND = 6,     /* unknown job id */
+    ATX_ERR_CANCELLED = 7,     /* the job was cancelled */
+    ATX_ERR_NO_DEVICE = 8,     /* no CUDA device is visible */
+    ATX_ERR_PARSE = 9          /* malformed scene file */
+} atx_status;
+
+/* ------------------------------------------------------------------ scene */
+
+/* Sphere: Engine/include/SceneNode.h:11-21 (glm::vec3 center; float radius;
+ * int id), 20 bytes.  material indexes the material array; out-of-range
+ * values render with material 0 (Renderer.cu:30-37). */
+typedef struct atx_sphere {
+    float center[3];
+    float radius;
+    int32_t material;
+} atx_sphere;
+
+/* Material: Engine/include/Scene.h:28-47, 52 bytes.  id is carried but unused. */
+typedef struct atx_material {
+    float albedo[3];
+    float roughness;
+    float metallic;
+    float f0[3];
+    float emission_color[3];
+    float emission_intensity;
+    int32_t id;
+} atx_material;
+
+/* Point light: Engine/include/Scene.h:17-26, 28 bytes. */
+typedef struct atx_light {
+    float position[3];
+    float color[3];
+    float intensity;
+} atx_light;
+
+/* Settings: Engine/include/Scene.h:49-56, same 8-byte layout (two bools and
+ * an int).  Defaults: accumulation = 1, sky_light = 0, max_bounces = 15. */
+typedef struct atx_settings {
+    uint8_t accumulation;
+    uint8_t sky_light;
+    uint8_t reserved[2];
+    int32_t max_bounces;
+} atx_settings;
+
+/* Camera parameters: Engine/include/Camera.h:63-75 (position, direction, fov
+ * in degrees, near and far clip).  The reference's default camera is
+ * fov 45, near 0.1, far 100, position (0, 0, 3), direction (0, 0, -1)
+ * (Engine/src/Camera.cpp:14-21). */
+typedef struct atx_camera {
+    float position[3];
+    float direction[3];
+    float fov_deg;
+    float near_clip;
+    float far_clip;
+} atx_camera;
+
+/* --------------------------------------------------------------- renderer */
+
+typedef struct atx_config {
+    int32_t device;            /* CUDA device ordinal */
+    uint32_t wave_paths;       /* paths in flight per wave; 0 = autotuned default */
+    uint32_t threads;          /* threads per block; 0 = default */
+    uint32_t bvh_threshold;    /* sphere count at which the LBVH replaces the brute-force loop; 0 = autotuned */
+    uint32_t bvh_leaf_size;    /* spheres per BVH leaf; 0 = autotuned */
+    uint32_t flags;            /* ATX_FLAG_* */
+    uint64_t hbm_budget_bytes; /* device bytes this renderer may hold; 0 = unlimited */
+} atx_config;
+
+#define ATX_FLAG_NO_GRAPHS 1u       /* launch kernels directly instead of replaying a CUDA graph */
+#define ATX_FLAG_PROFILE_KERNELS 2u /* record CUDA events around every kernel (atx_get_kernel_times) */
+
+typedef struct atx_stats {
+    uint64_t frames;           /* reference frames rendered (samples per pixel) since creation */
+    uint64_t paths;            /* pixel-samples traced */
+    uint64_t extension_rays;   /* nearest-hit rays traced */
+    uint64_t shadow_rays;      /* shadow rays traced */
+    uint64_t kernel_launches;  /* kernels this renderer launched */
+    uint64_t device_bytes;     /* device memory currently held */
+    double last_render_ms;     /* device time of the last atx_render (CUDA events) */
+    uint32_t bvh_in_use;       /* 1 if the current scene uses the LBVH */
+    uint32_t reserved;
+} atx_stats;
+
+typedef struct atx_renderer atx_renderer;
+
+ATX_API int atx_abi_version(void);
+ATX_API const char* atx_status_string(atx_status status);
+/* Message of the last failure on the calling thread (empty if none). */
+ATX_API const char* atx_last_error(void);
+ATX_API atx_status atx_device_count(int32_t* count);
+
+/* Renderer::Renderer (Engine/src/Renderer.cu:13-15).  config may be NULL. */
+ATX_API atx_status atx_renderer_create(const atx_config* config, atx_renderer** out);
+/* Renderer::~Renderer (Engine/src/Renderer.cu:17-23). */
+ATX_API atx_status atx_renderer_destroy(atx_renderer* r);
+
+/* Renderer::onResize (Engine/include/Renderer.h:23, Renderer.cu:98-146):
+ * reallocates the float4 accumulator and the RGBA8 image when the size
+ * changes and resets the frame index to 1. */
+ATX_API atx_status atx_resize(atx_renderer* r, uint32_t width, uint32_t height);
+
+/* Scene upload (Renderer::allocateDeviceMemory, Renderer.cu:25-57).  The
+ * scene graph is flattened by the caller (Renderer.cu:67-96); arrays are
+ * copied, so the caller may free them on return.  Spheres with a material
+ * index outside [0, n_materials) use material 0.  n_materials may be 0 only
+ * when n_spheres is 0.  Does not reset the frame index (the reference's UI
+ * resets it explicitly). */
+ATX_API atx_status atx_set_scene(atx_renderer* r, const atx_sphere* spheres, uint32_t n_spheres,
+                                 const atx_material* materials, uint32_t n_materials,
+                                 const atx_light* lights, uint32_t n_lights);
+
+/* Renderer::setSettings / getSettings (Engine/include/Renderer.h:28-29). */
+ATX_API atx_status atx_set_settings(atx_renderer* r, const atx_settings* settings);
+ATX_API atx_status atx_get_settings(const atx_renderer* r, atx_settings* settings);
+
+/* Renderer::resetFrameIndex (Engine/include/Renderer.h:31). */
+ATX_API atx_status atx_reset_frame_index(atx_renderer* r);
+ATX_API atx_status atx_get_frame_index(const atx_renderer* r, uint32_t* frame_index);
+
+/* Camera (Engine/src/Camera.cpp:134-195): the projection and view matrices
+ * are computed as the reference does for the current viewport and recomputed
+ * after a resize; primary rays are generated on the device. */
+ATX_API atx_status atx_set_camera(atx_renderer* r, const atx_camera* camera);
+/* Camera given directly by its inverse matrices (column-major, as glm) and
+ * position, the inputs of Camera::UpdateRayDirection (Camera.cpp:161-195). */
+ATX_API atx_status atx_set_camera_matrices(atx_renderer* r, const float inv_view[16], const float inv_proj[16],
+                                           const float position[3]);
+
+/* Renderer::Render (Engine/include/Renderer.h:24, Renderer.cu:173-249) for spp
+ * consecutive frames.  Frame f of the reference (seed = pixel * f) is sample
+ * f - frame_index of this call: with accumulation on, the accumulator after
+ * this call equals the reference's after the same frames and the frame index
+ * advances by spp; with accumulation off the accumulator is cleared, frames
+ * 1..spp are accumulated and the frame index stays 1.  A frame index of 1
+ * clears the accumulator first (Renderer.cu:181-182).  The RGBA8 image is
+ * packed for the last frame (Renderer.cu:166-168).  Asynchronous. */
+ATX_API atx_status atx_render(atx_renderer* r, uint32_t spp);
+ATX_API atx_status atx_synchronize(atx_renderer* r);
+
+/* Reads n_pixels float4 of the accumulator (sum of (r, g, b, 1) per frame). */
+ATX_API atx_status atx_read_accumulation(atx_renderer* r, float* host_rgba, uint64_t n_pixels);
+/* Reads the RGBA8 image (Renderer::getImage, Renderer.h:26; the reference
+ * copies it to the host every frame, Renderer.cu:240). */
+ATX_API atx_status atx_read_image(atx_renderer* r, uint32_t* host_rgba8, uint64_t n_pixels);
+/* Device pointers of the accumulator (float4) and image (uint32) for zero-copy consumers. */
+ATX_API atx_status atx_device_buffers(atx_renderer* r, void** accumulation, void** image);
+
+ATX_API atx_status atx_get_stats(const atx_renderer* r, atx_stats* stats);
+
+/* Device time per kernel family, summed over launches since the last reset,
+ * from CUDA events recorded on the renderer's stream when the renderer was
+ * created with ATX_FLAG_PROFILE_KERNELS (all zero otherwise).  No counterpart
+ * in the reference, which only times Render() on the host (main.cpp:213-219). */
+typedef struct atx_kernel_times {
+    double extend_ms;          /* nearest hit + shading + next ray, all bounces */
+    double shadow_ms;          /* shadow-ray any-hit */
+    double accumulate_ms;      /* accumulator update + RGBA8 pack */
+    double other_ms;           /* clears, BVH build */
+    uint64_t extend_launches;
+    uint64_t shadow_launches;
+    uint64_t accumulate_launches;
+    uint64_t other_launches;
+} atx_kernel_times;
+ATX_API atx_status atx_get_kernel_times(atx_renderer* r, atx_kernel_times* times);
+ATX_API atx_status atx_reset_kernel_times(atx_renderer* r);
+
+/* The renderer's CUDA stream (a cudaStream_t), so callers can order their own
+ * work and timing events after the renderer's. */
+ATX_API atx_status atx_get_stream(atx_renderer* r, void** stream);
+
+/* Measures the device's FP32 fused multiply-add throughput (TFLOP/s, FMA =
+ * 2 FLOP) with a register-resident FFMA loop on every SM: the roofline
+ * denominator for the FP32-bound kernels. */
+ATX_API atx_status atx_measure_fp32_peak(int32_t device, double* tflops);
+
+/* Page-locked host memory for fast copies in and out. */
+ATX_API atx_status atx_host_alloc(uint64_t bytes, void** out);
+ATX_API atx_status atx_host_free(void* p);
+
+/* --------------------------------------------------------- host helpers */
+
+/* Camera.cpp:134-159 on the host for a width x height viewport: view, inverse
+ * view, projection and inverse projection, column-major.  Needs no GPU. */
+ATX_API atx_status atx_camera_matrices(const atx_camera* camera, uint32_t width, uint32_t height, float view[16],
+                                       float inv_view[16], float proj[16], float inv_proj[16]);
+
+/* --------------------------------------------------------- parity hooks */
+
+/* Nearest hit of n rays against the renderer's current scene through the
+ * device code the renderer traces with (brute force or LBVH).  origins and
+ * dirs are host arrays of 3 floats per ray; t_out is -1 and id_out -1 on a
+ * miss (Renderer.cu:251-285). */
+ATX_API atx_status atx_trace_nearest(atx_renderer* r, const float* origins, const float* dirs, uint64_t n,
+                                     float* t_out, int32_t* id_out);
+/* W*H*3 primary ray directions for the current camera (Camera.cpp:161-195). */
+ATX_API atx_status atx_primary_directions(atx_renderer* r, float* host_dirs, uint64_t n_pixels);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
