@@ -311,6 +311,35 @@ def run_ours(args, dist: Dist):
     return out
 
 
+def run_render_only(args, dist: Dist):
+    """Warm-up and timed launches of the workload, nothing else (profiler captures)."""
+    import ataraxia_gb300 as atx
+    from ataraxia_gb300 import scenes
+
+    sc = scenes.config1()
+    if args.width and args.height:
+        sc = sc.with_resolution(args.width, args.height)
+    r = atx.Renderer(device=dist.local_rank)
+    r.on_resize(sc.width, sc.height)
+    r.set_scene(sc.spheres, sc.materials, sc.lights)
+    r.set_camera(atx.Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction))
+    r.set_settings(atx.Settings(accumulation=True, skyLight=False, maxBounces=sc.max_bounces))
+    for _ in range(args.warmup):
+        r.render_frames(sc.spp)
+    r.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r.render_frames(sc.spp)
+    r.synchronize()
+    dt = time.perf_counter() - t0
+    st = r.stats()
+    r.close()
+    return {"mode": "render", "width": sc.width, "height": sc.height, "steps": args.steps,
+            "wall_ms_per_step": round(dt * 1e3 / args.steps, 3),
+            "Mpaths_per_s_wall": round(args.steps * sc.pixels * sc.spp / dt / 1e6, 1),
+            "kernel_launches": st["kernel_launches"]}
+
+
 # -------------------------------------------------------- reference arm
 
 def run_reference(args, dist: Dist):
@@ -351,6 +380,10 @@ def main(argv=None) -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=3.0)
+    ap.add_argument("--mode", choices=["full", "render"], default="full",
+                    help="render: only warm-up + timed launches of the workload (for profiler captures)")
+    ap.add_argument("--width", type=int, default=0, help="render mode: override the viewport width")
+    ap.add_argument("--height", type=int, default=0, help="render mode: override the viewport height")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         log("warmup raised to 3 (minimum)")
@@ -358,7 +391,9 @@ def main(argv=None) -> int:
 
     dist = Dist()
     try:
-        if args.impl == "reference":
+        if args.mode == "render":
+            out = run_render_only(args, dist)
+        elif args.impl == "reference":
             if dist.rank != 0:
                 return 0
             out = run_reference(args, dist)

@@ -107,8 +107,8 @@ def f32vec(x) -> np.ndarray:
 def camera_matrices(position, direction, fov=45.0, near=0.1, far=100.0, width=1280, height=720):
     """(view, inv_view, proj, inv_proj), each a flat column-major float32[16]."""
     out = [np.zeros(16, dtype=np.float32) for _ in range(4)]
-    lib().orc_camera_matrices(_p(f32vec(position)), _p(f32vec(direction)), fov, near, far, width, height,
-                              *[_p(o) for o in out])
+    pos, dirv = f32vec(position), f32vec(direction)      # keep the arrays alive across the call
+    lib().orc_camera_matrices(_p(pos), _p(dirv), fov, near, far, width, height, *[_p(o) for o in out])
     return tuple(out)
 
 
@@ -196,23 +196,24 @@ def sincos2pi(u: float):
 
 def cook_torrance(albedo, f0, metallic, roughness, n, v, l, mode=EXACT):
     out = np.zeros(3, dtype=np.float32)
-    args = [f32vec(a) for a in (albedo, f0)]
-    lib().orc_cook_torrance(mode, _p(args[0]), _p(args[1]), metallic, roughness, _p(f32vec(n)), _p(f32vec(v)),
-                            _p(f32vec(l)), _p(out))
+    a, f, nn, vv, ll = (f32vec(x) for x in (albedo, f0, n, v, l))
+    lib().orc_cook_torrance(mode, _p(a), _p(f), metallic, roughness, _p(nn), _p(vv), _p(ll), _p(out))
     return out
 
 
 def sample_cosine(n, seed, mode=EXACT):
     out = np.zeros(3, dtype=np.float32)
     s = C.c_uint32(seed & 0xFFFFFFFF)
-    lib().orc_sample_cosine(mode, _p(f32vec(n)), C.byref(s), _p(out))
+    nn = f32vec(n)
+    lib().orc_sample_cosine(mode, _p(nn), C.byref(s), _p(out))
     return out, s.value
 
 
 def sample_ggx(n, roughness, seed, mode=EXACT):
     out = np.zeros(3, dtype=np.float32)
     s = C.c_uint32(seed & 0xFFFFFFFF)
-    lib().orc_sample_ggx(mode, _p(f32vec(n)), roughness, C.byref(s), _p(out))
+    nn = f32vec(n)
+    lib().orc_sample_ggx(mode, _p(nn), roughness, C.byref(s), _p(out))
     return out, s.value
 
 
