@@ -100,8 +100,8 @@ atx_status SceneStore::upload(const atx_sphere* s, uint32_t n, const atx_materia
 uint64_t WaveStore::bytes_for(uint32_t capacity, uint32_t max_bounces)
 {
     const uint64_t c = capacity;
-    return c * (7 * sizeof(float4) + 2 * sizeof(uint32_t)) + 2ull * (max_bounces + 1) * sizeof(uint32_t) + 16 +
-           10 * 256;
+    return c * (7 * sizeof(float4) + 2 * sizeof(uint32_t) + sizeof(uint2)) +
+           2ull * (max_bounces + 1) * sizeof(uint32_t) + 16 + 12 * 256;
 }
 
 atx_status WaveStore::ensure(uint32_t capacity, uint32_t max_bounces, Budget* budget)
@@ -127,6 +127,7 @@ atx_status WaveStore::ensure(uint32_t capacity, uint32_t max_bounces, Budget* bu
     view.sh_c = reinterpret_cast<float4*>(take(c * sizeof(float4)));
     view.q[0] = reinterpret_cast<uint32_t*>(take(c * sizeof(uint32_t)));
     view.q[1] = reinterpret_cast<uint32_t*>(take(c * sizeof(uint32_t)));
+    view.prim = reinterpret_cast<uint2*>(take(c * sizeof(uint2)));
     view.counters = reinterpret_cast<uint32_t*>(take(2ull * (b + 1) * sizeof(uint32_t)));
     view.capacity = cap;
     bounces = b;

@@ -127,7 +127,29 @@ __device__ __forceinline__ void stage_spheres(const SceneView& sc, float4* s_sph
     __syncthreads();
 }
 
-template <bool FIRST, bool SMEM>
+// Primary nearest hit once per pixel of the wave (shared by its samples).
+template <bool SMEM>
+__global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView cam, WaveState ws, WaveJob job)
+{
+    extern __shared__ float4 s_sph[];
+    const uint32_t n = job.n_pixels;
+    if (blockIdx.x * blockDim.x >= n) return;
+    if (SMEM) stage_spheres(sc, s_sph);
+    const float4* sph = SMEM ? s_sph : sc.sph;
+    const float3 o = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        const uint32_t p = job.pixel0 + j;
+        const float3 d = primary_dir(cam, p % cam.width, p / cam.width);
+        float t;
+        const int32_t id = scene_nearest<SMEM>(sc, sph, o, d, t);
+        ws.prim[j] = make_uint2(__float_as_uint(t), (uint32_t)id);
+    }
+}
+
+// SHARED (first bounce only): take the nearest hit from k_primary's per-pixel
+// record instead of tracing the primary ray again.
+template <bool FIRST, bool SMEM, bool SHARED>
 __global__ void __launch_bounds__(kThreads) k_extend(SceneView sc, CameraView cam, WaveState ws, WaveJob job,
                                                      int bounce)
 {
@@ -171,7 +193,14 @@ __global__ void __launch_bounds__(kThreads) k_extend(SceneView sc, CameraView ca
             seed += (uint32_t)bounce;
 
             float tmin;
-            const int32_t hit = scene_nearest<SMEM>(sc, sph, o, d, tmin);
+            int32_t hit;
+            if (SHARED) {
+                const uint2 pr = ws.prim[idx / job.spp];
+                tmin = __uint_as_float(pr.x);
+                hit = (int32_t)pr.y;
+            } else {
+                hit = scene_nearest<SMEM>(sc, sph, o, d, tmin);
+            }
             bool touch = false;
             float3 add = mk3(0.f, 0.f, 0.f);
             if (hit < 0) {
@@ -372,20 +401,20 @@ cudaError_t plan_launch(const SceneView& sc, int device, int threads, LaunchShap
     int per_sm_ext = 0, per_sm_sh = 0;
     if (smem) {
         if (bytes > 48 * 1024) {
-            e = cudaFuncSetAttribute(k_extend<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(k_extend<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(k_shadow<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(k_trace<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            const int b = (int)bytes;
+            const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+            e = cudaFuncSetAttribute(k_extend<true, true, false>, a, b);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_extend<false, true, false>, a, b);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_primary<true>, a, b);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shadow<true>, a, b);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace<true>, a, b);
             if (e != cudaSuccess) return e;
         }
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, true>, threads, bytes);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, true, false>, threads, bytes);
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<true>, threads, bytes);
     } else {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, false>, threads, 0);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, false, false>, threads, 0);
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<false>, threads, 0);
     }
@@ -414,20 +443,35 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
         cudaError_t e = cudaMemsetAsync(ws.counters, 0, sizeof(uint32_t) * 2 * ((size_t)bounces + 1), stream);
         if (e != cudaSuccess) return e;
         const int g0 = grid_for(paths, shape.threads, shape.blocks_extend);
+        const bool share = job.spp > 1;
+        if (share) {
+            const int gp = grid_for(job.n_pixels, shape.threads, shape.blocks_extend);
+            begin(kFamExtend);
+            if (smem)
+                k_primary<true><<<gp, shape.threads, sm, stream>>>(sc, cam, ws, job);
+            else
+                k_primary<false><<<gp, shape.threads, 0, stream>>>(sc, cam, ws, job);
+            end(kFamExtend);
+            ++nl;
+        }
         begin(kFamExtend);
-        if (smem)
-            k_extend<true, true><<<g0, shape.threads, sm, stream>>>(sc, cam, ws, job, 0);
-        else
-            k_extend<true, false><<<g0, shape.threads, 0, stream>>>(sc, cam, ws, job, 0);
+        if (share) {
+            // no sphere table needed: the nearest hit comes from k_primary
+            k_extend<true, false, true><<<g0, shape.threads, 0, stream>>>(sc, cam, ws, job, 0);
+        } else if (smem) {
+            k_extend<true, true, false><<<g0, shape.threads, sm, stream>>>(sc, cam, ws, job, 0);
+        } else {
+            k_extend<true, false, false><<<g0, shape.threads, 0, stream>>>(sc, cam, ws, job, 0);
+        }
         end(kFamExtend);
         ++nl;
         for (int b = 0; b < bounces; ++b) {
             if (b > 0) {
                 begin(kFamExtend);
                 if (smem)
-                    k_extend<false, true><<<shape.blocks_extend, shape.threads, sm, stream>>>(sc, cam, ws, job, b);
+                    k_extend<false, true, false><<<shape.blocks_extend, shape.threads, sm, stream>>>(sc, cam, ws, job, b);
                 else
-                    k_extend<false, false><<<shape.blocks_extend, shape.threads, 0, stream>>>(sc, cam, ws, job, b);
+                    k_extend<false, false, false><<<shape.blocks_extend, shape.threads, 0, stream>>>(sc, cam, ws, job, b);
                 end(kFamExtend);
                 ++nl;
             }

@@ -78,6 +78,9 @@ struct CameraView {
 //   sh_o   (shadow origin xyz, distance^2)   sh_d (direction xyz, path id bits)
 //   sh_c   (unoccluded contribution rgb, -)
 //   counters[2*b] extension rays queued for bounce b, [2*b+1] shadow rays of bounce b
+//   prim   one primary hit per pixel: the reference's primary ray depends on
+//          the pixel only (Camera.cpp:161-195, no jitter), so every sample of a
+//          pixel in one launch shares the same nearest hit
 struct WaveState {
     float4* ray_o;
     float4* ray_d;
@@ -89,6 +92,7 @@ struct WaveState {
     float4* sh_c;
     uint32_t* counters;
     unsigned long long* totals;   // [0] extension rays after bounce 0, [1] shadow rays (running sums)
+    uint2* prim;                  // per pixel of the wave: primary hit (t bits, sphere id), shared by its samples
     uint32_t capacity;
 };
 

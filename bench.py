@@ -288,6 +288,10 @@ def run_ours(args, dist: Dist):
         except ValueError:
             pass
 
+    ref_kernel = None
+    if dist.world == 1 and not args.no_ref_kernel:
+        ref_kernel = time_reference_kernel(sc, cam, dev, args)
+
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
@@ -302,6 +306,9 @@ def run_ours(args, dist: Dist):
         "roofline": roofline,
         "e2e": e2e,
     }
+    if ref_kernel:
+        out["ref_cuda_kernel"] = ref_kernel
+        out["vs_ref_cuda_kernel"] = round(value / ref_kernel["kernel_mpaths_s"], 2)
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         v, sample, cores, mr = cpu_reference(sc, args.cpu_seconds)
         out["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port",
@@ -309,6 +316,50 @@ def run_ours(args, dist: Dist):
                                "what": "reference per-pixel path restated in C (literal expression order), "
                                        "OpenMP over rows"}
     return out
+
+
+def time_reference_kernel(sc, cam, dev, args) -> dict:
+    """The reference's kernelRender restated (baseline/refport), one sample per launch as the reference
+    renders: kernel-only device time over the same number of samples per pixel as one of our steps, and
+    the reference's whole per-frame Render() sequence (ray-direction upload, syncs, image copy) by wall
+    clock."""
+    import torch
+
+    import ataraxia_gb300 as atx
+    from baseline import refport
+
+    _, iv, _, ip = atx.camera_matrices(cam, sc.width, sc.height)
+    dirs = refport.ray_dirs(iv, ip, sc.width, sc.height)
+    port = refport.RefPort(sc.spheres, sc.materials, sc.lights, sc.width, sc.height, dirs, sc.camera_position,
+                           sc.max_bounces)
+    try:
+        for _ in range(3):
+            port.frame()
+        port.sync()
+        frames = sc.spp * max(1, min(args.steps, 4))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(frames):
+            port.frame()
+        e1.record()
+        e1.synchronize()
+        k_ms = e0.elapsed_time(e1)
+        t0 = time.perf_counter()
+        for _ in range(sc.spp):
+            port.frame(full=True)
+        port.sync()
+        r_s = time.perf_counter() - t0
+        bx, by = port.block()
+    finally:
+        port.close()
+    return {"kernel_mpaths_s": round(frames * sc.pixels / (k_ms * 1e-3) / 1e6, 2),
+            "render_mpaths_s": round(sc.spp * sc.pixels / r_s / 1e6, 2),
+            "kernel_ms_per_frame": round(k_ms / frames, 3), "block": [bx, by],
+            "what": "reference kernelRender restated (baseline/refport/refport.cu), -use_fast_math, sm_103a, "
+                    "1 spp per launch; render_* includes the reference's per-frame ray-direction upload, syncs "
+                    "and image copy"}
 
 
 def run_render_only(args, dist: Dist):
@@ -378,6 +429,7 @@ def main(argv=None) -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ref-kernel", action="store_true", help="skip timing the restated reference kernel")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=3.0)
     ap.add_argument("--mode", choices=["full", "render"], default="full",
