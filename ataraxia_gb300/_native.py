@@ -104,6 +104,8 @@ SIGNATURES = {
     "atx_host_alloc": (_ST, [_U64, C.POINTER(_P)]),
     "atx_host_free": (_ST, [_P]),
     "atx_camera_matrices": (_ST, [C.POINTER(CameraDesc), _U32, _U32, _P, _P, _P, _P]),
+    "atx_render_noalloc": (_ST, [_P, _U32, _P, _U32, _P, _U32, _P, _P, _P, _U32, _U32, C.POINTER(Settings), _U32,
+                                 _U32, _P, _P, _P]),
     "atx_trace_nearest": (_ST, [_P, _P, _P, _U64, _P, _P]),
     "atx_primary_directions": (_ST, [_P, _P, _U64]),
 }

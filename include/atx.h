@@ -216,6 +216,37 @@ ATX_API atx_status atx_measure_fp32_peak(int32_t device, double* tflops);
 ATX_API atx_status atx_host_alloc(uint64_t bytes, void** out);
 ATX_API atx_status atx_host_free(void* p);
 
+/* ------------------------------------------------- allocation-free render */
+
+/* Renders spp frames without allocating device memory.  No counterpart in
+ * the reference (whose Renderer allocates with cudaMalloc on every frame).
+ * For callers that cannot call cudaMalloc: code embedded in a runtime that
+ * owns all device memory through its own pool, or code that must not
+ * allocate because cudaMalloc/cudaFree synchronise the device or are not
+ * allowed where it runs.  The scratch these kernels need (scene tables, path
+ * state, queues) is a 64 MiB array compiled into libatx.so, held by every
+ * device that loads the library until the process exits.
+ *   - spheres/materials/lights, accumulation (width*height float4, read and
+ *     updated) and image (width*height RGBA8, may be NULL) are DEVICE
+ *     pointers; inv_view/inv_proj/position/settings are host pointers.
+ *   - Frame semantics are atx_render's: frame frame_index (>= 1) onward,
+ *     frame 1 clears the accumulator, accumulation off renders frames 1..spp.
+ *   - Limits: 16384 spheres, 4096 materials, 1024 lights, 1024 bounces;
+ *     larger inputs return ATX_ERR_INVALID_ARG.  Always the brute-force
+ *     nearest-hit loop (no BVH, which would need its own scratch).
+ *   - Work is enqueued on stream (a cudaStream_t, NULL = default stream).
+ *     All calls share the one scratch array, so calls that overlap on the GPU
+ *     race: serialise them.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture. */
+ATX_API atx_status atx_render_noalloc(const atx_sphere* spheres, uint32_t n_spheres, const atx_material* materials,
+                                      uint32_t n_materials, const atx_light* lights, uint32_t n_lights,
+                                      const float inv_view[16], const float inv_proj[16], const float position[3],
+                                      uint32_t width, uint32_t height, const atx_settings* settings,
+                                      uint32_t frame_index, uint32_t spp, float* accumulation, uint32_t* image,
+                                      void* stream);
+
 /* --------------------------------------------------------- host helpers */
 
 /* Camera.cpp:134-159 on the host for a width x height viewport: view, inverse
