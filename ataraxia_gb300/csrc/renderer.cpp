@@ -11,7 +11,7 @@
 namespace atx {
 
 namespace {
-constexpr uint32_t kDefaultWavePaths = 4u << 20;   // 4 Mi paths, ~480 MB of state
+constexpr uint32_t kDefaultWavePaths = 16u << 20;  // 16 Mi paths, ~2.2 GB of state
 constexpr uint32_t kDefaultBvhThreshold = 1024;
 constexpr uint32_t kDefaultBvhLeaf = 2;
 constexpr uint32_t kMaxBounces = 4096;
@@ -208,7 +208,7 @@ atx_status EventTimer::collect(atx_kernel_times* t)
 atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore& ws, const LaunchShape& shape,
                           uint32_t frame0, uint32_t spp, int32_t max_bounces, int32_t sky, float4* accum,
                           uint32_t* image, uint32_t capacity, cudaStream_t stream, uint32_t* launches,
-                          KernelTimer* timer)
+                          KernelTimer* timer, uint64_t* primary_rays)
 {
     const uint64_t pixels = (uint64_t)cam.width * cam.height;
     const WavePlan plan = plan_waves(pixels, spp, capacity);
@@ -225,6 +225,8 @@ atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore&
             job.sky = sky;
             job.pack_frame = (s0 + job.spp >= spp && image) ? last_frame : 0u;
             ATX_CUDA(enqueue_wave(sc, cam, ws.view, job, shape, accum, image, stream, launches, timer));
+            // primary rays traced: once per pixel when its samples share the hit
+            if (primary_rays && max_bounces > 0) *primary_rays += job.spp > 1 ? np : (uint64_t)np * job.spp;
         }
     }
     return ATX_OK;
@@ -377,15 +379,17 @@ atx_status Renderer::render(uint32_t spp)
         if (timer) timer->end(kFamOther, stream_);
         ++launches;
     }
+    uint64_t primary_rays = 0;
     ATX_TRY(enqueue_frames(scene_.view, camv_, wave_, shape_, f0, spp, bounces, settings_.sky_light ? 1 : 0,
-                           accum_.as<float4>(), image_.as<uint32_t>(), capacity, stream_, &launches, timer));
+                           accum_.as<float4>(), image_.as<uint32_t>(), capacity, stream_, &launches, timer,
+                           &primary_rays));
     ATX_CUDA(cudaEventRecord(ev_stop_, stream_));
     timed_ = true;
     frame_ = settings_.accumulation ? f0 + spp : 1u;  // Renderer.cu:245-248
     st_.frames += spp;
     st_.paths += (uint64_t)width_ * height_ * spp;
     st_.kernel_launches += launches;
-    if (bounces > 0) totals_host_[0] += (uint64_t)width_ * height_ * spp;  // bounce-0 rays
+    totals_host_[0] += primary_rays;
     return ATX_OK;
 }
 

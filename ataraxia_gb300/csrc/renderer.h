@@ -50,7 +50,7 @@ WavePlan plan_waves(uint64_t pixels, uint32_t spp, uint32_t capacity);
 atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore& ws, const LaunchShape& shape,
                           uint32_t frame0, uint32_t spp, int32_t max_bounces, int32_t sky, float4* accum,
                           uint32_t* image, uint32_t capacity, cudaStream_t stream, uint32_t* launches,
-                          KernelTimer* timer = nullptr);
+                          KernelTimer* timer = nullptr, uint64_t* primary_rays = nullptr);
 
 // Records a pair of CUDA events around each kernel and sums their durations
 // per kernel family when collected.

@@ -19,6 +19,8 @@
 // order.  The random stream is consumed per path exactly as the reference
 // does: seed += b at the top of the bounce, PcgHash(seed) (no advance) for the
 // light, one PcgFloat for roulette and two for the new direction.
+#include <type_traits>
+
 #include "wavefront.h"
 #include "device_math.cuh"
 #include "bvh_traverse.cuh"
@@ -28,6 +30,9 @@ namespace {
 
 constexpr uint32_t kFull = 0xffffffffu;
 constexpr int kThreads = 256;
+
+// Nearest-hit structure a kernel instantiation is compiled for.
+enum : int { kIsGlobal = 0, kIsSmem = 1, kIsBvh = 2 };
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
@@ -66,6 +71,36 @@ __device__ __forceinline__ float3 primary_dir(const CameraView& cam, uint32_t x,
     return normalize3(mk3(dv[0], dv[1], dv[2]));
 }
 
+// Candidate bits of up to 32 spheres starting at base.  A sphere can only be
+// accepted when its discriminant is >= 0 (else the reference skips it) and its
+// half-b term is < 0: with b >= 0 the root -(b + sqrt(disc)) / a is <= 0 and
+// fails t > 0.  The bit is the sign of max(b, -disc), a superset of those
+// cases (disc is never -0, being b*b - a*c with b*b >= +0; max(b, -disc) = +0
+// only when b = +0, which is never accepted); candidates are then decided by
+// the exact test, so results equal the plain loop's.  The cheap pass has no
+// branches, which keeps the square root and the IEEE division out of the inner
+// loop.  Each sphere shifts its bit in from the right (one funnel shift), so
+// sphere base+k ends at bit 31-k: the highest set bit is the lowest index.
+template <bool SMEM, int CNT>
+__device__ __forceinline__ uint32_t candidate_bits(const float4* __restrict__ sph, uint32_t base, float3 o, float3 d,
+                                                   float a, uint32_t cnt)
+{
+    uint32_t mask = 0u;
+#pragma unroll
+    for (int k = 0; k < CNT; ++k) {
+        if (CNT == 32 || (uint32_t)k < cnt) {
+            const float4 s = SMEM ? sph[base + k] : __ldg(&sph[base + k]);
+            const float ox = o.x - s.x, oy = o.y - s.y, oz = o.z - s.z;
+            const float b = __fmaf_rn(oz, d.z, __fmaf_rn(oy, d.y, ox * d.x));
+            const float cc = __fmaf_rn(oz, oz, __fmaf_rn(oy, oy, __fmaf_rn(ox, ox, -s.w)));
+            const float disc = __fmaf_rn(b, b, -(a * cc));
+            mask = __funnelshift_l(__float_as_uint(fmaxf(b, -disc)), mask, 1);
+        }
+    }
+    if (CNT != 32) mask <<= (32u - cnt);   // align the first sphere to bit 31
+    return mask;
+}
+
 // Renderer.cu:256-279: brute-force nearest hit, lowest index on equal t.
 template <bool SMEM>
 __device__ __forceinline__ int32_t nearest_brute(const float4* __restrict__ sph, uint32_t n, float3 o, float3 d,
@@ -74,13 +109,19 @@ __device__ __forceinline__ int32_t nearest_brute(const float4* __restrict__ sph,
     const float a = dot3(d, d);
     int32_t best = -1;
     float tm = kFltMax;
-#pragma unroll 4
-    for (uint32_t i = 0; i < n; ++i) {
-        const float4 s = SMEM ? sph[i] : __ldg(&sph[i]);
-        float t;
-        if (sphere_t(s, o, d, a, t) && t > 0.0f && t < tm) {
-            tm = t;
-            best = (int32_t)i;
+    for (uint32_t base = 0; base < n; base += 32u) {
+        const uint32_t cnt = n - base;
+        uint32_t mask = cnt >= 32u ? candidate_bits<SMEM, 32>(sph, base, o, d, a, 32u)
+                                   : candidate_bits<SMEM, 31>(sph, base, o, d, a, cnt);
+        while (mask) {
+            const uint32_t k = (uint32_t)__clz(mask);   // lowest sphere index first (ties keep it)
+            mask &= ~(0x80000000u >> k);
+            const uint32_t i = base + k;
+            float t;
+            if (sphere_t(SMEM ? sph[i] : __ldg(&sph[i]), o, d, a, t) && t > 0.0f && t < tm) {
+                tm = t;
+                best = (int32_t)i;
+            }
         }
     }
     tmin = tm;
@@ -96,29 +137,35 @@ __device__ __forceinline__ bool occluded_brute(const float4* __restrict__ sph, u
                                                float dist2)
 {
     const float a = dot3(d, d);
-#pragma unroll 4
-    for (uint32_t i = 0; i < n; ++i) {
-        const float4 s = SMEM ? sph[i] : __ldg(&sph[i]);
-        float t;
-        if (sphere_t(s, o, d, a, t) && t > 0.0f && t * t < dist2) return true;
+    for (uint32_t base = 0; base < n; base += 32u) {
+        const uint32_t cnt = n - base;
+        uint32_t mask = cnt >= 32u ? candidate_bits<SMEM, 32>(sph, base, o, d, a, 32u)
+                                   : candidate_bits<SMEM, 31>(sph, base, o, d, a, cnt);
+        while (mask) {
+            const uint32_t k = (uint32_t)__clz(mask);
+            mask &= ~(0x80000000u >> k);
+            const uint32_t i = base + k;
+            float t;
+            if (sphere_t(SMEM ? sph[i] : __ldg(&sph[i]), o, d, a, t) && t > 0.0f && t * t < dist2) return true;
+        }
     }
     return false;
 }
 
-template <bool SMEM>
+template <int IS>
 __device__ __forceinline__ int32_t scene_nearest(const SceneView& sc, const float4* sph, float3 o, float3 d,
                                                  float& tmin)
 {
-    if (sc.use_bvh) return bvh_nearest(sc, o, d, tmin);
-    return nearest_brute<SMEM>(sph, sc.n_sph, o, d, tmin);
+    if (IS == kIsBvh) return bvh_nearest(sc, o, d, tmin);
+    return nearest_brute<IS == kIsSmem>(sph, sc.n_sph, o, d, tmin);
 }
 
-template <bool SMEM>
+template <int IS>
 __device__ __forceinline__ bool scene_occluded(const SceneView& sc, const float4* sph, float3 o, float3 d,
                                                float dist2)
 {
-    if (sc.use_bvh) return bvh_occluded(sc, o, d, dist2);
-    return occluded_brute<SMEM>(sph, sc.n_sph, o, d, dist2);
+    if (IS == kIsBvh) return bvh_occluded(sc, o, d, dist2);
+    return occluded_brute<IS == kIsSmem>(sph, sc.n_sph, o, d, dist2);
 }
 
 __device__ __forceinline__ void stage_spheres(const SceneView& sc, float4* s_sph)
@@ -128,9 +175,10 @@ __device__ __forceinline__ void stage_spheres(const SceneView& sc, float4* s_sph
 }
 
 // Primary nearest hit once per pixel of the wave (shared by its samples).
-template <bool SMEM>
+template <int IS>
 __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView cam, WaveState ws, WaveJob job)
 {
+    constexpr bool SMEM = IS == kIsSmem;
     extern __shared__ float4 s_sph[];
     const uint32_t n = job.n_pixels;
     if (blockIdx.x * blockDim.x >= n) return;
@@ -142,17 +190,18 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
         const uint32_t p = job.pixel0 + j;
         const float3 d = primary_dir(cam, p % cam.width, p / cam.width);
         float t;
-        const int32_t id = scene_nearest<SMEM>(sc, sph, o, d, t);
+        const int32_t id = scene_nearest<IS>(sc, sph, o, d, t);
         ws.prim[j] = make_uint2(__float_as_uint(t), (uint32_t)id);
     }
 }
 
 // SHARED (first bounce only): take the nearest hit from k_primary's per-pixel
 // record instead of tracing the primary ray again.
-template <bool FIRST, bool SMEM, bool SHARED>
-__global__ void __launch_bounds__(kThreads) k_extend(SceneView sc, CameraView cam, WaveState ws, WaveJob job,
-                                                     int bounce)
+template <bool FIRST, int IS, bool SHARED>
+__global__ void __launch_bounds__(kThreads, 4) k_extend(SceneView sc, CameraView cam, WaveState ws, WaveJob job,
+                                                        int bounce)
 {
+    constexpr bool SMEM = IS == kIsSmem;
     extern __shared__ float4 s_sph[];
     const uint32_t n = FIRST ? job.n_pixels * job.spp : ws.counters[2 * bounce];
     if (blockIdx.x * blockDim.x >= n) return;
@@ -199,7 +248,7 @@ __global__ void __launch_bounds__(kThreads) k_extend(SceneView sc, CameraView ca
                 tmin = __uint_as_float(pr.x);
                 hit = (int32_t)pr.y;
             } else {
-                hit = scene_nearest<SMEM>(sc, sph, o, d, tmin);
+                hit = scene_nearest<IS>(sc, sph, o, d, tmin);
             }
             bool touch = false;
             float3 add = mk3(0.f, 0.f, 0.f);
@@ -282,9 +331,10 @@ __global__ void __launch_bounds__(kThreads) k_extend(SceneView sc, CameraView ca
     }
 }
 
-template <bool SMEM>
+template <int IS>
 __global__ void __launch_bounds__(kThreads) k_shadow(SceneView sc, WaveState ws, int bounce)
 {
+    constexpr bool SMEM = IS == kIsSmem;
     extern __shared__ float4 s_sph[];
     const uint32_t n = ws.counters[2 * bounce + 1];
     if (blockIdx.x * blockDim.x >= n) return;
@@ -294,7 +344,7 @@ __global__ void __launch_bounds__(kThreads) k_shadow(SceneView sc, WaveState ws,
     for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += stride) {
         const float4 so = ws.sh_o[idx];
         const float4 sd = ws.sh_d[idx];
-        if (!scene_occluded<SMEM>(sc, sph, mk3(so.x, so.y, so.z), mk3(sd.x, sd.y, sd.z), so.w)) {
+        if (!scene_occluded<IS>(sc, sph, mk3(so.x, so.y, so.z), mk3(sd.x, sd.y, sd.z), so.w)) {
             const float4 c = ws.sh_c[idx];
             const uint32_t pid = __float_as_uint(sd.w);
             float4 col = ws.col[pid];
@@ -342,11 +392,12 @@ __global__ void k_clear(float4* p, uint64_t n)
         p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-template <bool SMEM>
+template <int IS>
 __global__ void __launch_bounds__(kThreads) k_trace(SceneView sc, const float* __restrict__ org,
                                                     const float* __restrict__ dir, uint64_t n, float* t_out,
                                                     int32_t* id_out)
 {
+    constexpr bool SMEM = IS == kIsSmem;
     extern __shared__ float4 s_sph[];
     if (SMEM) stage_spheres(sc, s_sph);
     const float4* sph = SMEM ? s_sph : sc.sph;
@@ -355,7 +406,7 @@ __global__ void __launch_bounds__(kThreads) k_trace(SceneView sc, const float* _
         const float3 o = mk3(org[3 * i], org[3 * i + 1], org[3 * i + 2]);
         const float3 d = mk3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
         float t;
-        const int32_t id = scene_nearest<SMEM>(sc, sph, o, d, t);
+        const int32_t id = scene_nearest<IS>(sc, sph, o, d, t);
         t_out[i] = id < 0 ? -1.0f : t;
         id_out[i] = id;
     }
@@ -375,9 +426,11 @@ __global__ void k_primary_dirs(CameraView cam, float* out)
 
 constexpr size_t kSmemSphereCap = 96 * 1024;  // 6144 spheres staged per CTA
 
-bool use_smem(const SceneView& sc)
+int isect_mode(const SceneView& sc)
 {
-    return !sc.use_bvh && (size_t)sc.n_sph * sizeof(float4) <= kSmemSphereCap && sc.n_sph > 0;
+    if (sc.use_bvh) return kIsBvh;
+    if (sc.n_sph > 0 && (size_t)sc.n_sph * sizeof(float4) <= kSmemSphereCap) return kIsSmem;
+    return kIsGlobal;
 }
 
 int grid_for(uint64_t n, int threads, int cap)
@@ -387,44 +440,53 @@ int grid_for(uint64_t n, int threads, int cap)
     return (int)(b < (uint64_t)cap ? b : (uint64_t)cap);
 }
 
+// Calls f with the intersection mode as a compile-time constant.
+template <class F>
+void with_mode(int mode, F&& f)
+{
+    if (mode == kIsSmem) f(std::integral_constant<int, kIsSmem>{});
+    else if (mode == kIsBvh) f(std::integral_constant<int, kIsBvh>{});
+    else f(std::integral_constant<int, kIsGlobal>{});
+}
+
+template <int IS>
+cudaError_t occupancy(int threads, size_t bytes, int* ext, int* sh, int* pr)
+{
+    if (bytes > 48 * 1024) {
+        const int b = (int)bytes;
+        const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+        cudaError_t e = cudaFuncSetAttribute(k_extend<true, IS, false>, a, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_extend<false, IS, false>, a, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_primary<IS>, a, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shadow<IS>, a, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace<IS>, a, b);
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ext, k_extend<false, IS, false>, threads, bytes);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(sh, k_shadow<IS>, threads, bytes);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(pr, k_primary<IS>, threads, bytes);
+    return e;
+}
+
 }  // namespace
 
 cudaError_t plan_launch(const SceneView& sc, int device, int threads, LaunchShape* out)
 {
-    if (threads <= 0) threads = kThreads;
-    if (threads > kThreads) threads = kThreads;
-    cudaDeviceProp prop;
-    cudaError_t e = cudaGetDeviceProperties(&prop, device);
+    if (threads <= 0 || threads > kThreads) threads = kThreads;
+    int sms = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) return e;
-    const bool smem = use_smem(sc);
-    const size_t bytes = smem ? (size_t)sc.n_sph * sizeof(float4) : 0;
-    int per_sm_ext = 0, per_sm_sh = 0;
-    if (smem) {
-        if (bytes > 48 * 1024) {
-            const int b = (int)bytes;
-            const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-            e = cudaFuncSetAttribute(k_extend<true, true, false>, a, b);
-            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_extend<false, true, false>, a, b);
-            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_primary<true>, a, b);
-            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shadow<true>, a, b);
-            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace<true>, a, b);
-            if (e != cudaSuccess) return e;
-        }
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, true, false>, threads, bytes);
-        if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<true>, threads, bytes);
-    } else {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, false, false>, threads, 0);
-        if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<false>, threads, 0);
-    }
+    const int mode = isect_mode(sc);
+    const size_t bytes = mode == kIsSmem ? (size_t)sc.n_sph * sizeof(float4) : 0;
+    int ext = 0, sh = 0, pr = 0;
+    with_mode(mode, [&](auto m) { e = occupancy<decltype(m)::value>(threads, bytes, &ext, &sh, &pr); });
     if (e != cudaSuccess) return e;
-    if (per_sm_ext < 1) per_sm_ext = 1;
-    if (per_sm_sh < 1) per_sm_sh = 1;
     out->threads = threads;
-    out->blocks_extend = prop.multiProcessorCount * per_sm_ext;
-    out->blocks_shadow = prop.multiProcessorCount * per_sm_sh;
+    out->blocks_extend = sms * (ext > 0 ? ext : 1);
+    out->blocks_shadow = sms * (sh > 0 ? sh : 1);
+    out->blocks_primary = sms * (pr > 0 ? pr : 1);
     out->smem_spheres = bytes;
+    out->mode = mode;
     return cudaSuccess;
 }
 
@@ -433,7 +495,6 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
                          uint32_t* launches, KernelTimer* timer)
 {
     uint32_t nl = 0;
-    const bool smem = shape.smem_spheres > 0;
     const size_t sm = shape.smem_spheres;
     const int bounces = job.max_bounces;
     const uint64_t paths = (uint64_t)job.n_pixels * job.spp;
@@ -444,45 +505,37 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
         if (e != cudaSuccess) return e;
         const int g0 = grid_for(paths, shape.threads, shape.blocks_extend);
         const bool share = job.spp > 1;
-        if (share) {
-            const int gp = grid_for(job.n_pixels, shape.threads, shape.blocks_extend);
-            begin(kFamExtend);
-            if (smem)
-                k_primary<true><<<gp, shape.threads, sm, stream>>>(sc, cam, ws, job);
-            else
-                k_primary<false><<<gp, shape.threads, 0, stream>>>(sc, cam, ws, job);
-            end(kFamExtend);
-            ++nl;
-        }
-        begin(kFamExtend);
-        if (share) {
-            // no sphere table needed: the nearest hit comes from k_primary
-            k_extend<true, false, true><<<g0, shape.threads, 0, stream>>>(sc, cam, ws, job, 0);
-        } else if (smem) {
-            k_extend<true, true, false><<<g0, shape.threads, sm, stream>>>(sc, cam, ws, job, 0);
-        } else {
-            k_extend<true, false, false><<<g0, shape.threads, 0, stream>>>(sc, cam, ws, job, 0);
-        }
-        end(kFamExtend);
-        ++nl;
-        for (int b = 0; b < bounces; ++b) {
-            if (b > 0) {
+        with_mode(shape.mode, [&](auto m) {
+            constexpr int IS = decltype(m)::value;
+            if (share) {
+                const int gp = grid_for(job.n_pixels, shape.threads, shape.blocks_primary);
                 begin(kFamExtend);
-                if (smem)
-                    k_extend<false, true, false><<<shape.blocks_extend, shape.threads, sm, stream>>>(sc, cam, ws, job, b);
-                else
-                    k_extend<false, false, false><<<shape.blocks_extend, shape.threads, 0, stream>>>(sc, cam, ws, job, b);
+                k_primary<IS><<<gp, shape.threads, sm, stream>>>(sc, cam, ws, job);
                 end(kFamExtend);
                 ++nl;
+                // no sphere table needed: the nearest hit comes from k_primary
+                begin(kFamExtend);
+                k_extend<true, kIsGlobal, true><<<g0, shape.threads, 0, stream>>>(sc, cam, ws, job, 0);
+                end(kFamExtend);
+            } else {
+                begin(kFamExtend);
+                k_extend<true, IS, false><<<g0, shape.threads, sm, stream>>>(sc, cam, ws, job, 0);
+                end(kFamExtend);
             }
-            begin(kFamShadow);
-            if (smem)
-                k_shadow<true><<<shape.blocks_shadow, shape.threads, sm, stream>>>(sc, ws, b);
-            else
-                k_shadow<false><<<shape.blocks_shadow, shape.threads, 0, stream>>>(sc, ws, b);
-            end(kFamShadow);
             ++nl;
-        }
+            for (int b = 0; b < bounces; ++b) {
+                if (b > 0) {
+                    begin(kFamExtend);
+                    k_extend<false, IS, false><<<shape.blocks_extend, shape.threads, sm, stream>>>(sc, cam, ws, job, b);
+                    end(kFamExtend);
+                    ++nl;
+                }
+                begin(kFamShadow);
+                k_shadow<IS><<<shape.blocks_shadow, shape.threads, sm, stream>>>(sc, ws, b);
+                end(kFamShadow);
+                ++nl;
+            }
+        });
     }
     begin(kFamAccumulate);
     k_accumulate<<<grid_for(job.n_pixels, kThreads, 4096), kThreads, 0, stream>>>(ws, job, accum, image);
@@ -503,16 +556,16 @@ cudaError_t enqueue_trace_nearest(const SceneView& sc, const float* origins, con
 {
     if (n == 0) return cudaSuccess;
     const int g = grid_for(n, kThreads, 4096);
-    if (use_smem(sc)) {
-        const size_t bytes = (size_t)sc.n_sph * sizeof(float4);
-        if (bytes > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(k_trace<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-            if (e != cudaSuccess) return e;
-        }
-        k_trace<true><<<g, kThreads, bytes, stream>>>(sc, origins, dirs, n, t_out, id_out);
-    } else {
-        k_trace<false><<<g, kThreads, 0, stream>>>(sc, origins, dirs, n, t_out, id_out);
-    }
+    const int mode = isect_mode(sc);
+    const size_t bytes = mode == kIsSmem ? (size_t)sc.n_sph * sizeof(float4) : 0;
+    cudaError_t e = cudaSuccess;
+    with_mode(mode, [&](auto m) {
+        constexpr int IS = decltype(m)::value;
+        if (bytes > 48 * 1024)
+            e = cudaFuncSetAttribute(k_trace<IS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e == cudaSuccess) k_trace<IS><<<g, kThreads, bytes, stream>>>(sc, origins, dirs, n, t_out, id_out);
+    });
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

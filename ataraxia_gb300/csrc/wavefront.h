@@ -123,8 +123,10 @@ public:
 struct LaunchShape {
     int blocks_extend;
     int blocks_shadow;
+    int blocks_primary;
     int threads;
     size_t smem_spheres;      // dynamic shared memory for the sphere table (0: read from global)
+    int mode;                 // nearest-hit structure: 0 brute force from global, 1 from shared memory, 2 LBVH
 };
 
 // Fills in grid sizes for this device and scene (occupancy-derived).

@@ -367,10 +367,11 @@ def run_render_only(args, dist: Dist):
     import ataraxia_gb300 as atx
     from ataraxia_gb300 import scenes
 
-    sc = scenes.config1()
+    sc = {"medium": scenes.config1, "large": scenes.config2, "small": scenes.config0}[args.workload]()
     if args.width and args.height:
         sc = sc.with_resolution(args.width, args.height)
-    r = atx.Renderer(device=dist.local_rank)
+    r = atx.Renderer(device=dist.local_rank, bvh_threshold=args.bvh_threshold, bvh_leaf_size=args.bvh_leaf,
+                     wave_paths=args.wave_paths)
     r.on_resize(sc.width, sc.height)
     r.set_scene(sc.spheres, sc.materials, sc.lights)
     r.set_camera(atx.Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction))
@@ -385,7 +386,8 @@ def run_render_only(args, dist: Dist):
     dt = time.perf_counter() - t0
     st = r.stats()
     r.close()
-    return {"mode": "render", "width": sc.width, "height": sc.height, "steps": args.steps,
+    return {"mode": "render", "workload": args.workload, "bvh": st["bvh_in_use"], "bvh_leaf": args.bvh_leaf,
+            "wave_paths": args.wave_paths, "width": sc.width, "height": sc.height, "steps": args.steps,
             "wall_ms_per_step": round(dt * 1e3 / args.steps, 3),
             "Mpaths_per_s_wall": round(args.steps * sc.pixels * sc.spp / dt / 1e6, 1),
             "kernel_launches": st["kernel_launches"]}
@@ -436,6 +438,12 @@ def main(argv=None) -> int:
                     help="render: only warm-up + timed launches of the workload (for profiler captures)")
     ap.add_argument("--width", type=int, default=0, help="render mode: override the viewport width")
     ap.add_argument("--height", type=int, default=0, help="render mode: override the viewport height")
+    ap.add_argument("--workload", choices=["medium", "large", "small"], default="medium",
+                    help="render mode: scene (small = 8+1 spheres 720p, medium = 256 spheres 1080p, "
+                         "large = 65,536 clustered spheres 4K)")
+    ap.add_argument("--bvh-threshold", type=int, default=0, help="render mode: LBVH from this sphere count (0 = default)")
+    ap.add_argument("--bvh-leaf", type=int, default=0, help="render mode: LBVH leaf size (0 = default)")
+    ap.add_argument("--wave-paths", type=int, default=0, help="render mode: paths per wave (0 = default)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         log("warmup raised to 3 (minimum)")

@@ -111,7 +111,7 @@ typedef struct atx_config {
 typedef struct atx_stats {
     uint64_t frames;           /* reference frames rendered (samples per pixel) since creation */
     uint64_t paths;            /* pixel-samples traced */
-    uint64_t extension_rays;   /* nearest-hit rays traced */
+    uint64_t extension_rays;   /* nearest-hit queries traced (a primary ray shared by a pixel's samples counts once) */
     uint64_t shadow_rays;      /* shadow rays traced */
     uint64_t kernel_launches;  /* kernels this renderer launched */
     uint64_t device_bytes;     /* device memory currently held */
