@@ -18,7 +18,7 @@ from . import _native as N
 from ._native import AtxError, LIGHT_DTYPE, MATERIAL_DTYPE, SPHERE_DTYPE
 
 __all__ = [
-    "AtxError", "Camera", "Light", "Material", "Renderer", "Scene", "Settings", "Sphere",
+    "AtxError", "Batch", "Camera", "Light", "Material", "Renderer", "Scene", "Settings", "Sphere",
     "SPHERE_DTYPE", "MATERIAL_DTYPE", "LIGHT_DTYPE", "camera_matrices", "device_count",
 ]
 
@@ -291,3 +291,103 @@ class Renderer:
         a, i = C.c_void_p(), C.c_void_p()
         N.check(N.lib().atx_device_buffers(self._h, C.byref(a), C.byref(i)))
         return a.value, i.value
+
+
+class Batch:
+    """Many scenes rendered together by one persistent kernel per pass (atx_batch_*).
+
+    add_scene(...) -> id; set_spp(id, spp); run() renders one pass for every scene with spp > 0.
+    Each scene keeps the reference's per-scene frame semantics, so its results are bit-identical to
+    rendering it alone with Renderer."""
+
+    def __init__(self, device: int = 0, bvh_threshold: int = 0, bvh_leaf_size: int = 0, hbm_budget_bytes: int = 0,
+                 flags: int = 0):
+        cfg = N.Config(device, 0, 0, bvh_threshold, bvh_leaf_size, flags, hbm_budget_bytes)
+        h = C.c_void_p()
+        N.check(N.lib().atx_batch_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self._sizes = {}
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().atx_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def add_scene(self, spheres, materials, lights, camera: Camera, width: int, height: int,
+                  settings: Settings = None) -> int:
+        settings = settings or Settings()
+        s, m, l = _as_spheres(spheres), _as_materials(materials), _as_lights(lights)
+        d = N.BatchScene(N.ptr(s) if len(s) else None, len(s), N.ptr(m) if len(m) else None, len(m),
+                         N.ptr(l) if len(l) else None, len(l), camera.desc(), width, height,
+                         N.Settings(int(bool(settings.accumulation)), int(bool(settings.skyLight)),
+                                    (C.c_uint8 * 2)(), int(settings.maxBounces)))
+        i = C.c_uint32()
+        N.check(N.lib().atx_batch_add_scene(self._h, C.byref(d), C.byref(i)))
+        self._sizes[i.value] = (width, height)
+        return i.value
+
+    def add_synthetic(self, sc, settings: Settings = None) -> int:
+        """Adds a scenes.SyntheticScene with its own camera and bounce depth."""
+        cam = Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction)
+        st = settings or Settings(accumulation=True, skyLight=sc.sky_light, maxBounces=sc.max_bounces)
+        return self.add_scene(sc.spheres, sc.materials, sc.lights, cam, sc.width, sc.height, st)
+
+    def remove_scene(self, i: int):
+        N.check(N.lib().atx_batch_remove_scene(self._h, i))
+        self._sizes.pop(i, None)
+
+    def set_spp(self, i: int, spp: int):
+        N.check(N.lib().atx_batch_set_spp(self._h, i, spp))
+
+    def reset(self, i: int):
+        N.check(N.lib().atx_batch_reset(self._h, i))
+
+    def frame_index(self, i: int) -> int:
+        f = C.c_uint32()
+        N.check(N.lib().atx_batch_frame_index(self._h, i, C.byref(f)))
+        return f.value
+
+    def run(self):
+        N.check(N.lib().atx_batch_run(self._h))
+
+    def synchronize(self):
+        N.check(N.lib().atx_batch_synchronize(self._h))
+
+    def get_accumulation(self, i: int) -> np.ndarray:
+        w, h = self._sizes[i]
+        out = np.empty((h * w, 4), dtype=np.float32)
+        N.check(N.lib().atx_batch_read_accumulation(self._h, i, N.ptr(out), w * h))
+        return out
+
+    def get_image(self, i: int) -> np.ndarray:
+        w, h = self._sizes[i]
+        out = np.empty(h * w, dtype=np.uint32)
+        N.check(N.lib().atx_batch_read_image(self._h, i, N.ptr(out), w * h))
+        return out
+
+    def stats(self) -> dict:
+        s = N.BatchStats()
+        N.check(N.lib().atx_batch_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in N.BatchStats._fields_}
+
+    def set_tuning(self, tile_w=0, tile_h=0, threads=0, bvh_threshold=0, bvh_leaf_size=0):
+        t = N.BatchTuning(tile_w, tile_h, threads, bvh_threshold, bvh_leaf_size, (C.c_uint32 * 3)())
+        N.check(N.lib().atx_batch_set_tuning(self._h, C.byref(t)))
+
+    def tuning(self) -> dict:
+        t = N.BatchTuning()
+        N.check(N.lib().atx_batch_get_tuning(self._h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in N.BatchTuning._fields_ if k != "reserved"}

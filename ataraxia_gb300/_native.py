@@ -64,6 +64,24 @@ class KernelTimes(C.Structure):
                 ("accumulate_launches", C.c_uint64), ("other_launches", C.c_uint64)]
 
 
+class BatchScene(C.Structure):
+    _fields_ = [("spheres", C.c_void_p), ("n_spheres", C.c_uint32), ("materials", C.c_void_p),
+                ("n_materials", C.c_uint32), ("lights", C.c_void_p), ("n_lights", C.c_uint32),
+                ("camera", CameraDesc), ("width", C.c_uint32), ("height", C.c_uint32), ("settings", Settings)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("passes", C.c_uint64), ("paths", C.c_uint64), ("extension_rays", C.c_uint64),
+                ("shadow_rays", C.c_uint64), ("kernel_launches", C.c_uint64), ("graph_launches", C.c_uint64),
+                ("device_bytes", C.c_uint64), ("last_pass_ms", C.c_double), ("scenes", C.c_uint32),
+                ("items_last_pass", C.c_uint32)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("threads", C.c_uint32),
+                ("bvh_threshold", C.c_uint32), ("bvh_leaf_size", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+
+
 FLAG_NO_GRAPHS = 1
 FLAG_PROFILE_KERNELS = 2
 
@@ -104,6 +122,20 @@ SIGNATURES = {
     "atx_host_alloc": (_ST, [_U64, C.POINTER(_P)]),
     "atx_host_free": (_ST, [_P]),
     "atx_camera_matrices": (_ST, [C.POINTER(CameraDesc), _U32, _U32, _P, _P, _P, _P]),
+    "atx_batch_create": (_ST, [C.POINTER(Config), C.POINTER(_P)]),
+    "atx_batch_destroy": (_ST, [_P]),
+    "atx_batch_add_scene": (_ST, [_P, C.POINTER(BatchScene), C.POINTER(C.c_uint32)]),
+    "atx_batch_remove_scene": (_ST, [_P, _U32]),
+    "atx_batch_set_spp": (_ST, [_P, _U32, _U32]),
+    "atx_batch_reset": (_ST, [_P, _U32]),
+    "atx_batch_frame_index": (_ST, [_P, _U32, C.POINTER(C.c_uint32)]),
+    "atx_batch_run": (_ST, [_P]),
+    "atx_batch_synchronize": (_ST, [_P]),
+    "atx_batch_read_accumulation": (_ST, [_P, _U32, _P, _U64]),
+    "atx_batch_read_image": (_ST, [_P, _U32, _P, _U64]),
+    "atx_batch_get_stats": (_ST, [_P, C.POINTER(BatchStats)]),
+    "atx_batch_set_tuning": (_ST, [_P, C.POINTER(BatchTuning)]),
+    "atx_batch_get_tuning": (_ST, [_P, C.POINTER(BatchTuning)]),
     "atx_render_noalloc": (_ST, [_P, _U32, _P, _U32, _P, _U32, _P, _P, _P, _U32, _U32, C.POINTER(Settings), _U32,
                                  _U32, _P, _P, _P]),
     "atx_trace_nearest": (_ST, [_P, _P, _P, _U64, _P, _P]),

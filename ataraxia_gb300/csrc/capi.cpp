@@ -280,3 +280,123 @@ ATX_API atx_status atx_primary_directions(atx_renderer* r, float* host_dirs, uin
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ batches
+
+#include "batch_host.h"
+
+struct atx_batch {
+    atx::Batch impl;
+    explicit atx_batch(const atx_config& c) : impl(c) {}
+};
+
+#define NEEDB(b) \
+    if (!(b)) return atx::fail(ATX_ERR_INVALID_ARG, "%s: null batch", __func__)
+
+extern "C" {
+
+ATX_API atx_status atx_batch_create(const atx_config* config, atx_batch** out)
+{
+    return guarded([&]() -> atx_status {
+        if (!out) return atx::fail(ATX_ERR_INVALID_ARG, "atx_batch_create: null out");
+        *out = nullptr;
+        atx_config c{};
+        if (config) c = *config;
+        atx_batch* b = new atx_batch(c);
+        atx_status st = b->impl.init();
+        if (st != ATX_OK) {
+            delete b;
+            return st;
+        }
+        *out = b;
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_batch_destroy(atx_batch* b)
+{
+    return guarded([&]() -> atx_status { delete b; return ATX_OK; });
+}
+
+ATX_API atx_status atx_batch_add_scene(atx_batch* b, const atx_batch_scene* scene, uint32_t* id)
+{
+    return guarded([&]() -> atx_status {
+        NEEDB(b);
+        if (!scene || !id) return atx::fail(ATX_ERR_INVALID_ARG, "atx_batch_add_scene: null argument");
+        return b->impl.add_scene(*scene, id);
+    });
+}
+
+ATX_API atx_status atx_batch_remove_scene(atx_batch* b, uint32_t id)
+{
+    return guarded([&]() -> atx_status { NEEDB(b); return b->impl.remove_scene(id); });
+}
+
+ATX_API atx_status atx_batch_set_spp(atx_batch* b, uint32_t id, uint32_t spp)
+{
+    return guarded([&]() -> atx_status { NEEDB(b); return b->impl.set_spp(id, spp); });
+}
+
+ATX_API atx_status atx_batch_reset(atx_batch* b, uint32_t id)
+{
+    return guarded([&]() -> atx_status { NEEDB(b); return b->impl.reset(id); });
+}
+
+ATX_API atx_status atx_batch_frame_index(atx_batch* b, uint32_t id, uint32_t* f)
+{
+    return guarded([&]() -> atx_status {
+        NEEDB(b);
+        if (!f) return atx::fail(ATX_ERR_INVALID_ARG, "atx_batch_frame_index: null pointer");
+        return b->impl.frame_index(id, f);
+    });
+}
+
+ATX_API atx_status atx_batch_run(atx_batch* b)
+{
+    return guarded([&]() -> atx_status { NEEDB(b); return b->impl.run(); });
+}
+
+ATX_API atx_status atx_batch_synchronize(atx_batch* b)
+{
+    return guarded([&]() -> atx_status { NEEDB(b); return b->impl.synchronize(); });
+}
+
+ATX_API atx_status atx_batch_read_accumulation(atx_batch* b, uint32_t id, float* host, uint64_t n)
+{
+    return guarded([&]() -> atx_status { NEEDB(b); return b->impl.read_accumulation(id, host, n); });
+}
+
+ATX_API atx_status atx_batch_read_image(atx_batch* b, uint32_t id, uint32_t* host, uint64_t n)
+{
+    return guarded([&]() -> atx_status { NEEDB(b); return b->impl.read_image(id, host, n); });
+}
+
+ATX_API atx_status atx_batch_get_stats(atx_batch* b, atx_batch_stats* s)
+{
+    return guarded([&]() -> atx_status {
+        NEEDB(b);
+        if (!s) return atx::fail(ATX_ERR_INVALID_ARG, "atx_batch_get_stats: null pointer");
+        return b->impl.stats(s);
+    });
+}
+
+ATX_API atx_status atx_batch_set_tuning(atx_batch* b, const atx_batch_tuning* t)
+{
+    return guarded([&]() -> atx_status {
+        NEEDB(b);
+        if (!t) return atx::fail(ATX_ERR_INVALID_ARG, "atx_batch_set_tuning: null pointer");
+        return b->impl.set_tuning(*t);
+    });
+}
+
+ATX_API atx_status atx_batch_get_tuning(atx_batch* b, atx_batch_tuning* t)
+{
+    return guarded([&]() -> atx_status {
+        NEEDB(b);
+        if (!t) return atx::fail(ATX_ERR_INVALID_ARG, "atx_batch_get_tuning: null pointer");
+        *t = b->impl.tuning();
+        return ATX_OK;
+    });
+}
+
+}  // extern "C"

@@ -253,50 +253,83 @@ __global__ void k_refit(int n, float4* node_ctr, float4* node_half, const uint32
 
 }  // namespace
 
+namespace {
+
+// The scratch block's parts.  carve() both measures (base == nullptr) and
+// assigns, so the size lbvh_bytes reports and the layout lbvh_build uses
+// cannot disagree.
+struct Parts {
+    float4* node_ctr;
+    float4* node_half;
+    uint2* range;
+    float4* leaf_sph;
+    uint32_t* leaf_id;
+    uint32_t *k0, *v0, *k1, *v1;
+    uint32_t* parent;
+    uint32_t* visits;
+    uint32_t* counts;
+    unsigned* bounds;
+};
+
+uint64_t carve(char* base, uint32_t n, Parts* q)
+{
+    uint64_t off = 0;
+    auto take = [&](uint64_t bytes) -> void* {
+        void* r = base ? static_cast<void*>(base + off) : nullptr;
+        off += (bytes + 255) & ~uint64_t(255);
+        return r;
+    };
+    const uint64_t nn = n;
+    const uint64_t blocks = (nn + kTile - 1) / kTile;
+    q->node_ctr = static_cast<float4*>(take(2 * nn * sizeof(float4)));
+    q->node_half = static_cast<float4*>(take(2 * nn * sizeof(float4)));
+    q->range = static_cast<uint2*>(take(nn * sizeof(uint2)));
+    q->leaf_sph = static_cast<float4*>(take(nn * sizeof(float4)));
+    q->leaf_id = static_cast<uint32_t*>(take(nn * sizeof(uint32_t)));
+    q->k0 = static_cast<uint32_t*>(take(nn * sizeof(uint32_t)));
+    q->v0 = static_cast<uint32_t*>(take(nn * sizeof(uint32_t)));
+    q->k1 = static_cast<uint32_t*>(take(nn * sizeof(uint32_t)));
+    q->v1 = static_cast<uint32_t*>(take(nn * sizeof(uint32_t)));
+    q->parent = static_cast<uint32_t*>(take(2 * nn * sizeof(uint32_t)));   // indexed by node, 2n-1 nodes
+    q->visits = static_cast<uint32_t*>(take(nn * sizeof(uint32_t)));
+    q->counts = static_cast<uint32_t*>(take(256 * blocks * sizeof(uint32_t)));
+    q->bounds = static_cast<unsigned*>(take(6 * sizeof(unsigned)));
+    return off;
+}
+
+__global__ void k_init_bounds(unsigned* bounds)
+{
+    if (threadIdx.x < 6) bounds[threadIdx.x] = threadIdx.x < 3 ? 0xffffffffu : 0u;
+}
+
+}  // namespace
+
 uint64_t lbvh_bytes(uint32_t n)
 {
-    const uint64_t nn = n ? n : 1;
-    const uint64_t blocks = (nn + kTile - 1) / kTile;
-    uint64_t b = 0;
-    b += 2 * (2 * nn) * sizeof(float4);   // node_ctr, node_half
-    b += nn * sizeof(uint2);              // ranges
-    b += nn * sizeof(float4);             // leaf_sph
-    b += nn * sizeof(uint32_t);           // leaf_id
-    b += 4 * nn * sizeof(uint32_t);       // keys/vals ping-pong
-    b += 2 * nn * sizeof(uint32_t);       // parent + visits
-    b += 256 * blocks * sizeof(uint32_t); // counts
-    b += 64;                              // bounds
-    b += 16 * 256;                        // alignment slack
-    return b;
+    Parts q;
+    return carve(nullptr, n ? n : 1, &q);
 }
 
 cudaError_t lbvh_build(const float4* sph, const float* radius, uint32_t n, uint32_t leaf_size, void* scratch,
                        uint64_t scratch_bytes, BvhView* out, cudaStream_t stream)
 {
     if (n == 0 || scratch_bytes < lbvh_bytes(n)) return cudaErrorInvalidValue;
-    char* p = static_cast<char*>(scratch);
-    auto take = [&](uint64_t bytes) {
-        char* r = p;
-        p += (bytes + 255) & ~uint64_t(255);
-        return static_cast<void*>(r);
-    };
+    Parts q;
+    carve(static_cast<char*>(scratch), n, &q);
     const uint32_t blocks = (n + kTile - 1) / kTile;
-    float4* node_ctr = static_cast<float4*>(take(2ull * n * sizeof(float4)));
-    float4* node_half = static_cast<float4*>(take(2ull * n * sizeof(float4)));
-    uint2* range = static_cast<uint2*>(take((uint64_t)n * sizeof(uint2)));
-    float4* leaf_sph = static_cast<float4*>(take((uint64_t)n * sizeof(float4)));
-    uint32_t* leaf_id = static_cast<uint32_t*>(take((uint64_t)n * sizeof(uint32_t)));
-    uint32_t* k0 = static_cast<uint32_t*>(take((uint64_t)n * 4));
-    uint32_t* v0 = static_cast<uint32_t*>(take((uint64_t)n * 4));
-    uint32_t* k1 = static_cast<uint32_t*>(take((uint64_t)n * 4));
-    uint32_t* v1 = static_cast<uint32_t*>(take((uint64_t)n * 4));
-    uint32_t* parent = static_cast<uint32_t*>(take((uint64_t)n * 2 * 4));
-    uint32_t* visits = static_cast<uint32_t*>(take((uint64_t)n * 4));
-    uint32_t* counts = static_cast<uint32_t*>(take(256ull * blocks * 4));
-    unsigned* bounds = static_cast<unsigned*>(take(64));
+    float4* node_ctr = q.node_ctr;
+    float4* node_half = q.node_half;
+    uint2* range = q.range;
+    float4* leaf_sph = q.leaf_sph;
+    uint32_t* leaf_id = q.leaf_id;
+    uint32_t *k0 = q.k0, *v0 = q.v0, *k1 = q.k1, *v1 = q.v1;
+    uint32_t* parent = q.parent;
+    uint32_t* visits = q.visits;
+    uint32_t* counts = q.counts;
+    unsigned* bounds = q.bounds;
 
-    const unsigned init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
-    cudaError_t e = cudaMemcpyAsync(bounds, init, sizeof(init), cudaMemcpyHostToDevice, stream);
+    k_init_bounds<<<1, 32, 0, stream>>>(bounds);
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(visits, 0, (size_t)n * 4, stream);
     if (e != cudaSuccess) return e;

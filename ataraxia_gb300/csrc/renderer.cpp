@@ -11,7 +11,7 @@
 namespace atx {
 
 namespace {
-constexpr uint32_t kDefaultWavePaths = 16u << 20;  // 16 Mi paths, ~2.2 GB of state
+constexpr uint32_t kDefaultWavePaths = 64u << 20;  // at most 64 Mi paths (8.7 GB of state) per wave
 constexpr uint32_t kDefaultBvhThreshold = 1024;
 constexpr uint32_t kDefaultBvhLeaf = 2;
 constexpr uint32_t kMaxBounces = 4096;
@@ -363,7 +363,13 @@ atx_status Renderer::render(uint32_t spp)
     ATX_TRY(activate());
     ATX_TRY(refresh_camera());
     ATX_TRY(ensure_shape());
-    const uint32_t capacity = cfg_.wave_paths ? cfg_.wave_paths : kDefaultWavePaths;
+    // One wave per launch when it fits: fewer, fuller kernels (the state is
+    // allocated for this launch's paths, rounded up to 1 Mi, and kept).
+    uint32_t capacity = cfg_.wave_paths;
+    if (!capacity) {
+        const uint64_t want = ((uint64_t)width_ * height_ * spp + (1u << 20) - 1) & ~uint64_t((1u << 20) - 1);
+        capacity = (uint32_t)std::min<uint64_t>(want, kDefaultWavePaths);
+    }
     const int32_t bounces = settings_.max_bounces;
     ATX_TRY(wave_.ensure(capacity, bounces > 0 ? (uint32_t)bounces : 0u, &budget_));
     wave_.view.totals = totals_.as<unsigned long long>();

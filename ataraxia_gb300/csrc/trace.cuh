@@ -1,0 +1,142 @@
+// Device-side tracing shared by the wavefront kernels (wavefront.cu) and the
+// batched persistent kernel (batch.cu): primary directions, the brute-force
+// nearest / any hit over a sphere table and their dispatch to the LBVH.
+#pragma once
+
+#include <cstdint>
+
+#include "bvh_traverse.cuh"
+#include "device_math.cuh"
+#include "wavefront.h"
+
+namespace atx {
+
+// Nearest-hit structure a kernel instantiation is compiled for.
+enum : int { kIsGlobal = 0, kIsSmem = 1, kIsBvh = 2 };
+
+// Camera.cpp:173-187 for pixel (x, y): NDC without a pixel-centre offset, y = 0
+// the bottom row; target = invProj * (cx, cy, 1, 1); direction =
+// normalize(invView * (normalize(target.xyz / target.w), 0)).
+__device__ __forceinline__ float3 primary_dir(const CameraView& cam, uint32_t x, uint32_t y)
+{
+    const float qx = __uint2float_rn(x) / __uint2float_rn(cam.width);
+    const float qy = __uint2float_rn(y) / __uint2float_rn(cam.height);
+    const float cx = qx * 2.0f - 1.0f;
+    const float cy = qy * 2.0f - 1.0f;
+    float t[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+        t[r] = (cam.inv_proj[r] * cx + cam.inv_proj[4 + r] * cy) + (cam.inv_proj[8 + r] + cam.inv_proj[12 + r]);
+    const float3 tv = normalize3(mk3(t[0] / t[3], t[1] / t[3], t[2] / t[3]));
+    float dv[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+        dv[r] = (cam.inv_view[r] * tv.x + cam.inv_view[4 + r] * tv.y) + cam.inv_view[8 + r] * tv.z;
+    return normalize3(mk3(dv[0], dv[1], dv[2]));
+}
+
+// Candidate bits of up to 32 spheres starting at base.  A sphere can only be
+// accepted when its discriminant is >= 0 (else the reference skips it) and its
+// half-b term is < 0: with b >= 0 the root -(b + sqrt(disc)) / a is <= 0 and
+// fails t > 0.  The bit is the sign of max(b, -disc), a superset of those
+// cases (disc is never -0, being b*b - a*c with b*b >= +0; max(b, -disc) = +0
+// only when b = +0, which is never accepted); candidates are then decided by
+// the exact test, so results equal the plain loop's.  The cheap pass has no
+// branches, which keeps the square root and the IEEE division out of the inner
+// loop.  Each sphere shifts its bit in from the right (one funnel shift), so
+// sphere base+k ends at bit 31-k: the highest set bit is the lowest index.
+template <bool SMEM, int CNT>
+__device__ __forceinline__ uint32_t candidate_bits(const float4* __restrict__ sph, uint32_t base, float3 o, float3 d,
+                                                   float a, uint32_t cnt)
+{
+    uint32_t mask = 0u;
+#pragma unroll
+    for (int k = 0; k < CNT; ++k) {
+        if (CNT == 32 || (uint32_t)k < cnt) {
+            const float4 s = SMEM ? sph[base + k] : __ldg(&sph[base + k]);
+            const float ox = o.x - s.x, oy = o.y - s.y, oz = o.z - s.z;
+            const float b = __fmaf_rn(oz, d.z, __fmaf_rn(oy, d.y, ox * d.x));
+            const float cc = __fmaf_rn(oz, oz, __fmaf_rn(oy, oy, __fmaf_rn(ox, ox, -s.w)));
+            const float disc = __fmaf_rn(b, b, -(a * cc));
+            mask = __funnelshift_l(__float_as_uint(fmaxf(b, -disc)), mask, 1);
+        }
+    }
+    if (CNT != 32) mask <<= (32u - cnt);   // align the first sphere to bit 31
+    return mask;
+}
+
+// Renderer.cu:256-279: brute-force nearest hit, lowest index on equal t.
+template <bool SMEM>
+__device__ __forceinline__ int32_t nearest_brute(const float4* __restrict__ sph, uint32_t n, float3 o, float3 d,
+                                                 float& tmin)
+{
+    const float a = dot3(d, d);
+    int32_t best = -1;
+    float tm = kFltMax;
+    for (uint32_t base = 0; base < n; base += 32u) {
+        const uint32_t cnt = n - base;
+        uint32_t mask = cnt >= 32u ? candidate_bits<SMEM, 32>(sph, base, o, d, a, 32u)
+                                   : candidate_bits<SMEM, 31>(sph, base, o, d, a, cnt);
+        while (mask) {
+            const uint32_t k = (uint32_t)__clz(mask);   // lowest sphere index first (ties keep it)
+            mask &= ~(0x80000000u >> k);
+            const uint32_t i = base + k;
+            float t;
+            if (sphere_t(SMEM ? sph[i] : __ldg(&sph[i]), o, d, a, t) && t > 0.0f && t < tm) {
+                tm = t;
+                best = (int32_t)i;
+            }
+        }
+    }
+    tmin = tm;
+    return best;
+}
+
+// Renderer.cu:351-352 as an any-hit query.  The reference takes the nearest
+// hit and tests t > 0 && t*t < dist2; since the nearest accepted t is <= every
+// accepted t and squaring is monotone, that equals "some sphere has t > 0 and
+// t*t < dist2", so the loop can stop at the first such sphere.
+template <bool SMEM>
+__device__ __forceinline__ bool occluded_brute(const float4* __restrict__ sph, uint32_t n, float3 o, float3 d,
+                                               float dist2)
+{
+    const float a = dot3(d, d);
+    for (uint32_t base = 0; base < n; base += 32u) {
+        const uint32_t cnt = n - base;
+        uint32_t mask = cnt >= 32u ? candidate_bits<SMEM, 32>(sph, base, o, d, a, 32u)
+                                   : candidate_bits<SMEM, 31>(sph, base, o, d, a, cnt);
+        while (mask) {
+            const uint32_t k = (uint32_t)__clz(mask);
+            mask &= ~(0x80000000u >> k);
+            const uint32_t i = base + k;
+            float t;
+            if (sphere_t(SMEM ? sph[i] : __ldg(&sph[i]), o, d, a, t) && t > 0.0f && t * t < dist2) return true;
+        }
+    }
+    return false;
+}
+
+template <int IS>
+__device__ __forceinline__ int32_t scene_nearest(const SceneView& sc, const float4* sph, float3 o, float3 d,
+                                                 float& tmin)
+{
+    if (IS == kIsBvh) return bvh_nearest(sc, o, d, tmin);
+    return nearest_brute<IS == kIsSmem>(sph, sc.n_sph, o, d, tmin);
+}
+
+template <int IS>
+__device__ __forceinline__ bool scene_occluded(const SceneView& sc, const float4* sph, float3 o, float3 d,
+                                               float dist2)
+{
+    if (IS == kIsBvh) return bvh_occluded(sc, o, d, dist2);
+    return occluded_brute<IS == kIsSmem>(sph, sc.n_sph, o, d, dist2);
+}
+
+__device__ __forceinline__ void stage_spheres(const SceneView& sc, float4* s_sph)
+{
+    for (uint32_t i = threadIdx.x; i < sc.n_sph; i += blockDim.x) s_sph[i] = __ldg(&sc.sph[i]);
+    __syncthreads();
+}
+
+
+}  // namespace atx

@@ -362,6 +362,71 @@ def time_reference_kernel(sc, cam, dev, args) -> dict:
                     "and image copy"}
 
 
+def run_batch_compare(args, dist: Dist):
+    """The batched mix (64 scenes, seed 3): the plain wavefront renderer launched once per scene (device
+    time of the render calls only) against one persistent batched pass per step."""
+    import torch
+
+    import ataraxia_gb300 as atx
+    from ataraxia_gb300 import scenes
+
+    dev = dist.local_rank
+    torch.cuda.set_device(dev)
+    mix = scenes.config3(count=args.mix_scenes)
+    paths = sum(s.width * s.height * s.spp for s in mix)
+
+    # plain: one renderer, one launch per scene
+    r = atx.Renderer(device=dev)
+    stream = torch.cuda.ExternalStream(r.stream, device=dev)
+    plain_ms = 0.0
+    for rep in range(2):                       # rep 0 warms up (allocations, BVH builds)
+        for sc in mix:
+            r.on_resize(sc.width, sc.height)
+            r.set_scene(sc.spheres, sc.materials, sc.lights)
+            r.set_camera(atx.Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction))
+            r.set_settings(atx.Settings(True, sc.sky_light, sc.max_bounces))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r.render_frames(sc.spp)
+            e1.record(stream)
+            e1.synchronize()
+            if rep == 1:
+                plain_ms += e0.elapsed_time(e1)
+    r.close()
+
+    b = atx.Batch(device=dev)
+    if args.tile:
+        tw, th = (int(x) for x in args.tile.split("x"))
+        b.set_tuning(tile_w=tw, tile_h=th)
+    ids = [b.add_synthetic(sc) for sc in mix]
+    for i, sc in zip(ids, mix):
+        b.set_spp(i, sc.spp)
+    for _ in range(args.warmup):
+        b.run()
+    b.synchronize()
+    s0 = b.stats()
+    t0 = time.perf_counter()
+    pass_ms = []
+    for _ in range(args.steps):
+        b.run()
+        b.synchronize()
+        pass_ms.append(b.stats()["last_pass_ms"])
+    wall = time.perf_counter() - t0
+    s1 = b.stats()
+    tun = b.tuning()
+    b.close()
+    batched_ms = statistics.mean(pass_ms)
+    return {"mode": "batch", "scenes": len(mix), "paths_per_pass": paths,
+            "plain_ms_per_pass": round(plain_ms, 3), "plain_mpaths_s": round(paths / (plain_ms * 1e-3) / 1e6, 1),
+            "batched_ms_per_pass": round(batched_ms, 3),
+            "batched_mpaths_s": round(paths / (batched_ms * 1e-3) / 1e6, 1),
+            "batched_wall_mpaths_s": round(args.steps * paths / wall / 1e6, 1),
+            "speedup": round(plain_ms / batched_ms, 3), "graph_launches": s1["graph_launches"] - s0["graph_launches"],
+            "rays_per_path": round(((s1["extension_rays"] - s0["extension_rays"]) +
+                                    (s1["shadow_rays"] - s0["shadow_rays"])) / (args.steps * paths), 3),
+            "tuning": tun}
+
+
 def run_render_only(args, dist: Dist):
     """Warm-up and timed launches of the workload, nothing else (profiler captures)."""
     import ataraxia_gb300 as atx
@@ -434,8 +499,11 @@ def main(argv=None) -> int:
     ap.add_argument("--no-ref-kernel", action="store_true", help="skip timing the restated reference kernel")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=3.0)
-    ap.add_argument("--mode", choices=["full", "render"], default="full",
-                    help="render: only warm-up + timed launches of the workload (for profiler captures)")
+    ap.add_argument("--mode", choices=["full", "render", "batch"], default="full",
+                    help="render: only warm-up + timed launches of the workload (for profiler captures); "
+                         "batch: the 64-scene mix, plain renderer per scene vs one batched pass")
+    ap.add_argument("--mix-scenes", type=int, default=64, help="batch mode: scenes in the mix")
+    ap.add_argument("--tile", default="", help="batch mode: work-item tile WxH (default from the library)")
     ap.add_argument("--width", type=int, default=0, help="render mode: override the viewport width")
     ap.add_argument("--height", type=int, default=0, help="render mode: override the viewport height")
     ap.add_argument("--workload", choices=["medium", "large", "small"], default="medium",
@@ -453,6 +521,8 @@ def main(argv=None) -> int:
     try:
         if args.mode == "render":
             out = run_render_only(args, dist)
+        elif args.mode == "batch":
+            out = run_batch_compare(args, dist)
         elif args.impl == "reference":
             if dist.rank != 0:
                 return 0

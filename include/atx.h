@@ -216,6 +216,68 @@ ATX_API atx_status atx_measure_fp32_peak(int32_t device, double* tflops);
 ATX_API atx_status atx_host_alloc(uint64_t bytes, void** out);
 ATX_API atx_status atx_host_free(void* p);
 
+/* ---------------------------------------------------------------- batches */
+
+/* Many scenes rendered together by one persistent kernel per pass.  No
+ * counterpart in the reference, which renders one scene per kernelRender
+ * launch (Renderer.cu:223); each scene keeps the reference's per-scene
+ * semantics (frame index, accumulate/reset, seed = pixel * frame), so a
+ * scene's images are bit-identical to rendering it alone with atx_render. */
+typedef struct atx_batch atx_batch;
+
+typedef struct atx_batch_scene {
+    const atx_sphere* spheres;
+    uint32_t n_spheres;
+    const atx_material* materials;
+    uint32_t n_materials;
+    const atx_light* lights;
+    uint32_t n_lights;
+    atx_camera camera;          /* matrices computed as Camera.cpp:134-159 for width x height */
+    uint32_t width, height;
+    atx_settings settings;      /* Scene.h:49-56 */
+} atx_batch_scene;
+
+typedef struct atx_batch_stats {
+    uint64_t passes;            /* atx_batch_run calls */
+    uint64_t paths;             /* pixel-samples traced */
+    uint64_t extension_rays;    /* nearest-hit queries */
+    uint64_t shadow_rays;
+    uint64_t kernel_launches;
+    uint64_t graph_launches;    /* passes replayed from a captured CUDA graph */
+    uint64_t device_bytes;
+    double last_pass_ms;        /* device time of the last pass */
+    uint32_t scenes;            /* scenes held */
+    uint32_t items_last_pass;   /* (scene, tile) work items of the last pass */
+} atx_batch_stats;
+
+/* Tuning knobs of the persistent kernel (0 = default / autotuned). */
+typedef struct atx_batch_tuning {
+    uint32_t tile_w, tile_h;    /* pixels per work item */
+    uint32_t threads;           /* threads per CTA */
+    uint32_t bvh_threshold;     /* sphere count from which a scene uses its LBVH */
+    uint32_t bvh_leaf_size;
+    uint32_t reserved[3];
+} atx_batch_tuning;
+
+ATX_API atx_status atx_batch_create(const atx_config* config, atx_batch** out);
+ATX_API atx_status atx_batch_destroy(atx_batch* b);
+/* Uploads a scene (arrays copied) and allocates its accumulator and image;
+ * its frame index starts at 1. */
+ATX_API atx_status atx_batch_add_scene(atx_batch* b, const atx_batch_scene* scene, uint32_t* id);
+ATX_API atx_status atx_batch_remove_scene(atx_batch* b, uint32_t id);
+/* Frames of this scene in the next pass (0 = idle). */
+ATX_API atx_status atx_batch_set_spp(atx_batch* b, uint32_t id, uint32_t spp);
+ATX_API atx_status atx_batch_reset(atx_batch* b, uint32_t id);
+ATX_API atx_status atx_batch_frame_index(atx_batch* b, uint32_t id, uint32_t* frame_index);
+/* One pass: every scene with spp > 0 renders its frames; asynchronous. */
+ATX_API atx_status atx_batch_run(atx_batch* b);
+ATX_API atx_status atx_batch_synchronize(atx_batch* b);
+ATX_API atx_status atx_batch_read_accumulation(atx_batch* b, uint32_t id, float* host_rgba, uint64_t n_pixels);
+ATX_API atx_status atx_batch_read_image(atx_batch* b, uint32_t id, uint32_t* host_rgba8, uint64_t n_pixels);
+ATX_API atx_status atx_batch_get_stats(atx_batch* b, atx_batch_stats* stats);
+ATX_API atx_status atx_batch_set_tuning(atx_batch* b, const atx_batch_tuning* tuning);
+ATX_API atx_status atx_batch_get_tuning(atx_batch* b, atx_batch_tuning* tuning);
+
 /* ------------------------------------------------- allocation-free render */
 
 /* Renders spp frames without allocating device memory.  No counterpart in
