@@ -18,7 +18,7 @@ from . import _native as N
 from ._native import AtxError, LIGHT_DTYPE, MATERIAL_DTYPE, SPHERE_DTYPE
 
 __all__ = [
-    "AtxError", "Batch", "Camera", "Light", "Material", "Renderer", "Scene", "Settings", "Sphere",
+    "AtxError", "Batch", "Camera", "Light", "Material", "Renderer", "Scene", "Server", "Settings", "Sphere",
     "SPHERE_DTYPE", "MATERIAL_DTYPE", "LIGHT_DTYPE", "camera_matrices", "device_count",
 ]
 
@@ -391,3 +391,103 @@ class Batch:
         t = N.BatchTuning()
         N.check(N.lib().atx_batch_get_tuning(self._h, C.byref(t)))
         return {k: getattr(t, k) for k, _ in N.BatchTuning._fields_ if k != "reserved"}
+
+
+def _batch_scene(spheres, materials, lights, camera: Camera, width: int, height: int, settings: Settings):
+    s, m, l = _as_spheres(spheres), _as_materials(materials), _as_lights(lights)
+    d = N.BatchScene(N.ptr(s) if len(s) else None, len(s), N.ptr(m) if len(m) else None, len(m),
+                     N.ptr(l) if len(l) else None, len(l), camera.desc(), width, height,
+                     N.Settings(int(bool(settings.accumulation)), int(bool(settings.skyLight)), (C.c_uint8 * 2)(),
+                                int(settings.maxBounces)))
+    return d, (s, m, l)
+
+
+class Server:
+    """Progressive render server with continuous batching (atx_server_*).
+
+    submit() copies the scene and returns a job id at once; a worker thread admits jobs in arrival order
+    when a slot and their device memory fit the HBM budget and renders all active jobs together, a slice
+    of frames per pass, until each reaches its target spp."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, max_active_jobs: int = 0, pass_spp: int = 0,
+                 max_pass_paths: int = 0, max_pending: int = 0, bvh_threshold: int = 0, flags: int = 0,
+                 host_executor: bool = False, host_fail_pass: int = 0):
+        if host_executor:
+            flags |= N.FLAG_HOST_EXECUTOR
+        cfg = N.ServerConfig(N.Config(device, 0, 0, bvh_threshold, 0, flags, hbm_budget_bytes), max_active_jobs,
+                             pass_spp, max_pass_paths, max_pending, host_fail_pass)
+        h = C.c_void_p()
+        N.check(N.lib().atx_server_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self._sizes = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().atx_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit_scene(self, spheres, materials, lights, camera: Camera, width: int, height: int,
+                     settings: Settings, target_spp: int) -> int:
+        d, keep = _batch_scene(spheres, materials, lights, camera, width, height, settings)
+        j = C.c_uint32()
+        N.check(N.lib().atx_server_submit(self._h, C.byref(d), target_spp, C.byref(j)))
+        del keep
+        self._sizes[j.value] = (width, height)
+        return j.value
+
+    def submit(self, sc, target_spp: int) -> int:
+        """Submits a scenes.SyntheticScene with its own camera and bounce depth."""
+        cam = Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction)
+        st = Settings(accumulation=True, skyLight=sc.sky_light, maxBounces=sc.max_bounces)
+        return self.submit_scene(sc.spheres, sc.materials, sc.lights, cam, sc.width, sc.height, st, target_spp)
+
+    def poll(self, job: int) -> dict:
+        i = N.JobInfo()
+        N.check(N.lib().atx_server_poll(self._h, job, C.byref(i)))
+        d = {k: getattr(i, k) for k, _ in N.JobInfo._fields_ if k != "reserved"}
+        d["state"] = N.JOB_STATES.get(d["state"], d["state"])
+        return d
+
+    def wait(self, job: int, timeout_ms: int = 60000):
+        N.check(N.lib().atx_server_wait(self._h, job, timeout_ms))
+
+    def image(self, job: int) -> np.ndarray:
+        w, h = self._sizes[job]
+        out = np.empty(w * h, dtype=np.uint32)
+        N.check(N.lib().atx_server_read_image(self._h, job, N.ptr(out), w * h))
+        return out
+
+    def accumulation(self, job: int) -> np.ndarray:
+        w, h = self._sizes[job]
+        out = np.empty((w * h, 4), dtype=np.float32)
+        N.check(N.lib().atx_server_read_accumulation(self._h, job, N.ptr(out), w * h))
+        return out
+
+    def cancel(self, job: int):
+        N.check(N.lib().atx_server_cancel(self._h, job))
+
+    def release(self, job: int):
+        N.check(N.lib().atx_server_release(self._h, job))
+        self._sizes.pop(job, None)
+
+    def stats(self) -> dict:
+        s = N.ServerStats()
+        N.check(N.lib().atx_server_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in N.ServerStats._fields_}
+
+    def now(self) -> float:
+        t = C.c_double()
+        N.check(N.lib().atx_server_now(self._h, C.byref(t)))
+        return t.value

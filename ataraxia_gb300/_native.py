@@ -82,8 +82,29 @@ class BatchTuning(C.Structure):
                 ("bvh_threshold", C.c_uint32), ("bvh_leaf_size", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("base", Config), ("max_active_jobs", C.c_uint32), ("pass_spp", C.c_uint32),
+                ("max_pass_paths", C.c_uint64), ("max_pending", C.c_uint32), ("host_fail_pass", C.c_uint32)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("frames_done", C.c_uint32), ("target_spp", C.c_uint32),
+                ("width", C.c_uint32), ("height", C.c_uint32), ("reserved", C.c_uint32),
+                ("submit_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
+                ("cancelled", C.c_uint64), ("failed", C.c_uint64), ("rejected", C.c_uint64),
+                ("passes", C.c_uint64), ("paths", C.c_uint64), ("busy_s", C.c_double),
+                ("device_bytes", C.c_uint64), ("active", C.c_uint32), ("queued", C.c_uint32)]
+
+
+JOB_STATES = {0: "queued", 1: "active", 2: "done", 3: "cancelled", 4: "failed"}
+
 FLAG_NO_GRAPHS = 1
 FLAG_PROFILE_KERNELS = 2
+FLAG_HOST_EXECUTOR = 4
 
 assert C.sizeof(Settings) == 8 and C.sizeof(CameraDesc) == 36
 
@@ -136,6 +157,17 @@ SIGNATURES = {
     "atx_batch_get_stats": (_ST, [_P, C.POINTER(BatchStats)]),
     "atx_batch_set_tuning": (_ST, [_P, C.POINTER(BatchTuning)]),
     "atx_batch_get_tuning": (_ST, [_P, C.POINTER(BatchTuning)]),
+    "atx_server_create": (_ST, [C.POINTER(ServerConfig), C.POINTER(_P)]),
+    "atx_server_destroy": (_ST, [_P]),
+    "atx_server_submit": (_ST, [_P, C.POINTER(BatchScene), _U32, C.POINTER(C.c_uint32)]),
+    "atx_server_poll": (_ST, [_P, _U32, C.POINTER(JobInfo)]),
+    "atx_server_wait": (_ST, [_P, _U32, _U32]),
+    "atx_server_read_image": (_ST, [_P, _U32, _P, _U64]),
+    "atx_server_read_accumulation": (_ST, [_P, _U32, _P, _U64]),
+    "atx_server_cancel": (_ST, [_P, _U32]),
+    "atx_server_release": (_ST, [_P, _U32]),
+    "atx_server_get_stats": (_ST, [_P, C.POINTER(ServerStats)]),
+    "atx_server_now": (_ST, [_P, C.POINTER(C.c_double)]),
     "atx_render_noalloc": (_ST, [_P, _U32, _P, _U32, _P, _U32, _P, _P, _P, _U32, _U32, C.POINTER(Settings), _U32,
                                  _U32, _P, _P, _P]),
     "atx_trace_nearest": (_ST, [_P, _P, _P, _U64, _P, _P]),

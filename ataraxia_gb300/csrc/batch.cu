@@ -10,9 +10,11 @@
 // Renderer.cu:165 does frame after frame; a lane that finishes its pixel pulls
 // the next pixel of the tile.  Every loop iteration is one bounce of the lane's
 // current path (a finished path immediately starts the pixel's next sample),
-// so lanes stay busy whatever their path lengths.  The primary hit of a pixel
-// is traced once and reused by its samples (the primary ray depends on the
-// pixel only), and shadow rays are traced inline.  Arithmetic and the random
+// so lanes stay busy whatever their path lengths.  The nearest-hit and shadow
+// queries of an iteration are shared by the whole warp (see the cooperative
+// queries below), so a warp with few pending queries still uses all 32 lanes
+// on them.  The primary hit of a pixel is traced once and reused by its samples
+// (the primary ray depends on the pixel only).  Arithmetic and the random
 // stream are those of the wavefront kernels, so results are bit-identical to
 // rendering each scene alone.
 #include <type_traits>
@@ -27,9 +29,145 @@ namespace {
 constexpr uint32_t kFull = 0xffffffffu;
 constexpr int kThreads = 256;
 
-struct TileCounters {
-    uint32_t next_px;
+// ------------------------------------------------ warp-cooperative queries
+//
+// In a loop iteration only some lanes of a warp need a nearest-hit (or shadow)
+// query.  All 32 lanes share the work: with k queries pending, each query gets
+// a group of g = 32/k lanes (rounded down to a power of two); lane r of a group
+// tests spheres r, r+g, r+2g, ... of the scene, in increasing index order, and
+// the group merges its partial results by (t, index).  Each sphere is tested
+// once with the same float test as the brute-force loop, and the lexicographic
+// (t, index) minimum is exactly the loop's answer (nearest t, lowest index on
+// equal t), so results are bit-identical.  LBVH scenes keep one query per lane.
+
+// Strided brute-force pieces over spheres first, first+stride, ...
+template <bool SMEM>
+__device__ __forceinline__ void strided_nearest(const float4* __restrict__ sph, uint32_t n, uint32_t first,
+                                                uint32_t stride, float3 o, float3 d, float a, float& tm, int32_t& best)
+{
+    for (uint32_t i = first; i < n; i += stride) {
+        const float4 s = SMEM ? sph[i] : __ldg(&sph[i]);
+        const float ox = o.x - s.x, oy = o.y - s.y, oz = o.z - s.z;
+        const float b = __fmaf_rn(oz, d.z, __fmaf_rn(oy, d.y, ox * d.x));
+        const float cc = __fmaf_rn(oz, oz, __fmaf_rn(oy, oy, __fmaf_rn(ox, ox, -s.w)));
+        const float disc = __fmaf_rn(b, b, -(a * cc));
+        // candidate filter of candidate_bits (trace.cuh): sign of max(b, -disc)
+        if ((int32_t)__float_as_uint(fmaxf(b, -disc)) < 0) {
+            float t;
+            if (sphere_t(s, o, d, a, t) && t > 0.0f && t < tm) {
+                tm = t;
+                best = (int32_t)i;
+            }
+        }
+    }
+}
+
+template <bool SMEM>
+__device__ __forceinline__ bool strided_occluded(const float4* __restrict__ sph, uint32_t n, uint32_t first,
+                                                 uint32_t stride, float3 o, float3 d, float a, float dist2)
+{
+    for (uint32_t i = first; i < n; i += stride) {
+        const float4 s = SMEM ? sph[i] : __ldg(&sph[i]);
+        const float ox = o.x - s.x, oy = o.y - s.y, oz = o.z - s.z;
+        const float b = __fmaf_rn(oz, d.z, __fmaf_rn(oy, d.y, ox * d.x));
+        const float cc = __fmaf_rn(oz, oz, __fmaf_rn(oy, oy, __fmaf_rn(ox, ox, -s.w)));
+        const float disc = __fmaf_rn(b, b, -(a * cc));
+        if ((int32_t)__float_as_uint(fmaxf(b, -disc)) < 0) {
+            float t;
+            if (sphere_t(s, o, d, a, t) && t > 0.0f && t * t < dist2) return true;
+        }
+    }
+    return false;
+}
+
+struct CoopGroup {
+    unsigned mask;   // lanes with a query
+    int g;           // lanes per query
+    int q;           // query this lane helps with (>= k: idle)
+    int owner;       // lane that owns query q
+    bool work;
 };
+
+__device__ __forceinline__ CoopGroup coop_plan(bool need)
+{
+    CoopGroup c;
+    c.mask = __ballot_sync(kFull, need);
+    const int k = __popc(c.mask);
+    int g = 32;
+    while (g > 1 && g * k > 32) g >>= 1;
+    c.g = g;
+    const int lane = (int)(threadIdx.x & 31u);
+    c.q = lane / g;
+    c.work = k > 0 && c.q < k;
+    c.owner = c.work ? (int)__fns(c.mask, 0, c.q + 1) : lane;
+    return c;
+}
+
+template <int IS>
+__device__ __forceinline__ void coop_nearest(const SceneView& sc, const float4* sph, bool need, float3 o, float3 d,
+                                             float& t_out, int32_t& id_out)
+{
+    if (IS == kIsBvh) {
+        if (need) id_out = bvh_nearest(sc, o, d, t_out);
+        return;
+    }
+    const CoopGroup c = coop_plan(need);
+    if (!c.mask) return;
+    const float3 qo = mk3(__shfl_sync(kFull, o.x, c.owner), __shfl_sync(kFull, o.y, c.owner),
+                          __shfl_sync(kFull, o.z, c.owner));
+    const float3 qd = mk3(__shfl_sync(kFull, d.x, c.owner), __shfl_sync(kFull, d.y, c.owner),
+                          __shfl_sync(kFull, d.z, c.owner));
+    float tm = kFltMax;
+    int32_t best = -1;
+    if (c.work) {
+        const uint32_t r = threadIdx.x & (uint32_t)(c.g - 1);
+        strided_nearest<IS == kIsSmem>(sph, sc.n_sph, r, (uint32_t)c.g, qo, qd, dot3(qd, qd), tm, best);
+    }
+    for (int off = 1; off < c.g; off <<= 1) {
+        const float t2 = __shfl_xor_sync(kFull, tm, off);
+        const int32_t b2 = __shfl_xor_sync(kFull, best, off);
+        if (b2 >= 0 && (best < 0 || t2 < tm || (t2 == tm && b2 < best))) {
+            tm = t2;
+            best = b2;
+        }
+    }
+    const int lane = (int)(threadIdx.x & 31u);
+    const int myq = __popc(c.mask & ((1u << lane) - 1u));
+    const int leader = (myq * c.g) & 31;
+    const float rt = __shfl_sync(kFull, tm, leader);
+    const int32_t rb = __shfl_sync(kFull, best, leader);
+    if (need) {
+        t_out = rt;
+        id_out = rb;
+    }
+}
+
+template <int IS>
+__device__ __forceinline__ bool coop_occluded(const SceneView& sc, const float4* sph, bool need, float3 o, float3 d,
+                                              float dist2)
+{
+    if (IS == kIsBvh) return need && bvh_occluded(sc, o, d, dist2);
+    const CoopGroup c = coop_plan(need);
+    if (!c.mask) return false;
+    const float3 qo = mk3(__shfl_sync(kFull, o.x, c.owner), __shfl_sync(kFull, o.y, c.owner),
+                          __shfl_sync(kFull, o.z, c.owner));
+    const float3 qd = mk3(__shfl_sync(kFull, d.x, c.owner), __shfl_sync(kFull, d.y, c.owner),
+                          __shfl_sync(kFull, d.z, c.owner));
+    const float qd2 = __shfl_sync(kFull, dist2, c.owner);
+    bool hit = false;
+    if (c.work) {
+        const uint32_t r = threadIdx.x & (uint32_t)(c.g - 1);
+        hit = strided_occluded<IS == kIsSmem>(sph, sc.n_sph, r, (uint32_t)c.g, qo, qd, dot3(qd, qd), qd2);
+    }
+    // OR within each group: a group's lanes are contiguous and aligned to g
+    const unsigned hits = __ballot_sync(kFull, hit);
+    const int lane = (int)(threadIdx.x & 31u);
+    const int myq = __popc(c.mask & ((1u << lane) - 1u));
+    const unsigned gmask = (c.g == 32) ? kFull : (((1u << c.g) - 1u) << ((myq * c.g) & 31));
+    return need && (hits & gmask) != 0u;
+}
+
+// ---------------------------------------------------------------- one tile
 
 template <int IS>
 __device__ __forceinline__ void render_tile(const BatchSceneDev& S, const float4* s_sph, uint32_t tile,
@@ -83,64 +221,73 @@ __device__ __forceinline__ void render_tile(const BatchSceneDev& S, const float4
         start_sample();
     }
     while (__any_sync(kFull, active)) {
-        if (!active) continue;
-        bool end_path = B <= 0;
-        if (!end_path) {
-            seed += (uint32_t)bounce;                              // Renderer.cu:306
-            float tmin;
-            int32_t hit;
-            if (bounce == 0 && pid != -2) {
-                tmin = pt;
-                hit = pid;
-            } else {
-                hit = scene_nearest<IS>(sc, sph, o, d, tmin);
-                ++nq;
-                if (bounce == 0) {
-                    pt = tmin;
-                    pid = hit;
-                }
+        // phase 1: the nearest hit of every active path (cooperatively)
+        bool traced = active && B > 0;
+        if (traced) seed += (uint32_t)bounce;                        // Renderer.cu:306
+        const bool need = traced && !(bounce == 0 && pid != -2);
+        float tmin = pt;
+        int32_t hit = pid;
+        coop_nearest<IS>(sc, sph, need, o, d, tmin, hit);
+        if (need) {
+            ++nq;
+            if (bounce == 0) {
+                pt = tmin;
+                pid = hit;
             }
+        }
+        // phase 2: shading and the shadow ray
+        bool end_path = active && !traced;                           // max_bounces <= 0: empty path
+        bool shadow = false;
+        float3 pos = cam_o, nrm = cam_o, L = cam_o, le = cam_o, albedo = cam_o, base = cam_o;
+        float dist2 = 0.0f, rough = 0.0f, metallic = 0.0f;
+        if (traced) {
             if (hit < 0) {
                 if (S.sky) col = add3(col, mul3(mk3(0.6f, 0.7f, 0.9f), thr));   // Renderer.cu:311-316
                 end_path = true;
             } else {
                 const float4 sv = (IS == kIsSmem) ? sph[hit] : __ldg(&sc.sph[hit]);
-                float3 pos, nrm;
                 ray_hit(sv, o, d, tmin, pos, nrm);
                 const int32_t mi = __ldg(&sc.sph_mat[hit]);
                 const float4* mrow = reinterpret_cast<const float4*>(sc.mat + mi);
                 const float4 m0 = __ldg(mrow), m1 = __ldg(mrow + 1), m2 = __ldg(mrow + 2);
-                const float3 albedo = mk3(m0.x, m0.y, m0.z);
-                const float rough = m0.w, metallic = m1.w;
+                albedo = mk3(m0.x, m0.y, m0.z);
+                rough = m0.w;
+                metallic = m1.w;
                 if (m2.w > 0.0f) col = add3(col, mul3(mk3(m2.x, m2.y, m2.z), thr));   // Renderer.cu:329-333
-                const float3 base = add3(muls3(mk3(m1.x, m1.y, m1.z), 1.0f - metallic), muls3(albedo, metallic));
-                if (sc.n_lights > 0u) {                                  // Renderer.cu:338-369
+                base = add3(muls3(mk3(m1.x, m1.y, m1.z), 1.0f - metallic), muls3(albedo, metallic));
+                if (sc.n_lights > 0u) {                                  // Renderer.cu:338-352
                     const uint32_t li = pcg_hash(seed) % sc.n_lights;
                     const float4* lrow = reinterpret_cast<const float4*>(sc.lights + li);
                     const float4 l0 = __ldg(lrow), l1 = __ldg(lrow + 1);
-                    float3 L = sub3(mk3(l0.x, l0.y, l0.z), pos);
-                    const float dist2 = dot3(L, L);
+                    L = sub3(mk3(l0.x, l0.y, l0.z), pos);
+                    dist2 = dot3(L, L);
                     L = muls3(L, 1.0f / sqrtf(dist2));
-                    const float3 so = add3(pos, muls3(nrm, kOffset));
+                    le = mk3(l1.x, l1.y, l1.z);
+                    shadow = true;
                     ++ns;
-                    if (!scene_occluded<IS>(sc, sph, so, L, dist2)) {
-                        const float3 f = cook_torrance(albedo, base, metallic, rough, nrm, neg3(d), L);
-                        col = add3(col, mul3(mul3(mk3(l1.x, l1.y, l1.z), f), thr));
-                    }
                 }
-                if (bounce + 1 >= B) {
+            }
+        }
+        const float3 so = add3(pos, muls3(nrm, kOffset));
+        const bool occluded = coop_occluded<IS>(sc, sph, shadow, so, L, dist2);
+        // phase 3: light contribution, roulette, next direction
+        if (traced && hit >= 0) {
+            if (shadow && !occluded) {                                   // Renderer.cu:356-368
+                const float3 f = cook_torrance(albedo, base, metallic, rough, nrm, neg3(d), L);
+                col = add3(col, mul3(mul3(le, f), thr));
+            }
+            if (bounce + 1 >= B) {
+                end_path = true;
+            } else {                                                     // Renderer.cu:371-384
+                thr = mul3(thr, albedo);
+                o = so;
+                const float prr = gmax(0.1f, gmin(1.0f, length3(thr)));
+                if (pcg_float(seed) > prr) {
                     end_path = true;
-                } else {                                                 // Renderer.cu:371-384
-                    thr = mul3(thr, albedo);
-                    o = add3(pos, muls3(nrm, kOffset));
-                    const float pr = gmax(0.1f, gmin(1.0f, length3(thr)));
-                    if (pcg_float(seed) > pr) {
-                        end_path = true;
-                    } else {
-                        thr = divs3(thr, pr);
-                        d = (metallic > 0.0f) ? sample_ggx(nrm, rough, seed) : sample_cosine(nrm, seed);
-                        ++bounce;
-                    }
+                } else {
+                    thr = divs3(thr, prr);
+                    d = (metallic > 0.0f) ? sample_ggx(nrm, rough, seed) : sample_cosine(nrm, seed);
+                    ++bounce;
                 }
             }
         }

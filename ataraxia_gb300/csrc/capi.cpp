@@ -400,3 +400,104 @@ ATX_API atx_status atx_batch_get_tuning(atx_batch* b, atx_batch_tuning* t)
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ serving
+
+#include "server.h"
+
+struct atx_server {
+    atx::Server impl;
+    explicit atx_server(const atx_server_config& c) : impl(c) {}
+};
+
+#define NEEDS(s) \
+    if (!(s)) return atx::fail(ATX_ERR_INVALID_ARG, "%s: null server", __func__)
+
+extern "C" {
+
+ATX_API atx_status atx_server_create(const atx_server_config* config, atx_server** out)
+{
+    return guarded([&]() -> atx_status {
+        if (!out) return atx::fail(ATX_ERR_INVALID_ARG, "atx_server_create: null out");
+        *out = nullptr;
+        atx_server_config c{};
+        if (config) c = *config;
+        atx_server* s = new atx_server(c);
+        atx_status st = s->impl.init();
+        if (st != ATX_OK) {
+            delete s;
+            return st;
+        }
+        *out = s;
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_server_destroy(atx_server* s)
+{
+    return guarded([&]() -> atx_status { delete s; return ATX_OK; });
+}
+
+ATX_API atx_status atx_server_submit(atx_server* s, const atx_batch_scene* scene, uint32_t target, uint32_t* job)
+{
+    return guarded([&]() -> atx_status {
+        NEEDS(s);
+        if (!scene || !job) return atx::fail(ATX_ERR_INVALID_ARG, "atx_server_submit: null argument");
+        return s->impl.submit(*scene, target, job);
+    });
+}
+
+ATX_API atx_status atx_server_poll(atx_server* s, uint32_t job, atx_job_info* info)
+{
+    return guarded([&]() -> atx_status {
+        NEEDS(s);
+        if (!info) return atx::fail(ATX_ERR_INVALID_ARG, "atx_server_poll: null info");
+        return s->impl.poll(job, info);
+    });
+}
+
+ATX_API atx_status atx_server_wait(atx_server* s, uint32_t job, uint32_t timeout_ms)
+{
+    return guarded([&]() -> atx_status { NEEDS(s); return s->impl.wait(job, timeout_ms); });
+}
+
+ATX_API atx_status atx_server_read_image(atx_server* s, uint32_t job, uint32_t* host, uint64_t n)
+{
+    return guarded([&]() -> atx_status { NEEDS(s); return s->impl.read_image(job, host, n); });
+}
+
+ATX_API atx_status atx_server_read_accumulation(atx_server* s, uint32_t job, float* host, uint64_t n)
+{
+    return guarded([&]() -> atx_status { NEEDS(s); return s->impl.read_accumulation(job, host, n); });
+}
+
+ATX_API atx_status atx_server_cancel(atx_server* s, uint32_t job)
+{
+    return guarded([&]() -> atx_status { NEEDS(s); return s->impl.cancel(job); });
+}
+
+ATX_API atx_status atx_server_release(atx_server* s, uint32_t job)
+{
+    return guarded([&]() -> atx_status { NEEDS(s); return s->impl.release(job); });
+}
+
+ATX_API atx_status atx_server_get_stats(atx_server* s, atx_server_stats* st)
+{
+    return guarded([&]() -> atx_status {
+        NEEDS(s);
+        if (!st) return atx::fail(ATX_ERR_INVALID_ARG, "atx_server_get_stats: null pointer");
+        return s->impl.stats(st);
+    });
+}
+
+ATX_API atx_status atx_server_now(atx_server* s, double* seconds)
+{
+    return guarded([&]() -> atx_status {
+        NEEDS(s);
+        if (!seconds) return atx::fail(ATX_ERR_INVALID_ARG, "atx_server_now: null pointer");
+        *seconds = s->impl.now();
+        return ATX_OK;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,93 @@
+// Render server: continuous batching of progressive render jobs over the
+// batched persistent renderer (batch_host.h), or over a host-only simulated
+// executor for scheduling tests on machines without a GPU.
+#pragma once
+
+#include <chrono>
+#include <condition_variable>
+#include <cstdint>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "atx.h"
+#include "batch_host.h"
+
+namespace atx {
+
+// What the server needs from the device: resident scenes and batched passes.
+class Executor {
+public:
+    virtual ~Executor() = default;
+    virtual atx_status init() = 0;
+    virtual atx_status add(const atx_batch_scene& d, uint64_t bytes, uint32_t* slot) = 0;
+    virtual atx_status remove(uint32_t slot) = 0;
+    virtual atx_status set_spp(uint32_t slot, uint32_t spp) = 0;
+    virtual atx_status run_pass() = 0;   // returns when the pass has finished
+    virtual atx_status read_image(uint32_t slot, uint32_t* host, uint64_t n) = 0;
+    virtual atx_status read_accumulation(uint32_t slot, float* host, uint64_t n) = 0;
+    virtual uint64_t device_bytes() const = 0;
+};
+
+std::unique_ptr<Executor> make_batch_executor(const atx_config& cfg);
+std::unique_ptr<Executor> make_host_executor(uint32_t fail_pass);
+
+class Server {
+public:
+    explicit Server(const atx_server_config& cfg);
+    ~Server();
+    atx_status init();
+
+    atx_status submit(const atx_batch_scene& scene, uint32_t target, uint32_t* id);
+    atx_status poll(uint32_t id, atx_job_info* info);
+    atx_status wait(uint32_t id, uint32_t timeout_ms);
+    atx_status read_image(uint32_t id, uint32_t* host, uint64_t n);
+    atx_status read_accumulation(uint32_t id, float* host, uint64_t n);
+    atx_status cancel(uint32_t id);
+    atx_status release(uint32_t id);
+    atx_status stats(atx_server_stats* out);
+    double now() const;
+
+    // Device bytes a job will hold while active (admission control).
+    static uint64_t job_bytes(const atx_batch_scene& s, uint32_t bvh_threshold);
+
+private:
+    struct Job {
+        atx_job_state state = ATX_JOB_QUEUED;
+        std::vector<atx_sphere> spheres;
+        std::vector<atx_material> materials;
+        std::vector<atx_light> lights;
+        atx_batch_scene desc{};
+        uint32_t target = 0;
+        uint32_t done = 0;
+        uint32_t slot = 0;          // executor scene id while active
+        uint64_t bytes = 0;
+        double t_submit = 0, t_admit = 0, t_done = 0;
+        std::vector<uint32_t> image;
+        std::vector<float> accum;
+        bool cancel = false;
+    };
+    void loop();
+    void admit_locked();
+    atx_status run_pass();
+
+    atx_server_config cfg_;
+    std::unique_ptr<Executor> exec_;
+    std::chrono::steady_clock::time_point t0_;
+    std::thread worker_;
+    mutable std::mutex mu_;
+    std::condition_variable cv_work_, cv_done_;
+    bool stop_ = false;
+    uint32_t next_id_ = 1;
+    std::unordered_map<uint32_t, Job> jobs_;
+    std::deque<uint32_t> pending_;
+    std::vector<uint32_t> active_;
+    atx_server_stats st_{};
+    atx_status worker_error_ = ATX_OK;
+    char worker_msg_[256] = "";
+};
+
+}  // namespace atx

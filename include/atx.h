@@ -107,6 +107,7 @@ typedef struct atx_config {
 
 #define ATX_FLAG_NO_GRAPHS 1u       /* launch kernels directly instead of replaying a CUDA graph */
 #define ATX_FLAG_PROFILE_KERNELS 2u /* record CUDA events around every kernel (atx_get_kernel_times) */
+#define ATX_FLAG_HOST_EXECUTOR 4u   /* server only: simulate the GPU on the host (scheduling tests, no device) */
 
 typedef struct atx_stats {
     uint64_t frames;           /* reference frames rendered (samples per pixel) since creation */
@@ -277,6 +278,70 @@ ATX_API atx_status atx_batch_read_image(atx_batch* b, uint32_t id, uint32_t* hos
 ATX_API atx_status atx_batch_get_stats(atx_batch* b, atx_batch_stats* stats);
 ATX_API atx_status atx_batch_set_tuning(atx_batch* b, const atx_batch_tuning* tuning);
 ATX_API atx_status atx_batch_get_tuning(atx_batch* b, atx_batch_tuning* tuning);
+
+/* ---------------------------------------------------------------- serving */
+
+/* A render server: jobs (a scene and a target sample count) are submitted
+ * from any thread and rendered progressively by a worker thread that runs
+ * batched passes (continuous batching).  A job is admitted, in arrival order,
+ * when an active slot is free and its device memory (scene tables, LBVH,
+ * accumulator, image) fits the HBM budget; its scene, frame index and
+ * accumulator stay resident until it reaches its target, when its image and
+ * accumulator are copied to host memory and its device memory is released.
+ * No counterpart in the reference (an interactive single-scene viewer). */
+typedef struct atx_server atx_server;
+
+typedef struct atx_server_config {
+    atx_config base;            /* device, hbm_budget_bytes (0 = unlimited), bvh settings, flags */
+    uint32_t max_active_jobs;   /* jobs rendered together (0 = 64) */
+    uint32_t pass_spp;          /* frames per job per pass (0 = 16) */
+    uint64_t max_pass_paths;    /* bound on pixel-samples per pass, scaling slices down (0 = 2^28) */
+    uint32_t max_pending;       /* queued jobs before submit returns ATX_ERR_BUSY (0 = unbounded) */
+    uint32_t host_fail_pass;    /* with ATX_FLAG_HOST_EXECUTOR: pass number at which the simulated device
+                                   reports an error (fault injection on the host; 0 = never) */
+} atx_server_config;
+
+typedef enum atx_job_state {
+    ATX_JOB_QUEUED = 0,
+    ATX_JOB_ACTIVE = 1,
+    ATX_JOB_DONE = 2,
+    ATX_JOB_CANCELLED = 3,
+    ATX_JOB_FAILED = 4
+} atx_job_state;
+
+typedef struct atx_job_info {
+    int32_t state;              /* atx_job_state */
+    uint32_t frames_done;
+    uint32_t target_spp;
+    uint32_t width, height;
+    uint32_t reserved;
+    double submit_s, admit_s, done_s;   /* server clock (atx_server_now) */
+} atx_job_info;
+
+typedef struct atx_server_stats {
+    uint64_t submitted, admitted, completed, cancelled, failed, rejected;
+    uint64_t passes, paths;
+    double busy_s;              /* wall time spent in passes */
+    uint64_t device_bytes;
+    uint32_t active, queued;
+} atx_server_stats;
+
+ATX_API atx_status atx_server_create(const atx_server_config* config, atx_server** out);
+/* Stops the worker (queued and active jobs are cancelled) and frees everything. */
+ATX_API atx_status atx_server_destroy(atx_server* s);
+/* Copies the scene; returns ATX_ERR_BUSY when max_pending jobs are queued and
+ * ATX_ERR_INVALID_ARG for a malformed scene or a zero target. */
+ATX_API atx_status atx_server_submit(atx_server* s, const atx_batch_scene* scene, uint32_t target_spp, uint32_t* job);
+ATX_API atx_status atx_server_poll(atx_server* s, uint32_t job, atx_job_info* info);
+/* Waits up to timeout_ms for the job to finish (ATX_ERR_TIMEOUT otherwise). */
+ATX_API atx_status atx_server_wait(atx_server* s, uint32_t job, uint32_t timeout_ms);
+ATX_API atx_status atx_server_read_image(atx_server* s, uint32_t job, uint32_t* host_rgba8, uint64_t n_pixels);
+ATX_API atx_status atx_server_read_accumulation(atx_server* s, uint32_t job, float* host_rgba, uint64_t n_pixels);
+ATX_API atx_status atx_server_cancel(atx_server* s, uint32_t job);
+/* Forgets a finished or cancelled job and its host copies. */
+ATX_API atx_status atx_server_release(atx_server* s, uint32_t job);
+ATX_API atx_status atx_server_get_stats(atx_server* s, atx_server_stats* stats);
+ATX_API atx_status atx_server_now(atx_server* s, double* seconds);
 
 /* ------------------------------------------------- allocation-free render */
 
