@@ -296,7 +296,19 @@ __device__ __forceinline__ void render_tile(const BatchSceneDev& S, const float4
             acc.y = acc.y + col.y;
             acc.z = acc.z + col.z;
             acc.w = acc.w + 1.0f;
-            if (++s < spp) {
+            ++s;
+            if (pid == -1 || !traced) {
+                // the pixel's primary ray missed (or no bounces): every remaining
+                // sample has this same colour, 0 + sky * 1 or 0; add them in order
+                const float3 m = (traced && S.sky) ? mk3(0.6f, 0.7f, 0.9f) : mk3(0.f, 0.f, 0.f);
+                for (; s < spp; ++s) {
+                    acc.x = acc.x + m.x;
+                    acc.y = acc.y + m.y;
+                    acc.z = acc.z + m.z;
+                    acc.w = acc.w + 1.0f;
+                }
+            }
+            if (s < spp) {
                 start_sample();
             } else {
                 S.accum[p] = acc;

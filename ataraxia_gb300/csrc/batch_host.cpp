@@ -9,7 +9,7 @@
 namespace atx {
 
 namespace {
-constexpr uint32_t kDefaultTileW = 32, kDefaultTileH = 16;
+constexpr uint32_t kDefaultTileW = 32, kDefaultTileH = 32;
 constexpr uint32_t kDefaultBvhThreshold = 1024;
 constexpr uint32_t kBatchSmemCap = 4096;   // spheres a CTA stages (64 KB)
 }  // namespace

@@ -13,7 +13,7 @@ namespace atx {
 namespace {
 constexpr uint32_t kDefaultWavePaths = 64u << 20;  // at most 64 Mi paths (8.7 GB of state) per wave
 constexpr uint32_t kDefaultBvhThreshold = 1024;
-constexpr uint32_t kDefaultBvhLeaf = 2;
+constexpr uint32_t kDefaultBvhLeaf = 16;   // fastest of 1..32 on the 65,536-sphere scene
 constexpr uint32_t kMaxBounces = 4096;
 }  // namespace
 
@@ -100,8 +100,8 @@ atx_status SceneStore::upload(const atx_sphere* s, uint32_t n, const atx_materia
 uint64_t WaveStore::bytes_for(uint32_t capacity, uint32_t max_bounces)
 {
     const uint64_t c = capacity;
-    return c * (7 * sizeof(float4) + 2 * sizeof(uint32_t) + sizeof(uint2)) +
-           2ull * (max_bounces + 1) * sizeof(uint32_t) + 16 + 12 * 256;
+    return c * (7 * sizeof(float4) + 3 * sizeof(uint32_t) + sizeof(uint2)) +
+           wave_counter_words((int)max_bounces) * sizeof(uint32_t) + 16 + 13 * 256;
 }
 
 atx_status WaveStore::ensure(uint32_t capacity, uint32_t max_bounces, Budget* budget)
@@ -128,7 +128,8 @@ atx_status WaveStore::ensure(uint32_t capacity, uint32_t max_bounces, Budget* bu
     view.q[0] = reinterpret_cast<uint32_t*>(take(c * sizeof(uint32_t)));
     view.q[1] = reinterpret_cast<uint32_t*>(take(c * sizeof(uint32_t)));
     view.prim = reinterpret_cast<uint2*>(take(c * sizeof(uint2)));
-    view.counters = reinterpret_cast<uint32_t*>(take(2ull * (b + 1) * sizeof(uint32_t)));
+    view.hitq = reinterpret_cast<uint32_t*>(take(c * sizeof(uint32_t)));
+    view.counters = reinterpret_cast<uint32_t*>(take(wave_counter_words((int)b) * sizeof(uint32_t)));
     view.capacity = cap;
     bounces = b;
     return ATX_OK;

@@ -60,12 +60,21 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
     const float4* sph = SMEM ? s_sph : sc.sph;
     const float3 o = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
-        const uint32_t p = job.pixel0 + j;
-        const float3 d = primary_dir(cam, p % cam.width, p / cam.width);
-        float t;
-        const int32_t id = scene_nearest<IS>(sc, sph, o, d, t);
-        ws.prim[j] = make_uint2(__float_as_uint(t), (uint32_t)id);
+    uint32_t* hits = &ws.counters[2 * ((uint32_t)job.max_bounces + 1u)];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {   // warp-uniform trip count
+        const uint32_t j = base + threadIdx.x;
+        int32_t id = -1;
+        if (j < n) {
+            const uint32_t p = job.pixel0 + j;
+            const float3 d = primary_dir(cam, p % cam.width, p / cam.width);
+            float t;
+            id = scene_nearest<IS>(sc, sph, o, d, t);
+            ws.prim[j] = make_uint2(__float_as_uint(t), (uint32_t)id);
+        }
+        // pixels whose primary ray hits get first-bounce paths; the others'
+        // samples are closed-form (accumulated by k_accumulate)
+        const uint32_t slot = warp_push(hits, id >= 0);
+        if (id >= 0) ws.hitq[slot] = j;
     }
 }
 
@@ -77,7 +86,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_extend(SceneView sc, CameraView
 {
     constexpr bool SMEM = IS == kIsSmem;
     extern __shared__ float4 s_sph[];
-    const uint32_t n = FIRST ? job.n_pixels * job.spp : ws.counters[2 * bounce];
+    const uint32_t n = !FIRST ? ws.counters[2 * bounce]
+                     : SHARED ? ws.counters[2 * ((uint32_t)job.max_bounces + 1u)] * job.spp
+                              : job.n_pixels * job.spp;
     if (blockIdx.x * blockDim.x >= n) return;
     if (SMEM) stage_spheres(sc, s_sph);
     const float4* sph = SMEM ? s_sph : sc.sph;
@@ -96,9 +107,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_extend(SceneView sc, CameraView
 
         if (idx < n) {
             if (FIRST) {
-                pid = idx;
-                const uint32_t p = job.pixel0 + idx / job.spp;
+                // SHARED: idx enumerates (hit pixel, sample); path ids stay pixel-major
+                const uint32_t j = SHARED ? ws.hitq[idx / job.spp] : idx / job.spp;
                 const uint32_t s = idx % job.spp;
+                pid = j * job.spp + s;
+                const uint32_t p = job.pixel0 + j;
                 o = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
                 d = primary_dir(cam, p % cam.width, p / cam.width);
                 thr = mk3(1.f, 1.f, 1.f);
@@ -118,7 +131,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_extend(SceneView sc, CameraView
             float tmin;
             int32_t hit;
             if (SHARED) {
-                const uint2 pr = ws.prim[idx / job.spp];
+                const uint2 pr = ws.prim[pid / job.spp];
                 tmin = __uint_as_float(pr.x);
                 hit = (int32_t)pr.y;
             } else {
@@ -243,12 +256,17 @@ __global__ void __launch_bounds__(kThreads) k_accumulate(WaveState ws, WaveJob j
         atomicAdd(&ws.totals[0], ext);
         atomicAdd(&ws.totals[1], sh);
     }
+    // a sample whose shared primary ray missed has colour 0 + sky * 1 (Renderer.cu:311-316)
+    const bool shared = job.spp > 1 && job.max_bounces > 0;
+    const float4 miss = job.sky ? make_float4(0.6f, 0.7f, 0.9f, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < job.n_pixels; j += stride) {
         const uint32_t p = job.pixel0 + j;
         float4 a = accum[p];
+        const bool missed = shared && (int32_t)ws.prim[j].y < 0;
         for (uint32_t s = 0; s < job.spp; ++s) {
             float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (job.max_bounces > 0) c = ws.col[(uint64_t)j * job.spp + s];
+            if (missed) c = miss;
+            else if (job.max_bounces > 0) c = ws.col[(uint64_t)j * job.spp + s];
             a.x = a.x + c.x;
             a.y = a.y + c.y;
             a.z = a.z + c.z;
@@ -375,7 +393,7 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
     auto begin = [&](int fam) { if (timer) timer->begin(fam, stream); };
     auto end = [&](int fam) { if (timer) timer->end(fam, stream); };
     if (bounces > 0) {
-        cudaError_t e = cudaMemsetAsync(ws.counters, 0, sizeof(uint32_t) * 2 * ((size_t)bounces + 1), stream);
+        cudaError_t e = cudaMemsetAsync(ws.counters, 0, sizeof(uint32_t) * wave_counter_words(bounces), stream);
         if (e != cudaSuccess) return e;
         const int g0 = grid_for(paths, shape.threads, shape.blocks_extend);
         const bool share = job.spp > 1;

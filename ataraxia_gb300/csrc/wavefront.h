@@ -93,8 +93,12 @@ struct WaveState {
     uint32_t* counters;
     unsigned long long* totals;   // [0] extension rays after bounce 0, [1] shadow rays (running sums)
     uint2* prim;                  // per pixel of the wave: primary hit (t bits, sphere id), shared by its samples
+    uint32_t* hitq;               // wave pixels whose primary ray hits (only those get first-bounce paths)
     uint32_t capacity;
 };
+
+// Counter slots after the per-bounce pairs: [2*(max_bounces+1)] = hit pixels.
+inline size_t wave_counter_words(int max_bounces) { return 2 * ((size_t)(max_bounces > 0 ? max_bounces : 0) + 1) + 2; }
 
 // One wave: pixels [pixel0, pixel0 + n_pixels) x samples [0, spp) with the
 // sample s of pixel p at path id (p - pixel0) * spp + s, traced as the

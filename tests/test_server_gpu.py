@@ -1,0 +1,92 @@
+"""Render server on the GPU: each job's result is bit-identical alone and in the mix (jobs arriving
+while others render, sliced over several batched passes), and admission respects the HBM budget."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from ataraxia_gb300 import Camera, Renderer, Server, Settings, scenes
+from tests.helpers import bit_mismatches
+
+pytestmark = pytest.mark.gpu
+
+
+def mix(count, scale=8, seed=4):
+    out = []
+    for j in scenes.config4(seed=seed, rate=200.0, duration_s=count / 200.0 + 1.0)[:count]:
+        sc = j.scene
+        out.append((scenes.SyntheticScene(**{**sc.__dict__, "width": max(8, sc.width // scale),
+                                             "height": max(8, sc.height // scale)}), min(j.target_spp, 64)))
+    return out
+
+
+def alone(sc, spp):
+    with Renderer() as r:
+        r.on_resize(sc.width, sc.height)
+        r.set_scene(sc.spheres, sc.materials, sc.lights)
+        r.set_camera(Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction))
+        r.set_settings(Settings(accumulation=True, skyLight=sc.sky_light, maxBounces=sc.max_bounces))
+        r.render_frames(spp)
+        return r.get_accumulation().reshape(-1, 4).copy(), r.get_image().reshape(-1).copy()
+
+
+def test_results_same_alone_and_in_the_mix():
+    jobs = mix(12)
+    with Server(pass_spp=8, max_active_jobs=6) as s:
+        ids = []
+        for k, (sc, target) in enumerate(jobs):
+            ids.append(s.submit(sc, target))
+            if k % 3 == 2:
+                time.sleep(0.01)       # later jobs arrive while earlier ones render
+        for j in ids:
+            s.wait(j, 60000)
+        for j, (sc, target) in zip(ids, jobs):
+            info = s.poll(j)
+            assert info["state"] == "done" and info["frames_done"] == target
+            ref_acc, ref_img = alone(sc, target)
+            assert bit_mismatches(s.accumulation(j), ref_acc) == 0, sc.name
+            assert np.array_equal(s.image(j), ref_img), sc.name
+        st = s.stats()
+        # retired jobs give their memory back; the batch's own small tables remain
+        assert st["completed"] == 12 and st["passes"] >= 8 and st["device_bytes"] < (1 << 20)
+
+
+def test_budget_bounds_device_memory_and_concurrent_submitters():
+    jobs = mix(16, scale=4, seed=9)
+    from ataraxia_gb300 import _native as N
+
+    per = max(N_bytes(sc) for sc, _ in jobs)
+    budget = 3 * per
+    with Server(hbm_budget_bytes=budget, pass_spp=4) as s:
+        ids, lock = [], threading.Lock()
+
+        def worker(part):
+            for sc, target in part:
+                j = s.submit(sc, target)
+                with lock:
+                    ids.append((j, target))
+
+        th = [threading.Thread(target=worker, args=(jobs[k::4],)) for k in range(4)]
+        for t in th:
+            t.start()
+        peak = 0
+        while any(t.is_alive() for t in th) or s.stats()["completed"] < len(jobs):
+            peak = max(peak, s.stats()["device_bytes"])
+            time.sleep(0.001)
+        for t in th:
+            t.join()
+        assert peak <= budget
+        for j, target in ids:
+            assert s.poll(j)["frames_done"] == target
+
+
+def N_bytes(sc):
+    """Upper bound of a job's device bytes (accumulator + image + tables + LBVH)."""
+    from ataraxia_gb300 import _native as N  # noqa: F401
+
+    n = len(sc.spheres)
+    px = sc.width * sc.height
+    tables = 24 * n + 48 * len(sc.materials) + 32 * len(sc.lights) + 8 * 256
+    bvh = 200 * n if n >= 1024 else 0
+    return tables + bvh + 20 * px + 512
