@@ -233,23 +233,31 @@ class Job:
     arrival_s: float
     scene: SyntheticScene
     target_spp: int
+    pool_index: int = -1
 
 
-def config4(seed: int = 4, rate: float = 50.0, duration_s: float = 60.0) -> list[Job]:
-    """Serving stream: Poisson arrivals at `rate` jobs/s over `duration_s`; each job a batch_scene
-    with a target spp drawn from TARGET_SPP."""
+def scene_pool(seed: int = 4, size: int = 512) -> list[SyntheticScene]:
+    """A pool of scenes drawn from the batched-mix distribution (batch_scene) for the serving stream."""
+    st = Stream(seed, "config4-pool")
+    return [batch_scene(st, i) for i in range(size)]
+
+
+def config4(seed: int = 4, rate: float = 50.0, duration_s: float = 60.0, pool: list | None = None) -> list[Job]:
+    """Serving stream: Poisson arrivals at `rate` jobs/s over `duration_s`; each job a scene of the
+    batched-mix distribution, drawn uniformly from a seeded pool of such scenes (scene_pool; generating a
+    distinct scene per job in Python would throttle arrivals at 800 jobs/s), with a target spp drawn from
+    TARGET_SPP."""
+    pool = pool if pool is not None else scene_pool(seed)
     st = Stream(seed, f"config4-{rate}")
     jobs: list[Job] = []
     t = 0.0
-    i = 0
     while True:
         t += -math.log(1.0 - float(st.uniform(1)[0])) / rate
         if t >= duration_s:
             break
-        sc = batch_scene(st, i)
+        k = int(st.integers(0, len(pool), 1)[0])
         target = TARGET_SPP[int(st.integers(0, len(TARGET_SPP), 1)[0])]
-        jobs.append(Job(t, sc, target))
-        i += 1
+        jobs.append(Job(t, pool[k], target, k))
     return jobs
 
 

@@ -427,6 +427,148 @@ def run_batch_compare(args, dist: Dist):
             "tuning": tun}
 
 
+def _pct(v, q):
+    import numpy as np
+
+    return round(float(np.percentile(np.asarray(v), q)), 4) if v else None
+
+
+def serve_batched(jobs, duration, args):
+    """Poisson arrivals into the continuous-batching server for `duration` seconds.  A driver thread
+    submits each job at its arrival time (BUSY = rejected once max_pending jobs wait); the main thread
+    collects finished jobs and releases them.  Latency = done time - intended arrival time."""
+    import threading
+
+    import ataraxia_gb300 as atx
+
+    s = atx.Server(hbm_budget_bytes=int(args.hbm_budget_gb * 1e9), max_active_jobs=args.max_active,
+                   pass_spp=args.pass_spp, max_pending=args.max_pending,
+                   host_executor=getattr(args, "host_executor", False))
+    lock = threading.Lock()
+    outstanding = {}   # job id -> (intended arrival on the server clock, paths)
+    rejected = [0]
+    t0 = s.now()
+    wall0 = time.perf_counter()
+
+    def driver():
+        for j in jobs:
+            if j.arrival_s >= duration:
+                break
+            delay = j.arrival_s - (time.perf_counter() - wall0)
+            if delay > 0:
+                time.sleep(delay)
+            try:
+                jid = s.submit(j.scene, j.target_spp)
+            except atx.AtxError:
+                rejected[0] += 1
+                continue
+            with lock:
+                outstanding[jid] = (t0 + j.arrival_s, j.scene.width * j.scene.height * j.target_spp)
+
+    th = threading.Thread(target=driver)
+    th.start()
+    lat, done_paths, submitted = [], 0, 0
+    end = t0 + duration
+    while True:
+        now = s.now()
+        with lock:
+            ids = list(outstanding.items())
+        for jid, (arr, paths) in ids:
+            info = s.poll(jid)
+            if info["state"] == "done" and info["done_s"] <= end:
+                lat.append(info["done_s"] - arr)
+                done_paths += paths
+                s.release(jid)
+                with lock:
+                    del outstanding[jid]
+        if now >= end:
+            break
+        time.sleep(0.02)
+    th.join()
+    st = s.stats()
+    with lock:
+        incomplete = len(outstanding)
+    for jid in list(outstanding):
+        s.cancel(jid)
+    s.close()
+    span = duration
+    return {"submitted": int(st["submitted"]), "rejected": rejected[0], "completed": len(lat),
+            "incomplete": incomplete, "jobs_per_s": round(len(lat) / span, 2),
+            "mpaths_s": round(st["paths"] / span / 1e6, 1), "completed_mpaths_s": round(done_paths / span / 1e6, 1),
+            "p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99), "passes": int(st["passes"]),
+            "busy_frac": round(st["busy_s"] / span, 3)}
+
+
+def serve_fifo(jobs, duration, max_pending):
+    """One launch per job in arrival order on the plain renderer, image read back after each; jobs
+    arriving while max_pending jobs wait are rejected, as the server's queue bound does."""
+    from collections import deque
+
+    import ataraxia_gb300 as atx
+
+    r = atx.Renderer()
+    wall0 = time.perf_counter()
+    lat, paths, rejected = [], 0, 0
+    queue, nxt = deque(), 0
+
+    def arrivals(upto):
+        nonlocal nxt, rejected
+        while nxt < len(jobs) and jobs[nxt].arrival_s <= min(upto, duration):
+            if len(queue) >= max_pending:
+                rejected += 1
+            else:
+                queue.append(jobs[nxt])
+            nxt += 1
+
+    while True:
+        now = time.perf_counter() - wall0
+        if now >= duration:
+            break
+        arrivals(now)
+        if not queue:
+            if nxt >= len(jobs) or jobs[nxt].arrival_s >= duration:
+                break
+            time.sleep(max(0.0, jobs[nxt].arrival_s - now))
+            continue
+        j = queue.popleft()
+        sc = j.scene
+        r.on_resize(sc.width, sc.height)
+        r.set_scene(sc.spheres, sc.materials, sc.lights)
+        r.set_camera(atx.Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction))
+        r.set_settings(atx.Settings(accumulation=False, skyLight=sc.sky_light, maxBounces=sc.max_bounces))
+        r.render_frames(j.target_spp)
+        r.get_image()
+        t = time.perf_counter() - wall0
+        if t > duration:
+            queue.appendleft(j)
+            break
+        lat.append(t - j.arrival_s)
+        paths += sc.width * sc.height * j.target_spp
+    arrivals(duration)
+    r.close()
+    return {"rejected": rejected, "completed": len(lat), "incomplete": len(queue),
+            "jobs_per_s": round(len(lat) / duration, 2), "mpaths_s": round(paths / duration / 1e6, 1),
+            "p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99)}
+
+
+def run_serve(args, dist: Dist):
+    """Serving workload (seed 4): Poisson arrivals at each rate for --serve-seconds; continuous batching
+    with an HBM budget against FIFO one-launch-per-job."""
+    from ataraxia_gb300 import scenes
+
+    pool = scenes.scene_pool(4, args.pool)
+    out = {"mode": "serve", "seconds": args.serve_seconds, "hbm_budget_gb": args.hbm_budget_gb,
+           "pool_scenes": len(pool), "rates": {}}
+    for rate in [float(x) for x in args.rates.split(",")]:
+        jobs = scenes.config4(seed=4, rate=rate, duration_s=args.serve_seconds, pool=pool)
+        res = {"batched": serve_batched(jobs, args.serve_seconds, args)}
+        if not args.no_fifo:
+            res["fifo"] = serve_fifo(jobs, args.serve_seconds, args.max_pending)
+        out["rates"][str(rate)] = res
+        log(json.dumps({str(rate): res}))
+    return out
+
+
 def run_render_only(args, dist: Dist):
     """Warm-up and timed launches of the workload, nothing else (profiler captures)."""
     import ataraxia_gb300 as atx
@@ -499,10 +641,18 @@ def main(argv=None) -> int:
     ap.add_argument("--no-ref-kernel", action="store_true", help="skip timing the restated reference kernel")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=3.0)
-    ap.add_argument("--mode", choices=["full", "render", "batch"], default="full",
+    ap.add_argument("--mode", choices=["full", "render", "batch", "serve"], default="full",
                     help="render: only warm-up + timed launches of the workload (for profiler captures); "
                          "batch: the 64-scene mix, plain renderer per scene vs one batched pass")
     ap.add_argument("--mix-scenes", type=int, default=64, help="batch mode: scenes in the mix")
+    ap.add_argument("--rates", default="50,200,800", help="serve mode: arrival rates (jobs/s)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="serve mode: run length per rate")
+    ap.add_argument("--hbm-budget-gb", type=float, default=120.0, help="serve mode: admission budget")
+    ap.add_argument("--max-active", type=int, default=64, help="serve mode: jobs rendered together")
+    ap.add_argument("--pass-spp", type=int, default=16, help="serve mode: frames per job per pass")
+    ap.add_argument("--max-pending", type=int, default=4096, help="serve mode: queue bound (then BUSY)")
+    ap.add_argument("--pool", type=int, default=512, help="serve mode: scenes in the job pool")
+    ap.add_argument("--no-fifo", action="store_true", help="serve mode: skip the FIFO baseline")
     ap.add_argument("--tile", default="", help="batch mode: work-item tile WxH (default from the library)")
     ap.add_argument("--width", type=int, default=0, help="render mode: override the viewport width")
     ap.add_argument("--height", type=int, default=0, help="render mode: override the viewport height")
@@ -523,6 +673,8 @@ def main(argv=None) -> int:
             out = run_render_only(args, dist)
         elif args.mode == "batch":
             out = run_batch_compare(args, dist)
+        elif args.mode == "serve":
+            out = run_serve(args, dist)
         elif args.impl == "reference":
             if dist.rank != 0:
                 return 0
