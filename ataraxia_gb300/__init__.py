@@ -16,10 +16,13 @@ import numpy as np
 
 from . import _native as N
 from ._native import AtxError, LIGHT_DTYPE, MATERIAL_DTYPE, SPHERE_DTYPE
+from .scene_graph import ROOT, SceneGraph
 
 __all__ = [
     "AtxError", "Batch", "Camera", "Light", "Material", "Renderer", "Scene", "Server", "Settings", "Sphere",
     "SPHERE_DTYPE", "MATERIAL_DTYPE", "LIGHT_DTYPE", "camera_matrices", "device_count",
+    "SceneGraph", "ROOT", "import_scene", "export_scene", "scene_from_json", "scene_to_json",
+    "importScene", "exportScene", "serializeScene", "deserializeScene",
 ]
 
 
@@ -78,17 +81,69 @@ class Camera:
 
 @dataclass
 class Scene:
-    """Flat scene (the caller flattens the reference's node hierarchy, Renderer.cu:67-96).
-    spheres/materials/lights may be lists of the dataclasses above or structured numpy arrays
-    with SPHERE_DTYPE / MATERIAL_DTYPE / LIGHT_DTYPE."""
+    """Scene.h:58-75.  spheres/materials/lights may be lists of the dataclasses above or structured
+    numpy arrays with SPHERE_DTYPE / MATERIAL_DTYPE / LIGHT_DTYPE.  With a scene graph (import_scene,
+    or a SceneGraph built node by node) the spheres are the graph's, flattened as Renderer.cu:67-96
+    does; otherwise `spheres` is already the world-space list."""
     spheres: object = field(default_factory=list)
     materials: object = field(default_factory=list)
     lights: object = field(default_factory=list)
     settings: Settings = field(default_factory=Settings)
     camera: Camera = field(default_factory=Camera)
+    graph: SceneGraph | None = None
 
     def arrays(self):
-        return _as_spheres(self.spheres), _as_materials(self.materials), _as_lights(self.lights)
+        s = self.graph.flatten() if self.graph is not None else _as_spheres(self.spheres)
+        return s, _as_materials(self.materials), _as_lights(self.lights)
+
+
+def import_scene(path) -> Scene:
+    """Utils::importScene (Utils.cpp:175-187): the scene file's graph, materials, lights, camera and
+    settings.  A missing file raises AtxError (ATX_ERR_NOT_FOUND); the reference returns an empty Scene."""
+    g = SceneGraph.load(path)
+    return _scene_from_graph(g)
+
+
+def _scene_from_graph(g: SceneGraph) -> Scene:
+    i = g.info()
+    c, st = i["camera"], i["settings"]
+    return Scene(spheres=g.flatten(), materials=g.materials(), lights=g.lights(),
+                 settings=Settings(st["accumulation"], st["skyLight"], st["maxBounces"]),
+                 camera=Camera(c["fov"], c["near"], c["far"], c["position"], c["direction"]), graph=g)
+
+
+def scene_from_json(text) -> Scene:
+    """Utils::deserializeScene (Utils.cpp:97-137)."""
+    return _scene_from_graph(SceneGraph.from_json(text))
+
+
+def _graph_for(scene: Scene) -> SceneGraph:
+    g = scene.graph
+    if g is None:                       # a flat scene: every sphere on the root node
+        g = SceneGraph()
+        g.add_spheres(ROOT, _as_spheres(scene.spheres))
+    g.set_materials(_as_materials(scene.materials))
+    g.set_lights(_as_lights(scene.lights))
+    g.set_camera(scene.camera.desc())
+    st = scene.settings
+    g.set_settings(N.Settings(int(bool(st.accumulation)), int(bool(st.skyLight)), (0, 0), int(st.maxBounces)))
+    return g
+
+
+def scene_to_json(scene: Scene) -> str:
+    """Utils::serializeScene + dump(4) (Utils.cpp:3-51)."""
+    return _graph_for(scene).to_json()
+
+
+def export_scene(scene: Scene, path):
+    """Utils::exportScene (Utils.cpp:53-62)."""
+    _graph_for(scene).save(path)
+
+
+importScene = import_scene
+exportScene = export_scene
+serializeScene = scene_to_json
+deserializeScene = scene_from_json
 
 
 def _as_spheres(x) -> np.ndarray:
@@ -230,6 +285,10 @@ class Renderer:
         s, m, l = _as_spheres(spheres), _as_materials(materials), _as_lights(lights)
         N.check(N.lib().atx_set_scene(self._h, N.ptr(s) if len(s) else None, len(s), N.ptr(m) if len(m) else None,
                                       len(m), N.ptr(l) if len(l) else None, len(l)))
+
+    def set_scene_graph(self, graph: SceneGraph):
+        """Flattens the graph (Renderer.cu:67-96) and uploads it (atx_set_scene_graph)."""
+        N.check(N.lib().atx_set_scene_graph(self._h, graph.handle))
 
     def set_camera(self, camera: Camera):
         d = camera.desc()

@@ -46,6 +46,11 @@ class CameraDesc(C.Structure):
                 ("near_clip", C.c_float), ("far_clip", C.c_float)]
 
 
+class SceneInfo(C.Structure):
+    _fields_ = [("n_spheres", C.c_uint32), ("n_materials", C.c_uint32), ("n_lights", C.c_uint32),
+                ("n_nodes", C.c_uint32), ("camera", CameraDesc), ("settings", Settings)]
+
+
 class Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("wave_paths", C.c_uint32), ("threads", C.c_uint32),
                 ("bvh_threshold", C.c_uint32), ("bvh_leaf_size", C.c_uint32), ("flags", C.c_uint32),
@@ -172,6 +177,24 @@ SIGNATURES = {
                                  _U32, _P, _P, _P]),
     "atx_trace_nearest": (_ST, [_P, _P, _P, _U64, _P, _P]),
     "atx_primary_directions": (_ST, [_P, _P, _U64]),
+    "atx_scene_create": (_ST, [C.POINTER(_P)]),
+    "atx_scene_destroy": (_ST, [_P]),
+    "atx_scene_parse_json": (_ST, [C.c_char_p, _U64, C.POINTER(_P)]),
+    "atx_scene_load": (_ST, [C.c_char_p, C.POINTER(_P)]),
+    "atx_scene_to_json": (_ST, [_P, _P, _U64, C.POINTER(C.c_uint64)]),
+    "atx_scene_save": (_ST, [_P, C.c_char_p]),
+    "atx_scene_get_info": (_ST, [_P, C.POINTER(SceneInfo)]),
+    "atx_scene_flatten": (_ST, [_P, _P, _U64]),
+    "atx_scene_get_materials": (_ST, [_P, _P, _U64]),
+    "atx_scene_get_lights": (_ST, [_P, _P, _U64]),
+    "atx_scene_add_node": (_ST, [_P, _U32, C.c_char_p, C.POINTER(C.c_uint32)]),
+    "atx_scene_set_transform": (_ST, [_P, _U32, _P, _P, _P]),
+    "atx_scene_add_spheres": (_ST, [_P, _U32, _P, _U32]),
+    "atx_scene_set_materials": (_ST, [_P, _P, _U32]),
+    "atx_scene_set_lights": (_ST, [_P, _P, _U32]),
+    "atx_scene_set_camera": (_ST, [_P, C.POINTER(CameraDesc)]),
+    "atx_scene_set_settings": (_ST, [_P, C.POINTER(Settings)]),
+    "atx_set_scene_graph": (_ST, [_P, _P]),
 }
 
 _lib = None

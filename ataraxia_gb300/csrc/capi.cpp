@@ -281,6 +281,246 @@ ATX_API atx_status atx_primary_directions(atx_renderer* r, float* host_dirs, uin
 
 }  // extern "C"
 
+// ------------------------------------------------------------ scene graph
+
+#include <cstdio>
+
+#include "scene_io.h"
+
+struct atx_scene {
+    atx::SceneGraph g;
+};
+
+#define NEED_SCENE(s) \
+    if (!(s)) return atx::fail(ATX_ERR_INVALID_ARG, "%s: null scene", __func__)
+#define NEED_NODE(s, k) \
+    if ((k) >= (s)->g.nodes.size()) return atx::fail(ATX_ERR_INVALID_ARG, "%s: no node %u", __func__, (unsigned)(k))
+
+extern "C" {
+
+ATX_API atx_status atx_scene_create(atx_scene** out)
+{
+    return guarded([&]() -> atx_status {
+        if (!out) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_create: null out");
+        *out = new atx_scene();
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_destroy(atx_scene* s)
+{
+    delete s;
+    return ATX_OK;
+}
+
+ATX_API atx_status atx_scene_parse_json(const char* text, uint64_t len, atx_scene** out)
+{
+    return guarded([&]() -> atx_status {
+        if (!out || (!text && len)) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_parse_json: null pointer");
+        *out = nullptr;
+        auto* s = new atx_scene();
+        const atx_status st = s->g.parse(text ? text : "", (size_t)len);
+        if (st != ATX_OK) {
+            delete s;
+            return st;
+        }
+        *out = s;
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_load(const char* path, atx_scene** out)
+{
+    return guarded([&]() -> atx_status {
+        if (!path || !out) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_load: null pointer");
+        *out = nullptr;
+        std::FILE* f = std::fopen(path, "rb");
+        if (!f) return atx::fail(ATX_ERR_NOT_FOUND, "atx_scene_load: cannot open %s", path);
+        std::string text;
+        char buf[65536];
+        size_t n;
+        while ((n = std::fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, n);
+        const bool bad = std::ferror(f) != 0;
+        std::fclose(f);
+        if (bad) return atx::fail(ATX_ERR_NOT_FOUND, "atx_scene_load: cannot read %s", path);
+        return atx_scene_parse_json(text.data(), text.size(), out);
+    });
+}
+
+ATX_API atx_status atx_scene_to_json(const atx_scene* s, char* buf, uint64_t cap, uint64_t* len)
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        if (!len) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_to_json: null len");
+        const std::string j = s->g.to_json();
+        *len = j.size();
+        if (buf) std::memcpy(buf, j.data(), j.size() < cap ? j.size() : (size_t)cap);
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_save(const atx_scene* s, const char* path)
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        if (!path) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_save: null path");
+        const std::string j = s->g.to_json();
+        std::FILE* f = std::fopen(path, "wb");
+        if (!f) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_save: cannot open %s", path);
+        const bool ok = std::fwrite(j.data(), 1, j.size(), f) == j.size();
+        if (std::fclose(f) != 0 || !ok) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_save: cannot write %s", path);
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_get_info(const atx_scene* s, atx_scene_info* info)
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        if (!info) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_get_info: null info");
+        info->n_spheres = (uint32_t)s->g.sphere_count();
+        info->n_materials = (uint32_t)s->g.materials.size();
+        info->n_lights = (uint32_t)s->g.lights.size();
+        info->n_nodes = (uint32_t)s->g.nodes.size();
+        info->camera = s->g.camera;
+        info->settings = s->g.settings;
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_flatten(const atx_scene* s, atx_sphere* out, uint64_t cap)
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        std::vector<atx_sphere> v;
+        s->g.flatten(v);
+        if (!out && !v.empty()) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_flatten: null out");
+        if (cap < v.size())
+            return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_flatten: %zu spheres, room for %llu", v.size(),
+                             (unsigned long long)cap);
+        if (!v.empty()) std::memcpy(out, v.data(), v.size() * sizeof(atx_sphere));
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_get_materials(const atx_scene* s, atx_material* out, uint64_t cap)
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        const auto& v = s->g.materials;
+        if (cap < v.size() || (!out && !v.empty()))
+            return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_get_materials: room for %llu of %zu",
+                             (unsigned long long)cap, v.size());
+        if (!v.empty()) std::memcpy(out, v.data(), v.size() * sizeof(atx_material));
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_get_lights(const atx_scene* s, atx_light* out, uint64_t cap)
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        const auto& v = s->g.lights;
+        if (cap < v.size() || (!out && !v.empty()))
+            return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_get_lights: room for %llu of %zu",
+                             (unsigned long long)cap, v.size());
+        if (!v.empty()) std::memcpy(out, v.data(), v.size() * sizeof(atx_light));
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_add_node(atx_scene* s, uint32_t parent, const char* name, uint32_t* node)
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        NEED_NODE(s, parent);
+        const uint32_t k = s->g.add_node(parent, name ? name : "Untitled");   // SceneNode() default name
+        if (k == atx::kNoNode) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_add_node: graph too deep");
+        if (node) *node = k;
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_set_transform(atx_scene* s, uint32_t node, const float position[3],
+                                           const float rotation_xyzw[4], const float scale[3])
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        NEED_NODE(s, node);
+        atx::GraphNode& n = s->g.nodes[node];
+        if (position) std::memcpy(n.position, position, sizeof n.position);
+        if (rotation_xyzw) std::memcpy(n.rotation, rotation_xyzw, sizeof n.rotation);
+        if (scale) std::memcpy(n.scale, scale, sizeof n.scale);
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_add_spheres(atx_scene* s, uint32_t node, const atx_sphere* spheres, uint32_t n)
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        NEED_NODE(s, node);
+        if (n && !spheres) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_add_spheres: null spheres");
+        auto& v = s->g.nodes[node].spheres;
+        v.insert(v.end(), spheres, spheres + n);
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_set_materials(atx_scene* s, const atx_material* m, uint32_t n)
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        if (n && !m) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_set_materials: null materials");
+        s->g.materials.assign(m, m + n);
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_set_lights(atx_scene* s, const atx_light* l, uint32_t n)
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        if (n && !l) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_set_lights: null lights");
+        s->g.lights.assign(l, l + n);
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_set_camera(atx_scene* s, const atx_camera* c)
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        if (!c) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_set_camera: null camera");
+        s->g.camera = *c;
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_scene_set_settings(atx_scene* s, const atx_settings* st)
+{
+    return guarded([&]() -> atx_status {
+        NEED_SCENE(s);
+        if (!st) return atx::fail(ATX_ERR_INVALID_ARG, "atx_scene_set_settings: null settings");
+        s->g.settings = *st;
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_set_scene_graph(atx_renderer* r, const atx_scene* s)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        NEED_SCENE(s);
+        std::vector<atx_sphere> v;
+        s->g.flatten(v);
+        return r->impl.set_scene(v.data(), (uint32_t)v.size(), s->g.materials.data(),
+                                 (uint32_t)s->g.materials.size(), s->g.lights.data(), (uint32_t)s->g.lights.size());
+    });
+}
+
+}  // extern "C"
+
 // ------------------------------------------------------------------ batches
 
 #include "batch_host.h"

@@ -374,6 +374,60 @@ ATX_API atx_status atx_render_noalloc(const atx_sphere* spheres, uint32_t n_sphe
                                       uint32_t frame_index, uint32_t spp, float* accumulation, uint32_t* image,
                                       void* stream);
 
+/* ----------------------------------------------------- scene files, graph */
+
+/* A scene as the reference stores it (Engine/include/Scene.h:58-75): a tree
+ * of nodes with a translation / rotation / scale and their own spheres
+ * (SceneNode.h:23-68), plus materials, lights, camera and settings.  Host
+ * only; no GPU is needed.  Node 0 is the root, named "Scene". */
+typedef struct atx_scene atx_scene;
+
+typedef struct atx_scene_info {
+    uint32_t n_spheres;      /* spheres of all nodes (the flattened count) */
+    uint32_t n_materials;
+    uint32_t n_lights;
+    uint32_t n_nodes;
+    atx_camera camera;       /* near/far are the Camera defaults 0.1 / 100 */
+    atx_settings settings;
+} atx_scene_info;
+
+/* Scene() (Scene.h:66): an empty root node, default camera and settings. */
+ATX_API atx_status atx_scene_create(atx_scene** out);
+ATX_API atx_status atx_scene_destroy(atx_scene* s);
+/* Utils::deserializeScene (Engine/src/Utils.cpp:97-173) of len bytes of JSON
+ * text.  Malformed text or a missing required key returns ATX_ERR_PARSE with
+ * the line, column or key in atx_last_error() (the reference throws). */
+ATX_API atx_status atx_scene_parse_json(const char* text, uint64_t len, atx_scene** out);
+/* Utils::importScene (Utils.cpp:175-187).  A file that cannot be opened
+ * returns ATX_ERR_NOT_FOUND (the reference returns an empty Scene). */
+ATX_API atx_status atx_scene_load(const char* path, atx_scene** out);
+/* Utils::serializeScene + dump(4) (Utils.cpp:3-51): writes at most cap bytes
+ * (no terminator) and the full length to *len; buf may be NULL to query. */
+ATX_API atx_status atx_scene_to_json(const atx_scene* s, char* buf, uint64_t cap, uint64_t* len);
+/* Utils::exportScene (Utils.cpp:53-62). */
+ATX_API atx_status atx_scene_save(const atx_scene* s, const char* path);
+ATX_API atx_status atx_scene_get_info(const atx_scene* s, atx_scene_info* info);
+/* World-space spheres as Renderer::allocateDeviceMemory collects them
+ * (Renderer.cu:25-37, 67-96): depth first, each node's centres through its
+ * global transform, radii times the mean column length of that transform,
+ * material indexes outside the material list set to 0.  cap >= n_spheres. */
+ATX_API atx_status atx_scene_flatten(const atx_scene* s, atx_sphere* out, uint64_t cap);
+ATX_API atx_status atx_scene_get_materials(const atx_scene* s, atx_material* out, uint64_t cap);
+ATX_API atx_status atx_scene_get_lights(const atx_scene* s, atx_light* out, uint64_t cap);
+/* Editing (SceneNode::addChild / setPosition / setRotation / setScale /
+ * addSphere, SceneNode.h:30-41).  rotation is a quaternion x, y, z, w. */
+ATX_API atx_status atx_scene_add_node(atx_scene* s, uint32_t parent, const char* name, uint32_t* node);
+ATX_API atx_status atx_scene_set_transform(atx_scene* s, uint32_t node, const float position[3],
+                                           const float rotation_xyzw[4], const float scale[3]);
+ATX_API atx_status atx_scene_add_spheres(atx_scene* s, uint32_t node, const atx_sphere* spheres, uint32_t n);
+ATX_API atx_status atx_scene_set_materials(atx_scene* s, const atx_material* materials, uint32_t n);
+ATX_API atx_status atx_scene_set_lights(atx_scene* s, const atx_light* lights, uint32_t n);
+ATX_API atx_status atx_scene_set_camera(atx_scene* s, const atx_camera* camera);
+ATX_API atx_status atx_scene_set_settings(atx_scene* s, const atx_settings* settings);
+/* Renderer::allocateDeviceMemory for a scene graph: flattens s and uploads it
+ * as atx_set_scene does. */
+ATX_API atx_status atx_set_scene_graph(atx_renderer* r, const atx_scene* s);
+
 /* --------------------------------------------------------- host helpers */
 
 /* Camera.cpp:134-159 on the host for a width x height viewport: view, inverse
