@@ -9,6 +9,7 @@ All rendering runs in libatx.so on the GPU; there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 from typing import Sequence
 
@@ -23,6 +24,7 @@ __all__ = [
     "SPHERE_DTYPE", "MATERIAL_DTYPE", "LIGHT_DTYPE", "camera_matrices", "device_count",
     "SceneGraph", "ROOT", "import_scene", "export_scene", "scene_from_json", "scene_to_json",
     "importScene", "exportScene", "serializeScene", "deserializeScene",
+    "CameraController", "write_image", "write_pfm",
 ]
 
 
@@ -174,6 +176,61 @@ def _as_lights(x) -> np.ndarray:
     return a
 
 
+class CameraController:
+    """Camera::onUpdate (Camera.cpp:31-108) with the window input passed in: keeps the camera and the
+    previous cursor position (Camera::m_lastMousePos).  keys is a string of the held keys among
+    "WSADQE"; nothing moves unless the right mouse button is held."""
+
+    def __init__(self, camera: Camera | None = None, last_mouse=(0.0, 0.0)):
+        self.camera = camera or Camera()
+        self.last_mouse = (C.c_float * 2)(*[float(v) for v in last_mouse])
+
+    @staticmethod
+    def _input(mouse, right_button: bool, keys: str) -> N.CameraInput:
+        k = keys.upper()
+        return N.CameraInput((C.c_float * 2)(*[float(v) for v in mouse]), int(bool(right_button)),
+                             int("W" in k), int("S" in k), int("A" in k), int("D" in k), int("Q" in k),
+                             int("E" in k), 0)
+
+    def _apply(self, fn, *head, dt, mouse, right_button, keys) -> bool:
+        d = self.camera.desc()
+        inp = self._input(mouse, right_button, keys)
+        moved = C.c_int32(0)
+        N.check(fn(*head, C.byref(d), self.last_mouse, C.byref(inp), float(dt), C.byref(moved)))
+        self.camera = Camera(d.fov_deg, d.near_clip, d.far_clip, tuple(d.position), tuple(d.direction))
+        return bool(moved.value)
+
+    def on_update(self, dt: float, mouse=(0.0, 0.0), right_button: bool = False, keys: str = "") -> bool:
+        return self._apply(N.lib().atx_camera_on_update, dt=dt, mouse=mouse, right_button=right_button, keys=keys)
+
+    onUpdate = on_update
+
+
+def write_image(path, rgba8: np.ndarray, fmt: str | None = None):
+    """RGBA8 pixels (H, W) uint32 to a PPM (RGB) or PAM (RGBA) file, top row first (atx_write_rgba8)."""
+    a = np.ascontiguousarray(rgba8, dtype=np.uint32)
+    h, w = a.shape
+    f = _image_format(path, fmt)
+    if f == N.IMAGE_PFM:
+        raise ValueError("PFM files are written from the float accumulator (write_pfm)")
+    N.check(N.lib().atx_write_rgba8(os.fsencode(path), N.ptr(a), w, h, f))
+
+
+def write_pfm(path, accum: np.ndarray):
+    """Float4 accumulator (H, W, 4) to a PFM file of accumulated colour / frames (atx_write_pfm)."""
+    a = np.ascontiguousarray(accum, dtype=np.float32)
+    h, w = a.shape[:2]
+    N.check(N.lib().atx_write_pfm(os.fsencode(path), N.ptr(a), w, h))
+
+
+def _image_format(path, fmt) -> int:
+    ext = (fmt or os.path.splitext(os.fspath(path))[1].lstrip(".")).lower()
+    table = {"ppm": N.IMAGE_PPM, "pam": N.IMAGE_PAM, "pfm": N.IMAGE_PFM}
+    if ext not in table:
+        raise ValueError(f"unknown image format {ext!r} (ppm, pam, pfm)")
+    return table[ext]
+
+
 def device_count() -> int:
     n = C.c_int32(0)
     N.check(N.lib().atx_device_count(C.byref(n)))
@@ -285,6 +342,17 @@ class Renderer:
         s, m, l = _as_spheres(spheres), _as_materials(materials), _as_lights(lights)
         N.check(N.lib().atx_set_scene(self._h, N.ptr(s) if len(s) else None, len(s), N.ptr(m) if len(m) else None,
                                       len(m), N.ptr(l) if len(l) else None, len(l)))
+
+    def update_camera(self, controller: CameraController, dt: float, mouse=(0.0, 0.0), right_button: bool = False,
+                      keys: str = "") -> bool:
+        """Ataraxia::onUpdate (main.cpp:22-32): Camera::onUpdate, and when it moved, the new camera
+        with the frame index reset to 1 (atx_update_camera)."""
+        return controller._apply(N.lib().atx_update_camera, self._h, dt=dt, mouse=mouse,
+                                 right_button=right_button, keys=keys)
+
+    def save_image(self, path, fmt: str | None = None):
+        """The image (.ppm, .pam) or the accumulator (.pfm) written to a file (atx_save_image)."""
+        N.check(N.lib().atx_save_image(self._h, os.fsencode(path), _image_format(path, fmt)))
 
     def set_scene_graph(self, graph: SceneGraph):
         """Flattens the graph (Renderer.cu:67-96) and uploads it (atx_set_scene_graph)."""

@@ -46,6 +46,15 @@ class CameraDesc(C.Structure):
                 ("near_clip", C.c_float), ("far_clip", C.c_float)]
 
 
+class CameraInput(C.Structure):
+    _fields_ = [("mouse", C.c_float * 2), ("right_button", C.c_uint8), ("key_w", C.c_uint8), ("key_s", C.c_uint8),
+                ("key_a", C.c_uint8), ("key_d", C.c_uint8), ("key_q", C.c_uint8), ("key_e", C.c_uint8),
+                ("reserved", C.c_uint8)]
+
+
+IMAGE_PPM, IMAGE_PAM, IMAGE_PFM = 1, 2, 3
+
+
 class SceneInfo(C.Structure):
     _fields_ = [("n_spheres", C.c_uint32), ("n_materials", C.c_uint32), ("n_lights", C.c_uint32),
                 ("n_nodes", C.c_uint32), ("camera", CameraDesc), ("settings", Settings)]
@@ -195,6 +204,13 @@ SIGNATURES = {
     "atx_scene_set_camera": (_ST, [_P, C.POINTER(CameraDesc)]),
     "atx_scene_set_settings": (_ST, [_P, C.POINTER(Settings)]),
     "atx_set_scene_graph": (_ST, [_P, _P]),
+    "atx_camera_on_update": (_ST, [C.POINTER(CameraDesc), _F, C.POINTER(CameraInput), C.c_float,
+                                   C.POINTER(C.c_int32)]),
+    "atx_update_camera": (_ST, [_P, C.POINTER(CameraDesc), _F, C.POINTER(CameraInput), C.c_float,
+                                C.POINTER(C.c_int32)]),
+    "atx_write_rgba8": (_ST, [C.c_char_p, _P, _U32, _U32, C.c_int32]),
+    "atx_write_pfm": (_ST, [C.c_char_p, _P, _U32, _U32]),
+    "atx_save_image": (_ST, [_P, C.c_char_p, C.c_int32]),
 }
 
 _lib = None

@@ -2,6 +2,7 @@
 // wrapper checks its handle, clears the thread's last error and converts C++
 // exceptions into status codes so nothing unwinds across the C boundary.
 #include <new>
+#include <vector>
 
 #include "atx.h"
 #include "host_common.h"
@@ -277,6 +278,63 @@ ATX_API atx_status atx_trace_nearest(atx_renderer* r, const float* origins, cons
 ATX_API atx_status atx_primary_directions(atx_renderer* r, float* host_dirs, uint64_t n_pixels)
 {
     return guarded([&]() -> atx_status { NEED(r); return r->impl.primary_directions(host_dirs, n_pixels); });
+}
+
+ATX_API atx_status atx_camera_on_update(atx_camera* camera, float last_mouse[2], const atx_camera_input* input,
+                                        float dt, int32_t* moved)
+{
+    return guarded([&]() -> atx_status {
+        if (!camera || !last_mouse || !input)
+            return atx::fail(ATX_ERR_INVALID_ARG, "atx_camera_on_update: null pointer");
+        const bool m = atx::camera_on_update(*camera, last_mouse, *input, dt);
+        if (moved) *moved = m ? 1 : 0;
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_update_camera(atx_renderer* r, atx_camera* camera, float last_mouse[2],
+                                     const atx_camera_input* input, float dt, int32_t* moved)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        if (!camera || !last_mouse || !input)
+            return atx::fail(ATX_ERR_INVALID_ARG, "atx_update_camera: null pointer");
+        const bool m = atx::camera_on_update(*camera, last_mouse, *input, dt);
+        if (moved) *moved = m ? 1 : 0;
+        if (!m) return ATX_OK;
+        ATX_TRY(r->impl.set_camera(*camera));          // main.cpp:24-29
+        r->impl.reset_frame_index();
+        return ATX_OK;
+    });
+}
+
+ATX_API atx_status atx_write_rgba8(const char* path, const uint32_t* rgba8, uint32_t width, uint32_t height,
+                                   int32_t format)
+{
+    return guarded([&]() -> atx_status { return atx::write_rgba8(path, rgba8, width, height, format); });
+}
+
+ATX_API atx_status atx_write_pfm(const char* path, const float* accum, uint32_t width, uint32_t height)
+{
+    return guarded([&]() -> atx_status { return atx::write_pfm(path, accum, width, height); });
+}
+
+ATX_API atx_status atx_save_image(atx_renderer* r, const char* path, int32_t format)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        const uint32_t w = r->impl.width(), h = r->impl.height();
+        if (!w || !h) return atx::fail(ATX_ERR_INVALID_ARG, "atx_save_image: no image (call atx_resize)");
+        const uint64_t n = (uint64_t)w * h;
+        if (format == ATX_IMAGE_PFM) {
+            std::vector<float> acc(n * 4);
+            ATX_TRY(r->impl.read_accumulation(acc.data(), n));
+            return atx::write_pfm(path, acc.data(), w, h);
+        }
+        std::vector<uint32_t> img(n);
+        ATX_TRY(r->impl.read_image(img.data(), n));
+        return atx::write_rgba8(path, img.data(), w, h, format);
+    });
 }
 
 }  // extern "C"

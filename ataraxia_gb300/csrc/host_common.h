@@ -95,4 +95,10 @@ void camera_matrices(const atx_camera& cam, uint32_t width, uint32_t height, flo
                      float proj[16], float inv_proj[16]);
 void mat4_inverse(const float m[16], float out[16]);
 
+// Camera::onUpdate (Camera.cpp:31-108) with the input passed in (host_tools.cpp).
+bool camera_on_update(atx_camera& cam, float last_mouse[2], const atx_camera_input& in, float dt);
+// Image files (host_tools.cpp): ATX_IMAGE_PPM / ATX_IMAGE_PAM from RGBA8, PFM from float4 sums.
+atx_status write_rgba8(const char* path, const uint32_t* px, uint32_t w, uint32_t h, int format);
+atx_status write_pfm(const char* path, const float* acc, uint32_t w, uint32_t h);
+
 }  // namespace atx

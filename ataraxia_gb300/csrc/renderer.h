@@ -96,6 +96,8 @@ public:
     atx_status kernel_times(atx_kernel_times* out);
     void reset_kernel_times() { ktimes_ = atx_kernel_times{}; }
     cudaStream_t stream() const { return stream_; }
+    uint32_t width() const { return width_; }
+    uint32_t height() const { return height_; }
 
 private:
     atx_status activate() const;

@@ -428,6 +428,49 @@ ATX_API atx_status atx_scene_set_settings(atx_scene* s, const atx_settings* sett
  * as atx_set_scene does. */
 ATX_API atx_status atx_set_scene_graph(atx_renderer* r, const atx_scene* s);
 
+/* -------------------------------------------- interactive camera, files */
+
+/* The window input Camera::onUpdate polls (Engine/src/Camera.cpp:31-108 via
+ * Input::GetMousePosition / IsMouseButtonPressed / IsKeyPressed), passed in
+ * by the caller: cursor position in window pixels, the right mouse button
+ * (look / move mode) and the W S A D Q E keys, nonzero = held. */
+typedef struct atx_camera_input {
+    float mouse[2];
+    uint8_t right_button;
+    uint8_t key_w, key_s, key_a, key_d, key_q, key_e;
+    uint8_t reserved;
+} atx_camera_input;
+
+/* Camera::onUpdate (Camera.cpp:31-108): moves camera->position at 5 units/s
+ * along the direction, direction x up and up, and turns the direction by the
+ * mouse delta (0.002 per pixel, 0.3 rotation speed), only while the right
+ * button is held.  last_mouse is the caller-held previous cursor position
+ * (Camera::m_lastMousePos), updated on every call.  *moved = 1 when the
+ * camera changed. */
+ATX_API atx_status atx_camera_on_update(atx_camera* camera, float last_mouse[2], const atx_camera_input* input,
+                                        float dt, int32_t* moved);
+/* Ataraxia::onUpdate (Engine/src/main.cpp:22-32): atx_camera_on_update, and
+ * when the camera moved, atx_set_camera and atx_reset_frame_index on r so the
+ * next render restarts the accumulation. */
+ATX_API atx_status atx_update_camera(atx_renderer* r, atx_camera* camera, float last_mouse[2],
+                                     const atx_camera_input* input, float dt, int32_t* moved);
+
+#define ATX_IMAGE_PPM 1   /* binary PPM (P6), RGB, 8 bits */
+#define ATX_IMAGE_PAM 2   /* PAM (P7) RGB_ALPHA, 8 bits */
+#define ATX_IMAGE_PFM 3   /* PFM (PF), RGB float: accumulated colour / frames */
+
+/* Headless stand-ins for the reference's Vulkan image upload
+ * (Core/src/Image.cpp:183-271).  Buffer row 0 is the bottom of the picture
+ * (Camera.cpp:180-182); PPM/PAM files store the top row first, as the
+ * reference displays it (main.cpp:186-187), PFM the bottom row first.
+ * rgba8: width*height pixels A<<24 | B<<16 | G<<8 | R (Renderer.h:70-78);
+ * accum: width*height float4 sums with the frame count in w. */
+ATX_API atx_status atx_write_rgba8(const char* path, const uint32_t* rgba8, uint32_t width, uint32_t height,
+                                   int32_t format);
+ATX_API atx_status atx_write_pfm(const char* path, const float* accum, uint32_t width, uint32_t height);
+/* Reads the renderer's image (PPM, PAM) or accumulator (PFM) back and writes it. */
+ATX_API atx_status atx_save_image(atx_renderer* r, const char* path, int32_t format);
+
 /* --------------------------------------------------------- host helpers */
 
 /* Camera.cpp:134-159 on the host for a width x height viewport: view, inverse

@@ -193,6 +193,95 @@ void orc_camera_matrices(const float pos[3], const float dir[3], float fov_deg, 
     if (inv_view) orc_mat4_inverse(V, inv_view);
 }
 
+/* Camera::onUpdate (Camera.cpp:31-108) with the window's input passed in:
+ * mouse delta (pos - last) * 0.002; nothing moves unless the right button is
+ * held; W/S, A/D, Q/E move at speed 5 along direction, right = direction x up
+ * (not normalised) and up, the first key of each pair winning; a mouse delta
+ * turns the direction by normalize(angleAxis(-pitch, right) x
+ * angleAxis(-yaw, up)) with yaw/pitch = delta * 0.3.  Quaternions are
+ * (w, x, y, z); products, normalisation and rotation as glm states them
+ * (Hamilton product; q * v = v + 2 (w (q x v) + q x (q x v))).  Returns 1 when
+ * the camera moved. */
+typedef struct { float w, x, y, z; } orc_quat;
+
+static orc_quat q_angle_axis(float angle, const float axis[3])
+{
+    const float s = sinf(angle * 0.5f);
+    orc_quat q = { cosf(angle * 0.5f), axis[0] * s, axis[1] * s, axis[2] * s };
+    return q;
+}
+
+static orc_quat q_mul(orc_quat p, orc_quat q)
+{
+    orc_quat r;
+    r.w = p.w * q.w - p.x * q.x - p.y * q.y - p.z * q.z;
+    r.x = p.w * q.x + p.x * q.w + p.y * q.z - p.z * q.y;
+    r.y = p.w * q.y + p.y * q.w + p.z * q.x - p.x * q.z;
+    r.z = p.w * q.z + p.z * q.w + p.x * q.y - p.y * q.x;
+    return r;
+}
+
+static orc_quat q_normalize(orc_quat q)
+{
+    const float len = sqrtf((q.x * q.x + q.y * q.y) + (q.z * q.z + q.w * q.w));
+    if (len <= 0.0f) {
+        orc_quat one = { 1.0f, 0.0f, 0.0f, 0.0f };
+        return one;
+    }
+    const float inv = 1.0f / len;
+    orc_quat r = { q.w * inv, q.x * inv, q.y * inv, q.z * inv };
+    return r;
+}
+
+static void q_rotate(orc_quat q, const float v[3], float out[3])
+{
+    const float qv[3] = { q.x, q.y, q.z };
+    float uv[3], uuv[3];
+    v3_cross(qv, v, uv);
+    v3_cross(qv, uv, uuv);
+    for (int k = 0; k < 3; ++k) out[k] = v[k] + ((uv[k] * q.w) + uuv[k]) * 2.0f;
+}
+
+int orc_camera_on_update(float pos[3], float dir[3], float last_mouse[2], const float mouse[2], int right_button,
+                         const int keys[6], float dt)
+{
+    const float mdx = (mouse[0] - last_mouse[0]) * 0.002f;
+    const float mdy = (mouse[1] - last_mouse[1]) * 0.002f;
+    last_mouse[0] = mouse[0];
+    last_mouse[1] = mouse[1];
+    if (!right_button) return 0;
+    int moved = 0;
+    const float up[3] = { 0.0f, 1.0f, 0.0f };
+    float right[3];
+    v3_cross(dir, up, right);
+    const float speed = 5.0f;
+    /* keys: W S A D Q E; each pair is if / else if, as Camera.cpp:51-88 */
+    const float* axis[3] = { dir, right, up };
+    const float sign_first[3] = { 1.0f, -1.0f, -1.0f };   /* W: +dir, A: -right, Q: -up */
+    for (int a = 0; a < 3; ++a) {
+        float sign = 0.0f;
+        if (keys[2 * a]) sign = sign_first[a];
+        else if (keys[2 * a + 1]) sign = -sign_first[a];
+        if (sign == 0.0f) continue;
+        for (int k = 0; k < 3; ++k) {
+            const float step = (axis[a][k] * speed) * dt;
+            pos[k] = (sign > 0.0f) ? pos[k] + step : pos[k] - step;
+        }
+        moved = 1;
+    }
+    if (mdx != 0.0f || mdy != 0.0f) {
+        const float yaw = mdx * 0.3f, pitch = mdy * 0.3f;
+        const orc_quat q = q_normalize(q_mul(q_angle_axis(-pitch, right), q_angle_axis(-yaw, up)));
+        float nd[3];
+        q_rotate(q, dir, nd);
+        dir[0] = nd[0];
+        dir[1] = nd[1];
+        dir[2] = nd[2];
+        moved = 1;
+    }
+    return moved;
+}
+
 void orc_ray_dirs(int mode, const orc_view* view, float* out)
 {
     const uint32_t W = view->width, H = view->height;

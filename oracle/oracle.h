@@ -108,6 +108,11 @@ void orc_camera_matrices(const float pos[3], const float dir[3], float fov_deg, 
                          float view[16], float inv_view[16], float proj[16], float inv_proj[16]);
 void orc_mat4_inverse(const float m[16], float out[16]);
 
+/* Camera::onUpdate (Camera.cpp:31-108); keys = W, S, A, D, Q, E held.  Updates
+ * pos, dir and last_mouse; returns 1 when the camera moved. */
+int orc_camera_on_update(float pos[3], float dir[3], float last_mouse[2], const float mouse[2], int right_button,
+                         const int keys[6], float dt);
+
 /* Camera.cpp:161-195: W*H*3 floats, pixel x + y*W. */
 void orc_ray_dirs(int mode, const orc_view* view, float* out);
 

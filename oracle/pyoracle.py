@@ -92,6 +92,8 @@ def lib(contract: bool = False):
         h.orc_pack_rgba8.argtypes = [P, C.c_uint64, C.c_uint32, P]
         h.orc_pack_rgba8.restype = None
         h.orc_max_threads.restype = C.c_int
+        h.orc_camera_on_update.argtypes = [P, P, P, P, C.c_int, P, C.c_float]
+        h.orc_camera_on_update.restype = C.c_int
         _libs[path] = h
     return _libs[path]
 
@@ -192,6 +194,14 @@ def sincos2pi(u: float):
     c, s = C.c_float(), C.c_float()
     lib().orc_sincos2pi(u, C.byref(c), C.byref(s))
     return c.value, s.value
+
+
+def camera_on_update(position, direction, last_mouse, mouse, right_button: bool, keys: str, dt: float):
+    """Camera::onUpdate restated (orc_camera_on_update); returns (moved, position, direction, last_mouse)."""
+    pos, d, lm, m = f32vec(position), f32vec(direction), f32vec(last_mouse), f32vec(mouse)
+    k = np.array([int(c in keys.upper()) for c in "WSADQE"], dtype=np.int32)
+    moved = lib().orc_camera_on_update(_p(pos), _p(d), _p(lm), _p(m), int(bool(right_button)), _p(k), dt)
+    return bool(moved), pos, d, lm
 
 
 def cook_torrance(albedo, f0, metallic, roughness, n, v, l, mode=EXACT):
