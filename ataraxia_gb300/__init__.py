@@ -421,15 +421,16 @@ class Renderer:
 
 
 class Batch:
-    """Many scenes rendered together by one persistent kernel per pass (atx_batch_*).
+    """Many resident scenes rendered together (atx_batch_*): each pass runs every scene with pending
+    frames through the wavefront kernels on concurrent lanes, captured as one CUDA graph.
 
     add_scene(...) -> id; set_spp(id, spp); run() renders one pass for every scene with spp > 0.
     Each scene keeps the reference's per-scene frame semantics, so its results are bit-identical to
     rendering it alone with Renderer."""
 
     def __init__(self, device: int = 0, bvh_threshold: int = 0, bvh_leaf_size: int = 0, hbm_budget_bytes: int = 0,
-                 flags: int = 0):
-        cfg = N.Config(device, 0, 0, bvh_threshold, bvh_leaf_size, flags, hbm_budget_bytes)
+                 flags: int = 0, lane_wave_paths: int = 0):
+        cfg = N.Config(device, lane_wave_paths, 0, bvh_threshold, bvh_leaf_size, flags, hbm_budget_bytes)
         h = C.c_void_p()
         N.check(N.lib().atx_batch_create(C.byref(cfg), C.byref(h)))
         self._h = h
@@ -487,6 +488,11 @@ class Batch:
         N.check(N.lib().atx_batch_frame_index(self._h, i, C.byref(f)))
         return f.value
 
+    def set_camera(self, i: int, camera: Camera):
+        """New camera for scene i; its accumulation restarts (atx_batch_set_camera)."""
+        d = camera.desc()
+        N.check(N.lib().atx_batch_set_camera(self._h, i, C.byref(d)))
+
     def run(self):
         N.check(N.lib().atx_batch_run(self._h))
 
@@ -510,8 +516,8 @@ class Batch:
         N.check(N.lib().atx_batch_get_stats(self._h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in N.BatchStats._fields_}
 
-    def set_tuning(self, tile_w=0, tile_h=0, threads=0, bvh_threshold=0, bvh_leaf_size=0):
-        t = N.BatchTuning(tile_w, tile_h, threads, bvh_threshold, bvh_leaf_size, (C.c_uint32 * 3)())
+    def set_tuning(self, lanes=0, lane_wave_paths=0, threads=0, bvh_threshold=0, bvh_leaf_size=0):
+        t = N.BatchTuning(lanes, lane_wave_paths, threads, bvh_threshold, bvh_leaf_size, (C.c_uint32 * 3)())
         N.check(N.lib().atx_batch_set_tuning(self._h, C.byref(t)))
 
     def tuning(self) -> dict:

@@ -88,11 +88,11 @@ class BatchStats(C.Structure):
     _fields_ = [("passes", C.c_uint64), ("paths", C.c_uint64), ("extension_rays", C.c_uint64),
                 ("shadow_rays", C.c_uint64), ("kernel_launches", C.c_uint64), ("graph_launches", C.c_uint64),
                 ("device_bytes", C.c_uint64), ("last_pass_ms", C.c_double), ("scenes", C.c_uint32),
-                ("items_last_pass", C.c_uint32)]
+                ("waves_last_pass", C.c_uint32)]
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("threads", C.c_uint32),
+    _fields_ = [("lanes", C.c_uint32), ("lane_wave_paths", C.c_uint32), ("threads", C.c_uint32),
                 ("bvh_threshold", C.c_uint32), ("bvh_leaf_size", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
@@ -170,6 +170,7 @@ SIGNATURES = {
     "atx_batch_read_image": (_ST, [_P, _U32, _P, _U64]),
     "atx_batch_get_stats": (_ST, [_P, C.POINTER(BatchStats)]),
     "atx_batch_set_tuning": (_ST, [_P, C.POINTER(BatchTuning)]),
+    "atx_batch_set_camera": (_ST, [_P, _U32, C.POINTER(CameraDesc)]),
     "atx_batch_get_tuning": (_ST, [_P, C.POINTER(BatchTuning)]),
     "atx_server_create": (_ST, [C.POINTER(ServerConfig), C.POINTER(_P)]),
     "atx_server_destroy": (_ST, [_P]),

@@ -1,5 +1,5 @@
-// Host side of the batched persistent renderer: resident per-scene state,
-// the per-pass work-item table and its CUDA-graph replay.
+// Batched renderer (batch_host.h): resident scenes, lanes of concurrent
+// streams, one captured CUDA graph per pass.
 #include "batch_host.h"
 
 #include <algorithm>
@@ -9,9 +9,20 @@
 namespace atx {
 
 namespace {
-constexpr uint32_t kDefaultTileW = 32, kDefaultTileH = 32;
+constexpr uint32_t kDefaultLanes = 8;
+constexpr uint32_t kMaxLanes = 64;
+constexpr uint32_t kDefaultLaneWavePaths = 8u << 20;   // 8 Mi paths (about 1.1 GB of path state) per lane
 constexpr uint32_t kDefaultBvhThreshold = 1024;
-constexpr uint32_t kBatchSmemCap = 4096;   // spheres a CTA stages (64 KB)
+
+// Relative device time of one pass of a scene: paths x (1 + B/2) rays, each
+// N brute-force tests or an LBVH walk, plus a fixed cost per dependent launch
+// (about B + 3 per wave).  Only the order of the estimates matters (LPT).
+double pass_cost(const SceneView& sc, uint64_t paths, int32_t bounces)
+{
+    const double b = std::max(0, bounces);
+    const double per_ray = sc.use_bvh ? 100.0 * std::log2((double)sc.n_sph + 2.0) : (double)sc.n_sph + 8.0;
+    return (double)paths * (1.0 + 0.5 * b) * per_ray + 2.0e7 * (b + 3.0);
+}
 }  // namespace
 
 Batch::Batch(const atx_config& cfg) : cfg_(cfg), budget_(cfg.hbm_budget_bytes) {}
@@ -20,10 +31,17 @@ Batch::~Batch()
 {
     if (cudaSetDevice(cfg_.device) == cudaSuccess) {
         if (stream_) cudaStreamSynchronize(stream_);
+        for (Lane& l : lanes_)
+            if (l.stream) cudaStreamSynchronize(l.stream);
         if (graph_) cudaGraphExecDestroy(graph_);
         slots_.clear();
-        if (h_scenes_) cudaFreeHost(h_scenes_);
-        if (h_items_) cudaFreeHost(h_items_);
+        for (Lane& l : lanes_) {
+            l.wave.buf.reset();
+            if (l.done) cudaEventDestroy(l.done);
+            if (l.stream) cudaStreamDestroy(l.stream);
+        }
+        totals_.reset();
+        if (fork_) cudaEventDestroy(fork_);
         if (ev0_) cudaEventDestroy(ev0_);
         if (ev1_) cudaEventDestroy(ev1_);
         if (stream_) cudaStreamDestroy(stream_);
@@ -41,13 +59,14 @@ atx_status Batch::init()
     if (cfg_.device < 0 || cfg_.device >= count) return fail(ATX_ERR_INVALID_ARG, "device %d out of range", cfg_.device);
     ATX_CUDA(cudaSetDevice(cfg_.device));
     ATX_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    ATX_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
     ATX_CUDA(cudaEventCreate(&ev0_));
     ATX_CUDA(cudaEventCreate(&ev1_));
-    ATX_TRY(counters_.ensure(64, &budget_, "batch counters"));
-    ATX_CUDA(cudaMemsetAsync(counters_.get(), 0, 64, stream_));
-    tuning_.tile_w = kDefaultTileW;
-    tuning_.tile_h = kDefaultTileH;
-    tuning_.threads = 256;
+    ATX_TRY(totals_.ensure(2 * sizeof(unsigned long long), &scratch_, "ray totals"));
+    ATX_CUDA(cudaMemsetAsync(totals_.get(), 0, 2 * sizeof(unsigned long long), stream_));
+    tuning_.lanes = kDefaultLanes;
+    tuning_.lane_wave_paths = cfg_.wave_paths ? cfg_.wave_paths : kDefaultLaneWavePaths;
+    tuning_.threads = cfg_.threads;
     tuning_.bvh_threshold = cfg_.bvh_threshold ? cfg_.bvh_threshold : kDefaultBvhThreshold;
     tuning_.bvh_leaf_size = cfg_.bvh_leaf_size;
     return ATX_OK;
@@ -63,6 +82,8 @@ atx_status Batch::add_scene(const atx_batch_scene& d, uint32_t* id)
 {
     if (d.width == 0 || d.height == 0 || (uint64_t)d.width * d.height > 0xffffffffull)
         return fail(ATX_ERR_INVALID_ARG, "batch_add_scene: bad viewport %ux%u", d.width, d.height);
+    if (d.settings.max_bounces > 4096)
+        return fail(ATX_ERR_INVALID_ARG, "batch_add_scene: max_bounces %d above 4096", d.settings.max_bounces);
     ATX_CUDA(cudaSetDevice(cfg_.device));
     auto s = std::make_unique<Slot>();
     s->scene.bvh_threshold = tuning_.bvh_threshold;
@@ -72,20 +93,41 @@ atx_status Batch::add_scene(const atx_batch_scene& d, uint32_t* id)
     const uint64_t px = (uint64_t)d.width * d.height;
     ATX_TRY(s->accum.ensure(px * sizeof(float4), &budget_, "batch accumulator"));
     ATX_TRY(s->image.ensure(px * sizeof(uint32_t), &budget_, "batch image"));
+    ATX_CUDA(plan_launch(s->scene.view, cfg_.device, (int)tuning_.threads, &s->shape));
     s->w = d.width;
     s->h = d.height;
     s->settings = d.settings;
+    s->desc = d.camera;
     camera_matrices(d.camera, d.width, d.height, nullptr, s->cam.inv_view, nullptr, s->cam.inv_proj);
     std::memcpy(s->cam.pos, d.camera.position, sizeof(s->cam.pos));
     s->cam.width = d.width;
     s->cam.height = d.height;
-    // reuse a free slot id
-    uint32_t i = 0;
+    uint32_t i = 0;   // reuse a free id
     while (i < slots_.size() && slots_[i]) ++i;
     if (i == slots_.size()) slots_.emplace_back();
     slots_[i] = std::move(s);
     *id = i;
     return ATX_OK;
+}
+
+void Batch::drop_graph()
+{
+    if (graph_) {
+        cudaStreamSynchronize(stream_);
+        cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+    }
+}
+
+void Batch::release_scratch()
+{
+    drop_graph();
+    for (Lane& l : lanes_) {
+        if (l.stream) cudaStreamSynchronize(l.stream);
+        l.wave.buf.reset();
+        l.wave.view = WaveState{};
+        l.wave.bounces = 0;
+    }
 }
 
 atx_status Batch::remove_scene(uint32_t id)
@@ -95,6 +137,9 @@ atx_status Batch::remove_scene(uint32_t id)
     ATX_CUDA(cudaSetDevice(cfg_.device));
     ATX_CUDA(cudaStreamSynchronize(stream_));
     slots_[id].reset();
+    bool any = false;
+    for (auto& p : slots_) any = any || (p != nullptr);
+    if (!any) release_scratch();   // an empty batch holds no path state
     return ATX_OK;
 }
 
@@ -122,183 +167,167 @@ atx_status Batch::frame_index(uint32_t id, uint32_t* f)
     return ATX_OK;
 }
 
-atx_status Batch::set_tuning(const atx_batch_tuning& t)
+atx_status Batch::set_camera(uint32_t id, const atx_camera& c)
 {
-    if (t.tile_w) tuning_.tile_w = t.tile_w;
-    if (t.tile_h) tuning_.tile_h = t.tile_h;
-    if (t.threads) tuning_.threads = std::min<uint32_t>(256, std::max<uint32_t>(32, t.threads & ~31u));
-    if (t.bvh_threshold) tuning_.bvh_threshold = t.bvh_threshold;
-    if (t.bvh_leaf_size) tuning_.bvh_leaf_size = t.bvh_leaf_size;
-    shape_valid_ = false;
+    Slot* s = slot(id);
+    if (!s) return fail(ATX_ERR_NOT_FOUND, "batch: no scene %u", id);
+    s->desc = c;
+    camera_matrices(c, s->w, s->h, nullptr, s->cam.inv_view, nullptr, s->cam.inv_proj);
+    std::memcpy(s->cam.pos, c.position, sizeof(s->cam.pos));
+    s->frame = 1;   // a moved camera restarts the accumulation (main.cpp:24-29)
     return ATX_OK;
 }
 
-// Relative cost of one path of a scene (a model for ordering work items,
-// largest first): ~(1 + bounces/2) rays, each N brute-force tests or a
-// logarithmic LBVH walk.
-static double path_cost(const SceneView& sc, int32_t bounces, int mode)
+atx_status Batch::set_tuning(const atx_batch_tuning& t)
 {
-    const double rays = 1.0 + 0.5 * std::max(0, bounces);
-    const double per_ray = mode == 2 ? 24.0 * std::log2((double)sc.n_sph + 2.0) : (double)sc.n_sph + 8.0;
-    return rays * per_ray;
+    ATX_CUDA(cudaSetDevice(cfg_.device));
+    if (t.lanes) tuning_.lanes = std::min(t.lanes, kMaxLanes);
+    if (t.lane_wave_paths && t.lane_wave_paths != tuning_.lane_wave_paths) {
+        tuning_.lane_wave_paths = std::max<uint32_t>(t.lane_wave_paths, 1u << 16);
+        release_scratch();
+    }
+    if (t.threads && t.threads != tuning_.threads) {
+        tuning_.threads = std::min<uint32_t>(1024, std::max<uint32_t>(32, t.threads & ~31u));
+        for (auto& p : slots_)
+            if (p) ATX_CUDA(plan_launch(p->scene.view, cfg_.device, (int)tuning_.threads, &p->shape));
+    }
+    if (t.bvh_threshold) tuning_.bvh_threshold = t.bvh_threshold;   // scenes added from now on
+    if (t.bvh_leaf_size) tuning_.bvh_leaf_size = t.bvh_leaf_size;
+    return ATX_OK;
+}
+
+atx_status Batch::ensure_lanes(uint32_t n)
+{
+    while (lanes_.size() < n) {
+        Lane l;
+        ATX_CUDA(cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking));
+        ATX_CUDA(cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming));
+        lanes_.push_back(std::move(l));
+    }
+    return ATX_OK;
 }
 
 atx_status Batch::run()
 {
     ATX_CUDA(cudaSetDevice(cfg_.device));
-    // the previous pass reads the pinned staging tables when it executes:
-    // let it finish before they are rewritten
-    ATX_CUDA(cudaStreamSynchronize(stream_));
-    // order scenes by item cost, largest first; a scene's tiles stay together
-    // so CTAs keep their staged sphere table
-    struct Act { uint32_t id; double cost; };
-    std::vector<Act> act;
-    uint32_t smem_need = 0;
+    struct Work {
+        uint32_t id;
+        double cost;
+        uint32_t frame0;
+    };
+    std::vector<Work> work;
+    uint64_t paths = 0;
     for (uint32_t i = 0; i < slots_.size(); ++i) {
         Slot* s = slots_[i].get();
         if (!s || s->spp_next == 0) continue;
-        const SceneView& sc = s->scene.view;
-        s->mode = sc.use_bvh ? 2 : (sc.n_sph > 0 && sc.n_sph <= kBatchSmemCap ? 1 : 0);
-        if (s->mode == 1) smem_need = std::max(smem_need, sc.n_sph);
-        const double c = path_cost(sc, s->settings.max_bounces, s->mode) * s->spp_next * tuning_.tile_w *
-                         tuning_.tile_h;
-        act.push_back({i, c});
+        const uint64_t p = (uint64_t)s->w * s->h * s->spp_next;
+        work.push_back({i, pass_cost(s->scene.view, p, s->settings.max_bounces), 0});
+        paths += p;
     }
-    std::stable_sort(act.begin(), act.end(), [](const Act& a, const Act& b) { return a.cost > b.cost; });
-
-    const uint32_t n_sc = (uint32_t)act.size();
-    uint64_t n_items = 0;
-    for (const Act& a : act) {
-        const Slot* s = slots_[a.id].get();
-        n_items += (uint64_t)((s->w + tuning_.tile_w - 1) / tuning_.tile_w) * ((s->h + tuning_.tile_h - 1) / tuning_.tile_h);
-    }
-    if (n_items > 0xffffffffull) return fail(ATX_ERR_INVALID_ARG, "batch: too many work items");
     ++st_.passes;
-    st_.items_last_pass = (uint32_t)n_items;
-    if (n_sc == 0) return ATX_OK;
+    st_.waves_last_pass = 0;
+    if (work.empty()) return ATX_OK;
 
-    // staging (pinned, so a captured graph reads the current contents)
-    if (n_sc > cap_scenes_) {
-        if (h_scenes_) cudaFreeHost(h_scenes_);
-        cap_scenes_ = std::max<uint32_t>(n_sc, 2 * cap_scenes_);
-        ATX_CUDA(cudaMallocHost(&h_scenes_, cap_scenes_ * sizeof(BatchSceneDev)));
-        ATX_TRY(d_scenes_.ensure(cap_scenes_ * sizeof(BatchSceneDev), &budget_, "batch scene table"));
-        invalidate_graph();
+    // longest first onto the least-loaded lane
+    std::stable_sort(work.begin(), work.end(), [](const Work& a, const Work& b) { return a.cost > b.cost; });
+    const uint32_t nl = std::min<uint32_t>(std::max<uint32_t>(tuning_.lanes, 1u), (uint32_t)work.size());
+    ATX_TRY(ensure_lanes(nl));
+    std::vector<std::vector<uint32_t>> plan(nl);
+    std::vector<double> load(nl, 0.0);
+    for (uint32_t k = 0; k < work.size(); ++k) {
+        const uint32_t lane = (uint32_t)(std::min_element(load.begin(), load.end()) - load.begin());
+        plan[lane].push_back(k);
+        load[lane] += work[k].cost;
     }
-    if (n_items > cap_items_) {
-        if (h_items_) cudaFreeHost(h_items_);
-        cap_items_ = std::max<uint64_t>(n_items, 2 * cap_items_);
-        ATX_CUDA(cudaMallocHost(&h_items_, cap_items_ * 2 * sizeof(uint32_t)));
-        ATX_TRY(d_items_.ensure(cap_items_ * 2 * sizeof(uint32_t), &budget_, "batch work items"));
-        invalidate_graph();
+    // path state: one buffer per lane, deep enough for its deepest scene
+    for (uint32_t l = 0; l < nl; ++l) {
+        int32_t maxb = 0;
+        for (uint32_t k : plan[l]) maxb = std::max(maxb, slots_[work[k].id]->settings.max_bounces);
+        Lane& ln = lanes_[l];
+        if (ln.wave.view.capacity < tuning_.lane_wave_paths || ln.wave.bounces < (uint32_t)maxb) drop_graph();
+        ATX_TRY(ln.wave.ensure(tuning_.lane_wave_paths, (uint32_t)maxb, &scratch_));
+        ln.wave.view.totals = totals_.as<unsigned long long>();
     }
-    uint32_t* item_scene = static_cast<uint32_t*>(h_items_);
-    uint32_t* item_tile = item_scene + cap_items_;
-    uint64_t k = 0;
-    uint64_t paths = 0;
-    for (uint32_t j = 0; j < n_sc; ++j) {
-        Slot* s = slots_[act[j].id].get();
-        BatchSceneDev& d = h_scenes_[j];
-        d.sc = s->scene.view;
-        d.cam = s->cam;
-        d.accum = s->accum.as<float4>();
-        d.image = s->image.as<uint32_t>();
-        d.max_bounces = s->settings.max_bounces;
-        d.sky = s->settings.sky_light ? 1 : 0;
-        if (!s->settings.accumulation) s->frame = 1;   // Renderer.cu:245-248
-        d.frame0 = s->frame;
-        d.spp = s->spp_next;
-        d.tile_w = tuning_.tile_w;
-        d.tile_h = tuning_.tile_h;
-        d.tiles_x = (s->w + tuning_.tile_w - 1) / tuning_.tile_w;
-        d.mode = s->mode;
-        const uint32_t tiles = d.tiles_x * ((s->h + tuning_.tile_h - 1) / tuning_.tile_h);
-        for (uint32_t t = 0; t < tiles; ++t, ++k) {
-            item_scene[k] = j;
-            item_tile[k] = t;
-        }
-        paths += (uint64_t)s->w * s->h * s->spp_next;
+    // frame bookkeeping (Renderer.cu:175-182, 245-248): this pass renders
+    // frames [frame0, frame0 + spp) of each scene
+    for (Work& w : work) {
+        Slot* s = slots_[w.id].get();
+        if (!s->settings.accumulation) s->frame = 1;
+        w.frame0 = s->frame;
         s->frame = s->settings.accumulation ? s->frame + s->spp_next : 1u;
     }
 
-    if (!shape_valid_ || smem_need > shape_smem_) {
-        shape_smem_ = std::max(smem_need, 256u);
-        ATX_CUDA(batch_plan(cfg_.device, (int)tuning_.threads, shape_smem_, &shape_));
-        shape_valid_ = true;
-        invalidate_graph();
-    }
-
-    BatchDev b;
-    b.scenes = d_scenes_.as<BatchSceneDev>();
-    b.item_scene = d_items_.as<uint32_t>();
-    b.item_tile = d_items_.as<uint32_t>() + cap_items_;
-    b.n_items = (uint32_t)n_items;
-    b.next_item = counters_.as<uint32_t>();
-    b.rays = reinterpret_cast<unsigned long long*>(counters_.as<char>() + 16);
-    b.smem_cap = shape_smem_;
-
     const bool graphs = !(cfg_.flags & ATX_FLAG_NO_GRAPHS);
-    if (graphs && graph_ && graph_scenes_ == n_sc && graph_items_ == n_items) {
+    uint32_t launches = 0, waves = 0;
+    uint64_t prim = 0;
+    auto enqueue = [&]() -> atx_status {
+        ATX_CUDA(cudaEventRecord(fork_, stream_));
+        for (uint32_t l = 0; l < nl; ++l) {
+            Lane& ln = lanes_[l];
+            ATX_CUDA(cudaStreamWaitEvent(ln.stream, fork_, 0));
+            for (uint32_t k : plan[l]) {
+                Slot* s = slots_[work[k].id].get();
+                const uint64_t px = (uint64_t)s->w * s->h;
+                if (work[k].frame0 == 1) {
+                    ATX_CUDA(enqueue_clear_accum(s->accum.as<float4>(), px, ln.stream));
+                    ++launches;
+                }
+                const WavePlan wp = plan_waves(px, s->spp_next, ln.wave.view.capacity);
+                waves += (uint32_t)(((px + wp.pixels_per_wave - 1) / wp.pixels_per_wave) *
+                                    ((s->spp_next + wp.spp_per_wave - 1) / wp.spp_per_wave));
+                ATX_TRY(enqueue_frames(s->scene.view, s->cam, ln.wave, s->shape, work[k].frame0, s->spp_next,
+                                       s->settings.max_bounces, s->settings.sky_light ? 1 : 0, s->accum.as<float4>(),
+                                       s->image.as<uint32_t>(), ln.wave.view.capacity, ln.stream, &launches, nullptr,
+                                       &prim));
+            }
+            ATX_CUDA(cudaEventRecord(ln.done, ln.stream));
+            ATX_CUDA(cudaStreamWaitEvent(stream_, ln.done, 0));
+        }
+        return ATX_OK;
+    };
+
+    if (graphs) {
+        ATX_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        const atx_status st = enqueue();
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(stream_, &g);
+        if (st != ATX_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            (void)cudaGetLastError();
+            drop_graph();
+            return st != ATX_OK ? st : cuda_fail(e, "batch pass capture");
+        }
+        bool updated = false;
+        if (graph_) {
+            cudaGraphExecUpdateResultInfo info{};
+            updated = cudaGraphExecUpdate(graph_, g, &info) == cudaSuccess;
+            if (!updated) {
+                (void)cudaGetLastError();
+                drop_graph();
+            }
+        }
+        cudaError_t ie = cudaSuccess;
+        if (!updated) ie = cudaGraphInstantiate(&graph_, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            graph_ = nullptr;
+            return cuda_fail(ie, "batch graph instantiate");
+        }
         ATX_CUDA(cudaEventRecord(ev0_, stream_));
         ATX_CUDA(cudaGraphLaunch(graph_, stream_));
         ATX_CUDA(cudaEventRecord(ev1_, stream_));
         ++st_.graph_launches;
     } else {
-        invalidate_graph();
-        if (graphs) ATX_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = enqueue_pass(b, n_sc, n_items);
-        if (graphs) {
-            cudaGraph_t g = nullptr;
-            cudaError_t e2 = cudaStreamEndCapture(stream_, &g);
-            if (e == cudaSuccess) e = e2;
-            if (e == cudaSuccess) e = cudaGraphInstantiate(&graph_, g, 0);
-            if (g) cudaGraphDestroy(g);
-            if (e != cudaSuccess) {
-                graph_ = nullptr;
-                return cuda_fail(e, "batch graph capture");
-            }
-            graph_scenes_ = n_sc;
-            graph_items_ = n_items;
-            ATX_CUDA(cudaEventRecord(ev0_, stream_));
-            ATX_CUDA(cudaGraphLaunch(graph_, stream_));
-            ATX_CUDA(cudaEventRecord(ev1_, stream_));
-        } else {
-            if (e != cudaSuccess) return cuda_fail(e, "batch pass");
-        }
+        ATX_CUDA(cudaEventRecord(ev0_, stream_));
+        ATX_TRY(enqueue());
+        ATX_CUDA(cudaEventRecord(ev1_, stream_));
     }
     timed_ = true;
     st_.paths += paths;
-    st_.kernel_launches += 1;
+    st_.kernel_launches += launches;
+    st_.waves_last_pass = waves;
+    primary_rays_ += prim;
     return ATX_OK;
-}
-
-cudaError_t Batch::enqueue_pass(const BatchDev& b, uint32_t n_sc, uint64_t n_items)
-{
-    const bool graphs = !(cfg_.flags & ATX_FLAG_NO_GRAPHS);
-    if (!graphs) {
-        cudaError_t e = cudaEventRecord(ev0_, stream_);
-        if (e != cudaSuccess) return e;
-    }
-    cudaError_t e = cudaMemcpyAsync(d_scenes_.get(), h_scenes_, n_sc * sizeof(BatchSceneDev), cudaMemcpyHostToDevice,
-                                    stream_);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_items_.get(), h_items_, n_items * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_items_.as<uint32_t>() + cap_items_, static_cast<uint32_t*>(h_items_) + cap_items_,
-                            n_items * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_);
-    if (e == cudaSuccess) e = cudaMemsetAsync(counters_.get(), 0, sizeof(uint32_t), stream_);
-    if (e == cudaSuccess) e = enqueue_batch(b, shape_, stream_);
-    if (!graphs && e == cudaSuccess) e = cudaEventRecord(ev1_, stream_);
-    return e;
-}
-
-void Batch::invalidate_graph()
-{
-    if (graph_) {
-        cudaStreamSynchronize(stream_);
-        cudaGraphExecDestroy(graph_);
-        graph_ = nullptr;
-    }
 }
 
 atx_status Batch::synchronize()
@@ -335,16 +364,16 @@ atx_status Batch::stats(atx_batch_stats* out)
     ATX_CUDA(cudaSetDevice(cfg_.device));
     ATX_CUDA(cudaStreamSynchronize(stream_));
     unsigned long long rays[2] = {0, 0};
-    ATX_CUDA(cudaMemcpy(rays, counters_.as<char>() + 16, sizeof(rays), cudaMemcpyDeviceToHost));
+    ATX_CUDA(cudaMemcpy(rays, totals_.get(), sizeof(rays), cudaMemcpyDeviceToHost));
     if (timed_) {
         float ms = 0.0f;
         ATX_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
         st_.last_pass_ms = ms;
     }
     *out = st_;
-    out->extension_rays = rays[0];
+    out->extension_rays = primary_rays_ + rays[0];
     out->shadow_rays = rays[1];
-    out->device_bytes = budget_.used();
+    out->device_bytes = budget_.used() + scratch_.used();
     uint32_t n = 0;
     for (auto& s : slots_) n += s ? 1 : 0;
     out->scenes = n;

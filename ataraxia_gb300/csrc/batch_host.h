@@ -1,5 +1,19 @@
-// Batched persistent renderer: many resident scenes, one persistent launch per
-// pass (batch.cu), the pass replayed from a captured CUDA graph.
+// Batched renderer: many resident scenes rendered together, one pass at a
+// time.  No counterpart in the reference, which renders one scene per
+// kernelRender launch (Renderer.cu:223) and synchronises after each frame.
+//
+// Each scene keeps its device state between passes (scene tables, LBVH,
+// float4 accumulator, RGBA8 image, frame index).  A pass renders every scene
+// with pending frames through the same wavefront kernels as the single-scene
+// renderer (enqueue_frames), so a scene's results are bit-identical to
+// rendering it alone.  Scenes are spread over `lanes` CUDA streams, each with
+// its own path-state buffer: a lane renders its scenes one after another while
+// the lanes run concurrently, so small scenes, the last bounces of a wave and
+// the tails of big launches overlap with other scenes' work instead of leaving
+// SMs idle.  Scenes are assigned to lanes longest-first by a cost model (LPT),
+// and the whole pass (fork, every lane's kernels, join) is captured as one
+// CUDA graph; passes with the same shape update the instantiated graph's
+// kernel arguments instead of re-instantiating it.
 #pragma once
 
 #include <cstdint>
@@ -7,7 +21,6 @@
 #include <vector>
 
 #include "atx.h"
-#include "batch.h"
 #include "host_common.h"
 #include "renderer.h"
 
@@ -24,6 +37,7 @@ public:
     atx_status set_spp(uint32_t id, uint32_t spp);
     atx_status reset(uint32_t id);
     atx_status frame_index(uint32_t id, uint32_t* f);
+    atx_status set_camera(uint32_t id, const atx_camera& c);
     atx_status run();
     atx_status synchronize();
     atx_status read_accumulation(uint32_t id, float* host, uint64_t n);
@@ -31,47 +45,49 @@ public:
     atx_status stats(atx_batch_stats* out);
     atx_status set_tuning(const atx_batch_tuning& t);
     atx_batch_tuning tuning() const { return tuning_; }
-    Budget& budget() { return budget_; }
+    // Device bytes held by resident scenes (charged to the configured budget).
+    uint64_t scene_bytes() const { return budget_.used(); }
+    // Device bytes of the lanes' path state (not charged to the budget).
+    uint64_t scratch_bytes() const { return scratch_.used(); }
     cudaStream_t stream() const { return stream_; }
 
 private:
     struct Slot {
         SceneStore scene;
         DeviceBuffer accum, image;
+        atx_camera desc{};
         CameraView cam{};
+        LaunchShape shape{};
         atx_settings settings{1, 0, {0, 0}, 15};
         uint32_t w = 0, h = 0;
         uint32_t frame = 1;
         uint32_t spp_next = 0;
-        int mode = 0;
+    };
+    struct Lane {
+        cudaStream_t stream = nullptr;
+        cudaEvent_t done = nullptr;
+        WaveStore wave;
     };
     Slot* slot(uint32_t id);
-    cudaError_t enqueue_pass(const BatchDev& b, uint32_t n_sc, uint64_t n_items);
-    void invalidate_graph();
+    atx_status ensure_lanes(uint32_t n);
+    void drop_graph();
+    void release_scratch();
 
     atx_config cfg_;
-    Budget budget_;
+    Budget budget_;      // resident scenes
+    Budget scratch_;     // lanes' path state
     cudaStream_t stream_ = nullptr;
-    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    cudaEvent_t fork_ = nullptr, ev0_ = nullptr, ev1_ = nullptr;
     bool timed_ = false;
     std::vector<std::unique_ptr<Slot>> slots_;
+    std::vector<Lane> lanes_;
+    DeviceBuffer totals_;
     atx_batch_tuning tuning_{};
 
-    BatchSceneDev* h_scenes_ = nullptr;   // pinned staging
-    void* h_items_ = nullptr;             // pinned: item_scene[cap], item_tile[cap]
-    uint32_t cap_scenes_ = 0;
-    uint64_t cap_items_ = 0;
-    DeviceBuffer d_scenes_, d_items_, counters_;
-
-    BatchShape shape_{};
-    bool shape_valid_ = false;
-    uint32_t shape_smem_ = 0;
-
     cudaGraphExec_t graph_ = nullptr;
-    uint32_t graph_scenes_ = 0;
-    uint64_t graph_items_ = 0;
 
     atx_batch_stats st_{};
+    uint64_t primary_rays_ = 0;
 };
 
 }  // namespace atx

@@ -649,6 +649,15 @@ ATX_API atx_status atx_batch_frame_index(atx_batch* b, uint32_t id, uint32_t* f)
     });
 }
 
+ATX_API atx_status atx_batch_set_camera(atx_batch* b, uint32_t id, const atx_camera* c)
+{
+    return guarded([&]() -> atx_status {
+        NEEDB(b);
+        if (!c) return atx::fail(ATX_ERR_INVALID_ARG, "atx_batch_set_camera: null camera");
+        return b->impl.set_camera(id, *c);
+    });
+}
+
 ATX_API atx_status atx_batch_run(atx_batch* b)
 {
     return guarded([&]() -> atx_status { NEEDB(b); return b->impl.run(); });

@@ -24,7 +24,7 @@ uint64_t up256(uint64_t x) { return (x + 255u) & ~uint64_t(255u); }
 
 bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
 
-// The batched persistent renderer.
+// The batched renderer.
 class BatchExecutor : public Executor {
 public:
     explicit BatchExecutor(const atx_config& cfg) : b_(cfg) {}
@@ -42,7 +42,7 @@ public:
     {
         return b_.read_accumulation(slot, host, n);
     }
-    uint64_t device_bytes() const override { return const_cast<Batch&>(b_).budget().used(); }
+    uint64_t device_bytes() const override { return b_.scene_bytes(); }
 
 private:
     Batch b_;

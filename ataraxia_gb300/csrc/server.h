@@ -1,5 +1,5 @@
 // Render server: continuous batching of progressive render jobs over the
-// batched persistent renderer (batch_host.h), or over a host-only simulated
+// batched renderer (batch_host.h), or over a host-only simulated
 // executor for scheduling tests on machines without a GPU.
 #pragma once
 

@@ -364,7 +364,7 @@ def time_reference_kernel(sc, cam, dev, args) -> dict:
 
 def run_batch_compare(args, dist: Dist):
     """The batched mix (64 scenes, seed 3): the plain wavefront renderer launched once per scene (device
-    time of the render calls only) against one persistent batched pass per step."""
+    time of the render calls only) against one batched pass (all scenes, one CUDA graph) per step."""
     import torch
 
     import ataraxia_gb300 as atx
@@ -395,9 +395,8 @@ def run_batch_compare(args, dist: Dist):
     r.close()
 
     b = atx.Batch(device=dev)
-    if args.tile:
-        tw, th = (int(x) for x in args.tile.split("x"))
-        b.set_tuning(tile_w=tw, tile_h=th)
+    if args.lanes or args.lane_wave:
+        b.set_tuning(lanes=args.lanes, lane_wave_paths=args.lane_wave << 20)
     ids = [b.add_synthetic(sc) for sc in mix]
     for i, sc in zip(ids, mix):
         b.set_spp(i, sc.spp)
@@ -653,7 +652,8 @@ def main(argv=None) -> int:
     ap.add_argument("--max-pending", type=int, default=4096, help="serve mode: queue bound (then BUSY)")
     ap.add_argument("--pool", type=int, default=512, help="serve mode: scenes in the job pool")
     ap.add_argument("--no-fifo", action="store_true", help="serve mode: skip the FIFO baseline")
-    ap.add_argument("--tile", default="", help="batch mode: work-item tile WxH (default from the library)")
+    ap.add_argument("--lanes", type=int, default=0, help="batch mode: concurrent lanes (0 = library default)")
+    ap.add_argument("--lane-wave", type=int, default=0, help="batch mode: path state per lane, Mi paths")
     ap.add_argument("--width", type=int, default=0, help="render mode: override the viewport width")
     ap.add_argument("--height", type=int, default=0, help="render mode: override the viewport height")
     ap.add_argument("--workload", choices=["medium", "large", "small"], default="medium",

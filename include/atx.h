@@ -219,11 +219,14 @@ ATX_API atx_status atx_host_free(void* p);
 
 /* ---------------------------------------------------------------- batches */
 
-/* Many scenes rendered together by one persistent kernel per pass.  No
+/* Many resident scenes rendered together, one pass at a time.  No
  * counterpart in the reference, which renders one scene per kernelRender
- * launch (Renderer.cu:223); each scene keeps the reference's per-scene
- * semantics (frame index, accumulate/reset, seed = pixel * frame), so a
- * scene's images are bit-identical to rendering it alone with atx_render. */
+ * launch (Renderer.cu:223).  A pass runs every scene with pending frames
+ * through the single-scene wavefront kernels, spread over concurrent lanes
+ * (CUDA streams with their own path state) and captured as one CUDA graph;
+ * each scene keeps the reference's per-scene semantics (frame index,
+ * accumulate/reset, seed = pixel * frame), so a scene's images are
+ * bit-identical to rendering it alone with atx_render. */
 typedef struct atx_batch atx_batch;
 
 typedef struct atx_batch_scene {
@@ -248,13 +251,14 @@ typedef struct atx_batch_stats {
     uint64_t device_bytes;
     double last_pass_ms;        /* device time of the last pass */
     uint32_t scenes;            /* scenes held */
-    uint32_t items_last_pass;   /* (scene, tile) work items of the last pass */
+    uint32_t waves_last_pass;   /* path waves (each up to lane_wave_paths) of the last pass */
 } atx_batch_stats;
 
-/* Tuning knobs of the persistent kernel (0 = default / autotuned). */
+/* Tuning knobs (0 = keep the current value). */
 typedef struct atx_batch_tuning {
-    uint32_t tile_w, tile_h;    /* pixels per work item */
-    uint32_t threads;           /* threads per CTA */
+    uint32_t lanes;             /* concurrent streams, each with its own path state (default 8) */
+    uint32_t lane_wave_paths;   /* path-state capacity of one lane, paths (default 8 Mi = 1.1 GB) */
+    uint32_t threads;           /* threads per CTA of the wavefront kernels (0 = per-kernel default) */
     uint32_t bvh_threshold;     /* sphere count from which a scene uses its LBVH */
     uint32_t bvh_leaf_size;
     uint32_t reserved[3];
@@ -270,6 +274,9 @@ ATX_API atx_status atx_batch_remove_scene(atx_batch* b, uint32_t id);
 ATX_API atx_status atx_batch_set_spp(atx_batch* b, uint32_t id, uint32_t spp);
 ATX_API atx_status atx_batch_reset(atx_batch* b, uint32_t id);
 ATX_API atx_status atx_batch_frame_index(atx_batch* b, uint32_t id, uint32_t* frame_index);
+/* New camera for a scene (matrices as Camera.cpp:134-159); its accumulation
+ * restarts at frame 1, as the reference resets on camera motion (main.cpp:24-29). */
+ATX_API atx_status atx_batch_set_camera(atx_batch* b, uint32_t id, const atx_camera* camera);
 /* One pass: every scene with spp > 0 renders its frames; asynchronous. */
 ATX_API atx_status atx_batch_run(atx_batch* b);
 ATX_API atx_status atx_batch_synchronize(atx_batch* b);

@@ -1,4 +1,4 @@
-"""Batched persistent renderer: every scene's accumulator and image are bit-identical to rendering
+"""Batched renderer: every scene's accumulator and image are bit-identical to rendering
 the scene alone (Renderer / atx_render) and to the oracle, whatever else shares the pass."""
 import numpy as np
 import pytest
@@ -110,11 +110,12 @@ def test_accumulation_off_in_batch():
         assert bit_mismatches(b.get_accumulation(i), ref) == 0
 
 
-@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (64, 4)])
-def test_tunings_do_not_change_results(tile):
+@pytest.mark.parametrize("lanes,wave", [(1, 1 << 16), (3, 1 << 17), (16, 1 << 20)])
+def test_tunings_do_not_change_results(lanes, wave):
+    """Lane count and path-state size (down to several waves per scene) leave results unchanged."""
     mix = small_mix(3)
     with Batch() as b:
-        b.set_tuning(tile_w=tile[0], tile_h=tile[1])
+        b.set_tuning(lanes=lanes, lane_wave_paths=wave)
         ids = [b.add_synthetic(sc) for sc in mix]
         for i, sc in zip(ids, mix):
             b.set_spp(i, 3)
@@ -122,3 +123,20 @@ def test_tunings_do_not_change_results(tile):
         for i, sc in zip(ids, mix):
             ref, _ = alone(sc, 3)
             assert bit_mismatches(b.get_accumulation(i), ref) == 0
+        assert b.stats()["waves_last_pass"] >= len(mix)
+
+
+def test_set_camera_restarts_accumulation():
+    sc = small_mix(1)[0]
+    with Batch() as b:
+        i = b.add_synthetic(sc)
+        b.set_spp(i, 2)
+        b.run()
+        assert b.frame_index(i) == 3
+        cam = Camera(sc.fov, sc.near, sc.far, tuple(p + 0.5 for p in sc.camera_position), sc.camera_direction)
+        b.set_camera(i, cam)
+        assert b.frame_index(i) == 1
+        b.run()
+        moved = scenes.SyntheticScene(**{**sc.__dict__, "camera_position": cam.position})
+        ref, _ = alone(moved, 2)
+        assert bit_mismatches(b.get_accumulation(i), ref) == 0
