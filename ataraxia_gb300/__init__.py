@@ -538,17 +538,19 @@ def _batch_scene(spheres, materials, lights, camera: Camera, width: int, height:
 class Server:
     """Progressive render server with continuous batching (atx_server_*).
 
-    submit() copies the scene and returns a job id at once; a worker thread admits jobs in arrival order
-    when a slot and their device memory fit the HBM budget and renders all active jobs together, a slice
-    of frames per pass, until each reaches its target spp."""
+    submit() copies the scene and returns a job id at once; a worker thread admits jobs (policy "arrival":
+    in arrival order; "smallest": fewest pixel-samples first) when a slot and their device memory fit the
+    HBM budget and renders all active jobs together, a slice of frames per pass, until each reaches its
+    target spp.  Passes are pipelined: the next one is queued while the current one runs."""
 
     def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, max_active_jobs: int = 0, pass_spp: int = 0,
                  max_pass_paths: int = 0, max_pending: int = 0, bvh_threshold: int = 0, flags: int = 0,
-                 host_executor: bool = False, host_fail_pass: int = 0):
+                 host_executor: bool = False, host_fail_pass: int = 0, policy: str = "arrival"):
         if host_executor:
             flags |= N.FLAG_HOST_EXECUTOR
+        pol = {"arrival": N.ADMIT_ARRIVAL, "smallest": N.ADMIT_SMALLEST}[policy]
         cfg = N.ServerConfig(N.Config(device, 0, 0, bvh_threshold, 0, flags, hbm_budget_bytes), max_active_jobs,
-                             pass_spp, max_pass_paths, max_pending, host_fail_pass)
+                             pass_spp, max_pass_paths, max_pending, host_fail_pass, pol)
         h = C.c_void_p()
         N.check(N.lib().atx_server_create(C.byref(cfg), C.byref(h)))
         self._h = h
@@ -610,6 +612,11 @@ class Server:
 
     def cancel(self, job: int):
         N.check(N.lib().atx_server_cancel(self._h, job))
+
+    def set_camera(self, job: int, camera: Camera):
+        """New camera for a queued or active job: it restarts from frame 1 (atx_server_set_camera)."""
+        d = camera.desc()
+        N.check(N.lib().atx_server_set_camera(self._h, job, C.byref(d)))
 
     def release(self, job: int):
         N.check(N.lib().atx_server_release(self._h, job))

@@ -98,7 +98,11 @@ class BatchTuning(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("base", Config), ("max_active_jobs", C.c_uint32), ("pass_spp", C.c_uint32),
-                ("max_pass_paths", C.c_uint64), ("max_pending", C.c_uint32), ("host_fail_pass", C.c_uint32)]
+                ("max_pass_paths", C.c_uint64), ("max_pending", C.c_uint32), ("host_fail_pass", C.c_uint32),
+                ("policy", C.c_uint32)]
+
+
+ADMIT_ARRIVAL, ADMIT_SMALLEST = 0, 1
 
 
 class JobInfo(C.Structure):
@@ -180,6 +184,7 @@ SIGNATURES = {
     "atx_server_read_image": (_ST, [_P, _U32, _P, _U64]),
     "atx_server_read_accumulation": (_ST, [_P, _U32, _P, _U64]),
     "atx_server_cancel": (_ST, [_P, _U32]),
+    "atx_server_set_camera": (_ST, [_P, _U32, C.POINTER(CameraDesc)]),
     "atx_server_release": (_ST, [_P, _U32]),
     "atx_server_get_stats": (_ST, [_P, C.POINTER(ServerStats)]),
     "atx_server_now": (_ST, [_P, C.POINTER(C.c_double)]),

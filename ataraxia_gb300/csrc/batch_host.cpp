@@ -30,20 +30,25 @@ Batch::Batch(const atx_config& cfg) : cfg_(cfg), budget_(cfg.hbm_budget_bytes) {
 Batch::~Batch()
 {
     if (cudaSetDevice(cfg_.device) == cudaSuccess) {
+        if (up_stream_) cudaStreamSynchronize(up_stream_);
         if (stream_) cudaStreamSynchronize(stream_);
         for (Lane& l : lanes_)
             if (l.stream) cudaStreamSynchronize(l.stream);
         if (graph_) cudaGraphExecDestroy(graph_);
-        slots_.clear();
+        slots_.clear();   // stream-ordered frees on stream_
+        if (stream_) cudaStreamSynchronize(stream_);
         for (Lane& l : lanes_) {
             l.wave.buf.reset();
             if (l.done) cudaEventDestroy(l.done);
             if (l.stream) cudaStreamDestroy(l.stream);
         }
         totals_.reset();
+        if (pool_) cudaMemPoolDestroy(pool_);
         if (fork_) cudaEventDestroy(fork_);
         if (ev0_) cudaEventDestroy(ev0_);
         if (ev1_) cudaEventDestroy(ev1_);
+        if (uploaded_) cudaEventDestroy(uploaded_);
+        if (up_stream_) cudaStreamDestroy(up_stream_);
         if (stream_) cudaStreamDestroy(stream_);
     }
 }
@@ -59,7 +64,19 @@ atx_status Batch::init()
     if (cfg_.device < 0 || cfg_.device >= count) return fail(ATX_ERR_INVALID_ARG, "device %d out of range", cfg_.device);
     ATX_CUDA(cudaSetDevice(cfg_.device));
     ATX_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    ATX_CUDA(cudaStreamCreateWithFlags(&up_stream_, cudaStreamNonBlocking));
+    ATX_CUDA(cudaEventCreateWithFlags(&uploaded_, cudaEventDisableTiming));
     ATX_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+    // scenes come and go between passes: their memory comes from a pool that
+    // keeps freed blocks for reuse instead of returning them at every sync
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = cfg_.device;
+    ATX_CUDA(cudaMemPoolCreate(&pool_, &props));
+    uint64_t keep = ~0ull;
+    ATX_CUDA(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep));
+    order_ = StreamOrder{pool_, up_stream_, stream_};
     ATX_CUDA(cudaEventCreate(&ev0_));
     ATX_CUDA(cudaEventCreate(&ev1_));
     ATX_TRY(totals_.ensure(2 * sizeof(unsigned long long), &scratch_, "ray totals"));
@@ -88,11 +105,16 @@ atx_status Batch::add_scene(const atx_batch_scene& d, uint32_t* id)
     auto s = std::make_unique<Slot>();
     s->scene.bvh_threshold = tuning_.bvh_threshold;
     s->scene.bvh_leaf = tuning_.bvh_leaf_size;
+    s->scene.order = &order_;
+    s->accum.use_stream_order(&order_);
+    s->image.use_stream_order(&order_);
+    // on the upload stream: a pass running on the batch stream is not waited for
     ATX_TRY(s->scene.upload(d.spheres, d.n_spheres, d.materials, d.n_materials, d.lights, d.n_lights, &budget_,
-                            stream_));
+                            up_stream_));
     const uint64_t px = (uint64_t)d.width * d.height;
     ATX_TRY(s->accum.ensure(px * sizeof(float4), &budget_, "batch accumulator"));
     ATX_TRY(s->image.ensure(px * sizeof(uint32_t), &budget_, "batch image"));
+    ATX_CUDA(cudaEventRecord(uploaded_, up_stream_));
     ATX_CUDA(plan_launch(s->scene.view, cfg_.device, (int)tuning_.threads, &s->shape));
     s->w = d.width;
     s->h = d.height;
@@ -113,8 +135,7 @@ atx_status Batch::add_scene(const atx_batch_scene& d, uint32_t* id)
 void Batch::drop_graph()
 {
     if (graph_) {
-        cudaStreamSynchronize(stream_);
-        cudaGraphExecDestroy(graph_);
+        cudaGraphExecDestroy(graph_);   // a graph still running is freed when it completes
         graph_ = nullptr;
     }
 }
@@ -135,11 +156,7 @@ atx_status Batch::remove_scene(uint32_t id)
     Slot* s = slot(id);
     if (!s) return fail(ATX_ERR_NOT_FOUND, "batch: no scene %u", id);
     ATX_CUDA(cudaSetDevice(cfg_.device));
-    ATX_CUDA(cudaStreamSynchronize(stream_));
-    slots_[id].reset();
-    bool any = false;
-    for (auto& p : slots_) any = any || (p != nullptr);
-    if (!any) release_scratch();   // an empty batch holds no path state
+    slots_[id].reset();   // freed on the batch stream after the passes queued there
     return ATX_OK;
 }
 
@@ -207,7 +224,7 @@ atx_status Batch::ensure_lanes(uint32_t n)
     return ATX_OK;
 }
 
-atx_status Batch::run()
+atx_status Batch::run(cudaEvent_t done)
 {
     ATX_CUDA(cudaSetDevice(cfg_.device));
     struct Work {
@@ -226,7 +243,11 @@ atx_status Batch::run()
     }
     ++st_.passes;
     st_.waves_last_pass = 0;
-    if (work.empty()) return ATX_OK;
+    if (work.empty()) {
+        if (done) ATX_CUDA(cudaEventRecord(done, stream_));
+        return ATX_OK;
+    }
+    ATX_CUDA(cudaStreamWaitEvent(stream_, uploaded_, 0));   // scenes added since the last pass
 
     // longest first onto the least-loaded lane
     std::stable_sort(work.begin(), work.end(), [](const Work& a, const Work& b) { return a.cost > b.cost; });
@@ -257,7 +278,27 @@ atx_status Batch::run()
         s->frame = s->settings.accumulation ? s->frame + s->spp_next : 1u;
     }
 
-    const bool graphs = !(cfg_.flags & ATX_FLAG_NO_GRAPHS);
+    // The graph's shape: lanes, their scenes in order, whether each clears its
+    // accumulator, its waves and bounces.  A pass of the same shape as the
+    // last one replays the graph with updated kernel arguments; a pass of a
+    // new shape (scenes come and go in a server) is launched directly, since
+    // capturing and instantiating a graph used once costs more host time.
+    std::vector<uint64_t> sig;
+    for (uint32_t l = 0; l < nl; ++l) {
+        sig.push_back(0xffffffff00000000ull | l);
+        for (uint32_t k : plan[l]) {
+            const Slot* s = slots_[work[k].id].get();
+            const uint64_t px = (uint64_t)s->w * s->h;
+            const WavePlan wp = plan_waves(px, s->spp_next, lanes_[l].wave.view.capacity);
+            sig.push_back(work[k].id);
+            sig.push_back(((uint64_t)(work[k].frame0 == 1) << 63) | ((uint64_t)(uint32_t)s->settings.max_bounces << 32) |
+                          (((px + wp.pixels_per_wave - 1) / wp.pixels_per_wave) *
+                           ((s->spp_next + wp.spp_per_wave - 1) / wp.spp_per_wave)));
+        }
+    }
+    const bool graphs = !(cfg_.flags & ATX_FLAG_NO_GRAPHS) && sig == last_sig_;
+    last_sig_.swap(sig);
+    if (!graphs) drop_graph();
     uint32_t launches = 0, waves = 0;
     uint64_t prim = 0;
     auto enqueue = [&]() -> atx_status {
@@ -322,6 +363,7 @@ atx_status Batch::run()
         ATX_TRY(enqueue());
         ATX_CUDA(cudaEventRecord(ev1_, stream_));
     }
+    if (done) ATX_CUDA(cudaEventRecord(done, stream_));
     timed_ = true;
     st_.paths += paths;
     st_.kernel_launches += launches;
@@ -356,6 +398,18 @@ atx_status Batch::read_image(uint32_t id, uint32_t* host, uint64_t n)
     ATX_CUDA(cudaSetDevice(cfg_.device));
     ATX_CUDA(cudaMemcpyAsync(host, s->image.get(), n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
     ATX_CUDA(cudaStreamSynchronize(stream_));
+    return ATX_OK;
+}
+
+atx_status Batch::read_async(uint32_t id, uint32_t* image, float* accum, uint64_t n)
+{
+    Slot* s = slot(id);
+    if (!s) return fail(ATX_ERR_NOT_FOUND, "batch: no scene %u", id);
+    if (n > (uint64_t)s->w * s->h) return fail(ATX_ERR_INVALID_ARG, "batch read: %llu pixels > image",
+                                               (unsigned long long)n);
+    ATX_CUDA(cudaSetDevice(cfg_.device));
+    if (image) ATX_CUDA(cudaMemcpyAsync(image, s->image.get(), n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+    if (accum) ATX_CUDA(cudaMemcpyAsync(accum, s->accum.get(), n * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
     return ATX_OK;
 }
 

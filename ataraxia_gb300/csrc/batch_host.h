@@ -10,10 +10,11 @@
 // its own path-state buffer: a lane renders its scenes one after another while
 // the lanes run concurrently, so small scenes, the last bounces of a wave and
 // the tails of big launches overlap with other scenes' work instead of leaving
-// SMs idle.  Scenes are assigned to lanes longest-first by a cost model (LPT),
-// and the whole pass (fork, every lane's kernels, join) is captured as one
-// CUDA graph; passes with the same shape update the instantiated graph's
-// kernel arguments instead of re-instantiating it.
+// SMs idle.  Scenes are assigned to lanes longest-first by a cost model (LPT).
+// A pass with the same shape as the previous one (same scenes on the same
+// lanes, same waves) is captured as one CUDA graph (fork, every lane's
+// kernels, join) and replayed, the instantiated graph's kernel arguments
+// updated in place; a pass of a new shape is launched directly.
 #pragma once
 
 #include <cstdint>
@@ -38,10 +39,15 @@ public:
     atx_status reset(uint32_t id);
     atx_status frame_index(uint32_t id, uint32_t* f);
     atx_status set_camera(uint32_t id, const atx_camera& c);
-    atx_status run();
+    // One pass; `done`, if given, is recorded on the batch stream after it.
+    atx_status run(cudaEvent_t done = nullptr);
     atx_status synchronize();
     atx_status read_accumulation(uint32_t id, float* host, uint64_t n);
     atx_status read_image(uint32_t id, uint32_t* host, uint64_t n);
+    // Queues copies of a scene's image and accumulator (either may be null)
+    // after the passes already queued; complete when a later `done` event is.
+    // Host buffers should be page-locked for the copies to be asynchronous.
+    atx_status read_async(uint32_t id, uint32_t* image, float* accum, uint64_t n);
     atx_status stats(atx_batch_stats* out);
     atx_status set_tuning(const atx_batch_tuning& t);
     atx_batch_tuning tuning() const { return tuning_; }
@@ -76,7 +82,11 @@ private:
     atx_config cfg_;
     Budget budget_;      // resident scenes
     Budget scratch_;     // lanes' path state
-    cudaStream_t stream_ = nullptr;
+    cudaStream_t stream_ = nullptr;      // passes, read-backs, frees
+    cudaStream_t up_stream_ = nullptr;   // scene uploads and LBVH builds
+    cudaEvent_t uploaded_ = nullptr;     // after the last upload
+    cudaMemPool_t pool_ = nullptr;       // per-scene device memory, stream-ordered
+    StreamOrder order_{};
     cudaEvent_t fork_ = nullptr, ev0_ = nullptr, ev1_ = nullptr;
     bool timed_ = false;
     std::vector<std::unique_ptr<Slot>> slots_;
@@ -85,6 +95,7 @@ private:
     atx_batch_tuning tuning_{};
 
     cudaGraphExec_t graph_ = nullptr;
+    std::vector<uint64_t> last_sig_;   // shape of the last pass
 
     atx_batch_stats st_{};
     uint64_t primary_rays_ = 0;

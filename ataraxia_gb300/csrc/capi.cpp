@@ -783,6 +783,15 @@ ATX_API atx_status atx_server_cancel(atx_server* s, uint32_t job)
     return guarded([&]() -> atx_status { NEEDS(s); return s->impl.cancel(job); });
 }
 
+ATX_API atx_status atx_server_set_camera(atx_server* s, uint32_t job, const atx_camera* c)
+{
+    return guarded([&]() -> atx_status {
+        NEEDS(s);
+        if (!c) return atx::fail(ATX_ERR_INVALID_ARG, "atx_server_set_camera: null camera");
+        return s->impl.set_camera(job, *c);
+    });
+}
+
 ATX_API atx_status atx_server_release(atx_server* s, uint32_t job)
 {
     return guarded([&]() -> atx_status { NEEDS(s); return s->impl.release(job); });

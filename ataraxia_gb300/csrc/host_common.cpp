@@ -45,7 +45,8 @@ atx_status DeviceBuffer::ensure(uint64_t bytes, Budget* budget, const char* what
         return fail(ATX_ERR_OUT_OF_MEMORY, "%s: %llu bytes exceed the HBM budget (%llu of %llu in use)", what,
                     (unsigned long long)bytes, (unsigned long long)budget->used(),
                     (unsigned long long)budget->cap());
-    cudaError_t e = cudaMalloc(&ptr_, bytes);
+    cudaError_t e = order_ ? cudaMallocFromPoolAsync(&ptr_, bytes, order_->pool, order_->alloc)
+                           : cudaMalloc(&ptr_, bytes);
     if (e != cudaSuccess) {
         ptr_ = nullptr;
         if (budget) budget->release(bytes);
@@ -59,7 +60,8 @@ atx_status DeviceBuffer::ensure(uint64_t bytes, Budget* budget, const char* what
 void DeviceBuffer::reset()
 {
     if (ptr_) {
-        cudaFree(ptr_);
+        if (order_) cudaFreeAsync(ptr_, order_->release);
+        else cudaFree(ptr_);
         if (budget_) budget_->release(bytes_);
     }
     ptr_ = nullptr;

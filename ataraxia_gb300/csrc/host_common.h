@@ -55,8 +55,20 @@ private:
     std::atomic<uint64_t> used_{0};
 };
 
-// Owning device allocation charged to a Budget.  Freed with cudaFree, which
-// synchronises the device: buffers are replaced only on resize / scene upload.
+// Where a buffer is allocated and freed in stream order: allocated from pool
+// on `alloc` (cudaMallocFromPoolAsync), freed on `release` (cudaFreeAsync)
+// after the work already queued there.  Neither call synchronises the device,
+// which lets a server admit and retire jobs while a pass is running.
+struct StreamOrder {
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t alloc = nullptr;
+    cudaStream_t release = nullptr;
+};
+
+// Owning device allocation charged to a Budget.  By default freed with
+// cudaFree, which synchronises the device (buffers are then replaced only on
+// resize / scene upload); with a StreamOrder, allocated and freed in stream
+// order.
 class DeviceBuffer {
 public:
     DeviceBuffer() = default;
@@ -68,7 +80,7 @@ public:
     {
         if (this != &o) {
             reset();
-            ptr_ = o.ptr_; bytes_ = o.bytes_; budget_ = o.budget_;
+            ptr_ = o.ptr_; bytes_ = o.bytes_; budget_ = o.budget_; order_ = o.order_;
             o.ptr_ = nullptr; o.bytes_ = 0; o.budget_ = nullptr;
         }
         return *this;
@@ -82,11 +94,18 @@ public:
     void* get() const { return ptr_; }
     template <class T> T* as() const { return static_cast<T*>(ptr_); }
     uint64_t bytes() const { return bytes_; }
+    // Allocate / free this buffer in stream order from now on (nullptr: cudaMalloc / cudaFree).
+    // Takes effect when the buffer holds no memory.
+    void use_stream_order(const StreamOrder* order)
+    {
+        if (!ptr_) order_ = order;
+    }
 
 private:
     void* ptr_ = nullptr;
     uint64_t bytes_ = 0;
     Budget* budget_ = nullptr;
+    const StreamOrder* order_ = nullptr;
 };
 
 // Camera.cpp:134-159: perspective (right-handed, clip z in [-1, 1]) and lookAt

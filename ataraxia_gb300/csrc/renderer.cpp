@@ -24,6 +24,7 @@ atx_status SceneStore::upload(const atx_sphere* s, uint32_t n, const atx_materia
 {
     if ((n && !s) || (nm && !m) || (nl && !l)) return fail(ATX_ERR_INVALID_ARG, "set_scene: null array");
     if (n > 0 && nm == 0) return fail(ATX_ERR_INVALID_ARG, "set_scene: spheres need at least one material");
+    for (DeviceBuffer* b : {&this->sph, &sph_mat, &sph_rad, &mat, &lights, &bvh}) b->use_stream_order(order);
 
     std::vector<float4> sph(n);
     std::vector<int32_t> smat(n);
@@ -209,13 +210,15 @@ atx_status EventTimer::collect(atx_kernel_times* t)
 atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore& ws, const LaunchShape& shape,
                           uint32_t frame0, uint32_t spp, int32_t max_bounces, int32_t sky, float4* accum,
                           uint32_t* image, uint32_t capacity, cudaStream_t stream, uint32_t* launches,
-                          KernelTimer* timer, uint64_t* primary_rays)
+                          KernelTimer* timer, uint64_t* primary_rays, uint64_t pix_begin, uint64_t pix_end)
 {
-    const uint64_t pixels = (uint64_t)cam.width * cam.height;
-    const WavePlan plan = plan_waves(pixels, spp, capacity);
+    const uint64_t all = (uint64_t)cam.width * cam.height;
+    const uint64_t pend = std::min(pix_end, all);
+    const uint64_t pbeg = std::min(pix_begin, pend);
+    const WavePlan plan = plan_waves(pend - pbeg, spp, capacity);
     const uint32_t last_frame = frame0 + spp - 1;
-    for (uint64_t p0 = 0; p0 < pixels; p0 += plan.pixels_per_wave) {
-        const uint32_t np = (uint32_t)std::min<uint64_t>(plan.pixels_per_wave, pixels - p0);
+    for (uint64_t p0 = pbeg; p0 < pend; p0 += plan.pixels_per_wave) {
+        const uint32_t np = (uint32_t)std::min<uint64_t>(plan.pixels_per_wave, pend - p0);
         for (uint32_t s0 = 0; s0 < spp; s0 += plan.spp_per_wave) {
             WaveJob job;
             job.pixel0 = (uint32_t)p0;
@@ -241,8 +244,13 @@ Renderer::~Renderer()
 {
     if (cudaSetDevice(cfg_.device) == cudaSuccess) {
         if (stream_) cudaStreamSynchronize(stream_);
+        if (stream2_) cudaStreamSynchronize(stream2_);
         scene_ = SceneStore();
-        wave_.buf.reset();
+        wave_[0].buf.reset();
+        wave_[1].buf.reset();
+        if (fork_) cudaEventDestroy(fork_);
+        if (join_) cudaEventDestroy(join_);
+        if (stream2_) cudaStreamDestroy(stream2_);
         accum_.reset();
         image_.reset();
         totals_.reset();
@@ -270,6 +278,9 @@ atx_status Renderer::init()
         return fail(ATX_ERR_INVALID_ARG, "device %d out of range (%d visible)", cfg_.device, count);
     ATX_TRY(activate());
     ATX_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    ATX_CUDA(cudaStreamCreateWithFlags(&stream2_, cudaStreamNonBlocking));
+    ATX_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+    ATX_CUDA(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
     ATX_CUDA(cudaEventCreate(&ev_start_));
     ATX_CUDA(cudaEventCreate(&ev_stop_));
     ATX_TRY(totals_.ensure(2 * sizeof(unsigned long long), &budget_, "ray totals"));
@@ -364,32 +375,53 @@ atx_status Renderer::render(uint32_t spp)
     ATX_TRY(activate());
     ATX_TRY(refresh_camera());
     ATX_TRY(ensure_shape());
-    // One wave per launch when it fits: fewer, fuller kernels (the state is
-    // allocated for this launch's paths, rounded up to 1 Mi, and kept).
+    // One wave per lane when it fits: fewer, fuller kernels (the state is
+    // allocated for this launch's paths, rounded up to 1 Mi, and kept).  Two
+    // lanes unless the caller fixed the wave size, kernels are being timed
+    // one by one, or the launch is too small to fill two.
+    const uint64_t px = (uint64_t)width_ * height_;
+    const bool profile = (cfg_.flags & ATX_FLAG_PROFILE_KERNELS) != 0;
+    const uint32_t lanes = (cfg_.wave_paths || profile || px < 2 || px * spp < (8ull << 20)) ? 1u : 2u;
+    const uint64_t half = (px + 1) / 2;
     uint32_t capacity = cfg_.wave_paths;
     if (!capacity) {
-        const uint64_t want = ((uint64_t)width_ * height_ * spp + (1u << 20) - 1) & ~uint64_t((1u << 20) - 1);
+        const uint64_t lane_paths = (lanes == 2 ? half : px) * spp;
+        const uint64_t want = (lane_paths + (1u << 20) - 1) & ~uint64_t((1u << 20) - 1);
         capacity = (uint32_t)std::min<uint64_t>(want, kDefaultWavePaths);
     }
     const int32_t bounces = settings_.max_bounces;
-    ATX_TRY(wave_.ensure(capacity, bounces > 0 ? (uint32_t)bounces : 0u, &budget_));
-    wave_.view.totals = totals_.as<unsigned long long>();
+    for (uint32_t l = 0; l < lanes; ++l) {
+        ATX_TRY(wave_[l].ensure(capacity, bounces > 0 ? (uint32_t)bounces : 0u, &budget_));
+        wave_[l].view.totals = totals_.as<unsigned long long>();
+    }
 
     if (!settings_.accumulation) frame_ = 1;
     const uint32_t f0 = frame_;
     uint32_t launches = 0;
-    KernelTimer* timer = (cfg_.flags & ATX_FLAG_PROFILE_KERNELS) ? &timer_ : nullptr;
+    KernelTimer* timer = profile ? &timer_ : nullptr;
     ATX_CUDA(cudaEventRecord(ev_start_, stream_));
     if (f0 == 1) {  // Renderer.cu:181-182
         if (timer) timer->begin(kFamOther, stream_);
-        ATX_CUDA(enqueue_clear_accum(accum_.as<float4>(), (uint64_t)width_ * height_, stream_));
+        ATX_CUDA(enqueue_clear_accum(accum_.as<float4>(), px, stream_));
         if (timer) timer->end(kFamOther, stream_);
         ++launches;
     }
     uint64_t primary_rays = 0;
-    ATX_TRY(enqueue_frames(scene_.view, camv_, wave_, shape_, f0, spp, bounces, settings_.sky_light ? 1 : 0,
-                           accum_.as<float4>(), image_.as<uint32_t>(), capacity, stream_, &launches, timer,
-                           &primary_rays));
+    const int32_t sky = settings_.sky_light ? 1 : 0;
+    if (lanes == 1) {
+        ATX_TRY(enqueue_frames(scene_.view, camv_, wave_[0], shape_, f0, spp, bounces, sky, accum_.as<float4>(),
+                               image_.as<uint32_t>(), capacity, stream_, &launches, timer, &primary_rays));
+    } else {
+        ATX_CUDA(cudaEventRecord(fork_, stream_));
+        ATX_CUDA(cudaStreamWaitEvent(stream2_, fork_, 0));
+        ATX_TRY(enqueue_frames(scene_.view, camv_, wave_[0], shape_, f0, spp, bounces, sky, accum_.as<float4>(),
+                               image_.as<uint32_t>(), capacity, stream_, &launches, nullptr, &primary_rays, 0, half));
+        ATX_TRY(enqueue_frames(scene_.view, camv_, wave_[1], shape_, f0, spp, bounces, sky, accum_.as<float4>(),
+                               image_.as<uint32_t>(), capacity, stream2_, &launches, nullptr, &primary_rays, half,
+                               px));
+        ATX_CUDA(cudaEventRecord(join_, stream2_));
+        ATX_CUDA(cudaStreamWaitEvent(stream_, join_, 0));
+    }
     ATX_CUDA(cudaEventRecord(ev_stop_, stream_));
     timed_ = true;
     frame_ = settings_.accumulation ? f0 + spp : 1u;  // Renderer.cu:245-248

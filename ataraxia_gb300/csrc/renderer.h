@@ -18,6 +18,7 @@ struct SceneStore {
     SceneView view{};
     uint32_t bvh_threshold = 0;
     uint32_t bvh_leaf = 0;
+    const StreamOrder* order = nullptr;   // stream-ordered allocation (batches); nullptr: cudaMalloc
 
     // Validates, converts and uploads on stream (Renderer.cu:25-57).
     atx_status upload(const atx_sphere* s, uint32_t n, const atx_material* m, uint32_t nm, const atx_light* l,
@@ -46,11 +47,13 @@ struct WavePlan {
 };
 WavePlan plan_waves(uint64_t pixels, uint32_t spp, uint32_t capacity);
 
-// Enqueues frames [frame0, frame0 + spp) for all pixels of the view.
+// Enqueues frames [frame0, frame0 + spp) for pixels [pix_begin, pix_end) of
+// the view (default: all of them).
 atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore& ws, const LaunchShape& shape,
                           uint32_t frame0, uint32_t spp, int32_t max_bounces, int32_t sky, float4* accum,
                           uint32_t* image, uint32_t capacity, cudaStream_t stream, uint32_t* launches,
-                          KernelTimer* timer = nullptr, uint64_t* primary_rays = nullptr);
+                          KernelTimer* timer = nullptr, uint64_t* primary_rays = nullptr, uint64_t pix_begin = 0,
+                          uint64_t pix_end = ~uint64_t(0));
 
 // Records a pair of CUDA events around each kernel and sums their durations
 // per kernel family when collected.
@@ -121,7 +124,12 @@ private:
     bool cam_dirty_ = true;
 
     SceneStore scene_;
-    WaveStore wave_;
+    // Two lanes: a launch's pixels are split in halves rendered on two
+    // streams with their own path state, so one half's last, sparse bounces
+    // overlap the other half's work instead of leaving SMs idle.
+    WaveStore wave_[2];
+    cudaStream_t stream2_ = nullptr;
+    cudaEvent_t fork_ = nullptr, join_ = nullptr;
     DeviceBuffer accum_, image_, totals_;
     LaunchShape shape_{};
     bool shape_valid_ = false;

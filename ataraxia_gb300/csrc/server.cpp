@@ -1,14 +1,18 @@
-// Render server: a worker thread admits jobs in arrival order when a slot and
-// their device memory fit, runs batched passes over all active jobs (each
-// renders a slice of its remaining frames), and retires jobs that reach their
-// target: image and accumulator are copied to the host and the job's device
-// memory is released.  Submitters never touch the GPU.
+// Render server: a worker thread admits jobs when a slot and their device
+// memory fit, queues batched passes over all active jobs (each renders a
+// slice of its remaining frames) and retires jobs that reach their target
+// (image and accumulator copied to host buffers, device memory released).
+// Passes are pipelined: while pass k runs on the GPU the worker admits jobs,
+// uploads their scenes and queues pass k+1 with the read-backs of the jobs it
+// completes, then waits for pass k.  Submitters never touch the GPU.
 #include "server.h"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 
 #include "lbvh.h"
 
@@ -17,42 +21,135 @@ namespace atx {
 namespace {
 constexpr uint32_t kDefaultActive = 64;
 constexpr uint32_t kDefaultPassSpp = 16;
-constexpr uint64_t kDefaultPassPaths = 1ull << 28;
+constexpr uint64_t kDefaultPassPaths = 1ull << 30;
 constexpr uint32_t kDefaultBvhThreshold = 1024;
+constexpr size_t kPassesInFlight = 2;                 // the one running and the next
+constexpr uint64_t kPinnedCacheBytes = 4ull << 30;    // result buffers kept for reuse
 
 uint64_t up256(uint64_t x) { return (x + 255u) & ~uint64_t(255u); }
 
 bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
 
-// The batched renderer.
+// The batched renderer.  Each commit records a pair of events around the pass
+// and its read-backs; result buffers are page-locked, cached by size.
 class BatchExecutor : public Executor {
 public:
-    explicit BatchExecutor(const atx_config& cfg) : b_(cfg) {}
+    explicit BatchExecutor(const atx_config& cfg) : b_(cfg), device_(cfg.device) {}
+    ~BatchExecutor() override
+    {
+        if (cudaSetDevice(device_) != cudaSuccess) return;
+        cudaStreamSynchronize(b_.stream());
+        for (auto& kv : marks_) {
+            cudaEventDestroy(kv.second.first);
+            cudaEventDestroy(kv.second.second);
+        }
+        for (cudaEvent_t e : free_events_) cudaEventDestroy(e);
+        for (auto& kv : pinned_)
+            for (void* p : kv.second) cudaFreeHost(p);
+    }
     atx_status init() override { return b_.init(); }
     atx_status add(const atx_batch_scene& d, uint64_t, uint32_t* slot) override { return b_.add_scene(d, slot); }
     atx_status remove(uint32_t slot) override { return b_.remove_scene(slot); }
     atx_status set_spp(uint32_t slot, uint32_t spp) override { return b_.set_spp(slot, spp); }
-    atx_status run_pass() override
+    atx_status set_camera(uint32_t slot, const atx_camera& c) override { return b_.set_camera(slot, c); }
+    atx_status enqueue_pass() override
     {
-        ATX_TRY(b_.run());
-        return b_.synchronize();
+        ATX_CUDA(cudaSetDevice(device_));
+        if (!start_) ATX_TRY(take(&start_));
+        ATX_CUDA(cudaEventRecord(start_, b_.stream()));
+        return b_.run();
     }
-    atx_status read_image(uint32_t slot, uint32_t* host, uint64_t n) override { return b_.read_image(slot, host, n); }
-    atx_status read_accumulation(uint32_t slot, float* host, uint64_t n) override
+    atx_status enqueue_read(uint32_t slot, uint32_t* image, float* accum, uint64_t n) override
     {
-        return b_.read_accumulation(slot, host, n);
+        return b_.read_async(slot, image, accum, n);
+    }
+    atx_status commit(uint64_t* ticket) override
+    {
+        ATX_CUDA(cudaSetDevice(device_));
+        if (!start_) return fail(ATX_ERR_INVALID_ARG, "server: commit without a pass");
+        cudaEvent_t end = nullptr;
+        ATX_TRY(take(&end));
+        ATX_CUDA(cudaEventRecord(end, b_.stream()));
+        marks_[next_] = {start_, end};
+        start_ = nullptr;
+        *ticket = next_++;
+        return ATX_OK;
+    }
+    atx_status wait(uint64_t ticket, double* device_ms) override
+    {
+        ATX_CUDA(cudaSetDevice(device_));
+        auto it = marks_.find(ticket);
+        if (it == marks_.end()) return fail(ATX_ERR_NOT_FOUND, "server: no pass %llu", (unsigned long long)ticket);
+        const auto ev = it->second;
+        marks_.erase(it);
+        free_events_.push_back(ev.first);
+        free_events_.push_back(ev.second);
+        ATX_CUDA(cudaEventSynchronize(ev.second));
+        float ms = 0.0f;
+        ATX_CUDA(cudaEventElapsedTime(&ms, ev.first, ev.second));
+        *device_ms = ms;
+        return ATX_OK;
     }
     uint64_t device_bytes() const override { return b_.scene_bytes(); }
+    void* host_alloc(uint64_t bytes) override
+    {
+        auto& list = pinned_[bytes];
+        if (!list.empty()) {
+            void* p = list.back();
+            list.pop_back();
+            cached_ -= bytes;
+            return p;
+        }
+        if (cudaSetDevice(device_) != cudaSuccess) return nullptr;
+        void* p = nullptr;
+        if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return nullptr;
+        }
+        return p;
+    }
+    void host_free(void* p, uint64_t bytes) override
+    {
+        if (!p) return;
+        if (cached_ + bytes <= kPinnedCacheBytes) {
+            pinned_[bytes].push_back(p);
+            cached_ += bytes;
+        } else {
+            cudaFreeHost(p);
+        }
+    }
 
 private:
+    atx_status take(cudaEvent_t* e)
+    {
+        if (!free_events_.empty()) {
+            *e = free_events_.back();
+            free_events_.pop_back();
+            return ATX_OK;
+        }
+        ATX_CUDA(cudaEventCreate(e));
+        return ATX_OK;
+    }
+
     Batch b_;
+    int device_;
+    cudaEvent_t start_ = nullptr;
+    uint64_t next_ = 1;
+    std::map<uint64_t, std::pair<cudaEvent_t, cudaEvent_t>> marks_;
+    std::vector<cudaEvent_t> free_events_;
+    std::map<uint64_t, std::vector<void*>> pinned_;
+    uint64_t cached_ = 0;
 };
 
-// Host-only stand-in for the device: accounts memory by the admission
-// estimate, takes 1 ns of wall time per path of a pass, and fills images with
-// the number of frames rendered.  fail_pass > 0 makes that pass report an
-// error, so failure handling can be tested without a GPU.
+// Host-only stand-in for the device, for scheduling tests without a GPU: a
+// pass takes 1 ns of simulated device time per path on a timeline that runs
+// behind the host like a stream; memory is accounted by the admission
+// estimate; read-backs fill images with the frame count reached.  fail_pass
+// > 0 makes that pass report an error, so failure handling is tested on the
+// host.
 class HostExecutor : public Executor {
+    using Clock = std::chrono::steady_clock;
+
 public:
     explicit HostExecutor(uint32_t fail_pass) : fail_pass_(fail_pass) {}
     atx_status init() override { return ATX_OK; }
@@ -79,7 +176,13 @@ public:
         slots_[slot].spp = spp;
         return ATX_OK;
     }
-    atx_status run_pass() override
+    atx_status set_camera(uint32_t slot, const atx_camera&) override
+    {
+        if (slot >= slots_.size() || !slots_[slot].used) return fail(ATX_ERR_NOT_FOUND, "host executor: slot %u", slot);
+        slots_[slot].frames = 0;
+        return ATX_OK;
+    }
+    atx_status enqueue_pass() override
     {
         if (fail_pass_ && ++passes_ == fail_pass_) return fail(ATX_ERR_CUDA, "host executor: injected device error");
         uint64_t paths = 0;
@@ -88,29 +191,58 @@ public:
                 paths += (uint64_t)s.w * s.h * s.spp;
                 s.frames += s.spp;
             }
-        std::this_thread::sleep_for(std::chrono::nanoseconds(paths));
+        const Clock::time_point start = std::max(Clock::now(), busy_until_);
+        busy_until_ = start + std::chrono::nanoseconds(paths);
+        pass_ms_ += (double)paths * 1e-6;
         return ATX_OK;
     }
-    atx_status read_image(uint32_t slot, uint32_t* host, uint64_t n) override
+    atx_status enqueue_read(uint32_t slot, uint32_t* image, float* accum, uint64_t n) override
     {
-        std::fill(host, host + n, slots_[slot].frames);
+        if (slot >= slots_.size() || !slots_[slot].used) return fail(ATX_ERR_NOT_FOUND, "host executor: slot %u", slot);
+        reads_.push_back(Read{image, accum, n, slots_[slot].frames});
         return ATX_OK;
     }
-    atx_status read_accumulation(uint32_t slot, float* host, uint64_t n) override
+    atx_status commit(uint64_t* ticket) override
     {
-        for (uint64_t i = 0; i < n; ++i) {
-            host[4 * i] = host[4 * i + 1] = host[4 * i + 2] = 0.0f;
-            host[4 * i + 3] = (float)slots_[slot].frames;
+        marks_[next_] = Mark{busy_until_, pass_ms_, std::move(reads_)};
+        reads_.clear();
+        pass_ms_ = 0.0;
+        *ticket = next_++;
+        return ATX_OK;
+    }
+    atx_status wait(uint64_t ticket, double* device_ms) override
+    {
+        auto it = marks_.find(ticket);
+        if (it == marks_.end()) return fail(ATX_ERR_NOT_FOUND, "server: no pass %llu", (unsigned long long)ticket);
+        std::this_thread::sleep_until(it->second.ready);
+        for (const Read& r : it->second.reads) {
+            if (r.image) std::fill(r.image, r.image + r.n, r.frames);
+            if (r.accum)
+                for (uint64_t i = 0; i < r.n; ++i) {
+                    r.accum[4 * i] = r.accum[4 * i + 1] = r.accum[4 * i + 2] = 0.0f;
+                    r.accum[4 * i + 3] = (float)r.frames;
+                }
         }
+        *device_ms = it->second.ms;
+        marks_.erase(it);
         return ATX_OK;
     }
     uint64_t device_bytes() const override { return bytes_; }
+    void* host_alloc(uint64_t bytes) override { return std::malloc(bytes); }
+    void host_free(void* p, uint64_t) override { std::free(p); }
 
 private:
     struct Slot { bool used; uint32_t w, h, spp, frames; uint64_t bytes; };
+    struct Read { uint32_t* image; float* accum; uint64_t n; uint32_t frames; };
+    struct Mark { Clock::time_point ready; double ms; std::vector<Read> reads; };
     std::vector<Slot> slots_;
+    std::vector<Read> reads_;
+    std::map<uint64_t, Mark> marks_;
+    uint64_t next_ = 1;
     uint64_t bytes_ = 0;
     uint32_t fail_pass_ = 0, passes_ = 0;
+    Clock::time_point busy_until_{};
+    double pass_ms_ = 0.0;
 };
 }  // namespace
 
@@ -134,6 +266,7 @@ Server::~Server()
     }
     cv_work_.notify_all();
     if (worker_.joinable()) worker_.join();
+    for (auto& kv : jobs_) free_results(kv.second);
 }
 
 atx_status Server::init()
@@ -203,18 +336,28 @@ atx_status Server::submit(const atx_batch_scene& d, uint32_t target, uint32_t* i
     return ATX_OK;
 }
 
-// Moves queued jobs to the executor, in arrival order, while slots and memory allow.
+// Moves queued jobs to the executor while slots and memory allow: in arrival
+// order, or the job with the fewest pixel-samples first.
 void Server::admit_locked()
 {
     const uint64_t cap = cfg_.base.hbm_budget_bytes;
     while (!pending_.empty() && active_.size() < cfg_.max_active_jobs) {
-        const uint32_t jid = pending_.front();
+        auto pick = pending_.begin();
+        if (cfg_.policy == ATX_ADMIT_SMALLEST) {
+            auto work = [&](uint32_t id) {
+                const Job& j = jobs_[id];
+                return (uint64_t)j.desc.width * j.desc.height * j.target;
+            };
+            for (auto it = pending_.begin(); it != pending_.end(); ++it)
+                if (work(*it) < work(*pick)) pick = it;
+        }
+        const uint32_t jid = *pick;
         Job& j = jobs_[jid];
         if (cap && exec_->device_bytes() + j.bytes > cap) break;   // wait for a job to retire
         uint32_t slot = 0;
         const atx_status s = exec_->add(j.desc, j.bytes, &slot);
-        if (s == ATX_ERR_OUT_OF_MEMORY && !active_.empty()) break;
-        pending_.pop_front();
+        if (s == ATX_ERR_OUT_OF_MEMORY && (!active_.empty() || !flights_.empty())) break;
+        pending_.erase(pick);
         if (s != ATX_OK) {
             j.state = ATX_JOB_FAILED;
             j.t_done = now();
@@ -230,96 +373,190 @@ void Server::admit_locked()
     }
 }
 
-atx_status Server::run_pass()
+void Server::free_results(Job& j)
 {
-    // slices: up to pass_spp frames per job, scaled so a pass stays bounded
+    if (j.image) exec_->host_free(j.image, j.result_bytes);
+    j.image = nullptr;
+    j.accum = nullptr;
+    j.result_bytes = 0;
+}
+
+atx_status Server::queue_pass_locked(bool* queued)
+{
+    *queued = false;
+    // cancelled jobs leave now (their device memory after the queued passes);
+    // a new camera restarts a job's accumulation
+    std::vector<uint32_t> keep;
+    for (uint32_t jid : active_) {
+        Job& j = jobs_[jid];
+        if (j.cancel) {
+            ATX_TRY(exec_->remove(j.slot));
+            j.state = ATX_JOB_CANCELLED;
+            j.t_done = now();
+            ++st_.cancelled;
+            cv_done_.notify_all();
+            continue;
+        }
+        if (j.restart) {
+            ATX_TRY(exec_->set_camera(j.slot, j.desc.camera));
+            j.restart = false;
+            j.queued = 0;
+            j.done = 0;
+            ++j.epoch;
+        }
+        keep.push_back(jid);
+    }
+    active_.swap(keep);
+
+    // slices: up to pass_spp frames per job, scaled down so a pass stays bounded
     std::vector<std::pair<uint32_t, uint32_t>> plan;   // job, frames this pass
     uint64_t total = 0;
-    {
-        std::lock_guard<std::mutex> lock(mu_);
-        for (uint32_t jid : active_) {
-            const Job& j = jobs_[jid];
-            const uint32_t q = std::min(j.target - j.done, cfg_.pass_spp);
-            plan.emplace_back(jid, q);
-            total += (uint64_t)j.desc.width * j.desc.height * q;
-        }
-        if (total > cfg_.max_pass_paths) {
-            const double scale = (double)cfg_.max_pass_paths / (double)total;
-            total = 0;
-            for (auto& p : plan) {
-                const Job& j = jobs_[p.first];
-                p.second = std::max<uint32_t>(1, (uint32_t)std::floor(p.second * scale));
-                total += (uint64_t)j.desc.width * j.desc.height * p.second;
-            }
-        }
-        for (auto& p : plan) ATX_TRY(exec_->set_spp(jobs_[p.first].slot, p.second));
+    for (uint32_t jid : active_) {
+        const Job& j = jobs_[jid];
+        const uint32_t q = std::min(j.target - j.queued, cfg_.pass_spp);
+        plan.emplace_back(jid, q);
+        total += (uint64_t)j.desc.width * j.desc.height * q;
     }
-    const double t = now();
-    ATX_TRY(exec_->run_pass());
-    std::lock_guard<std::mutex> lock(mu_);
-    st_.busy_s += now() - t;
-    ++st_.passes;
-    st_.paths += total;
+    if (plan.empty()) return ATX_OK;
+    if (total > cfg_.max_pass_paths) {
+        const double scale = (double)cfg_.max_pass_paths / (double)total;
+        total = 0;
+        for (auto& p : plan) {
+            const Job& j = jobs_[p.first];
+            p.second = std::max<uint32_t>(1, (uint32_t)std::floor(p.second * scale));
+            total += (uint64_t)j.desc.width * j.desc.height * p.second;
+        }
+    }
+    for (auto& p : plan) ATX_TRY(exec_->set_spp(jobs_[p.first].slot, p.second));
+    ATX_TRY(exec_->enqueue_pass());
+
+    Flight f;
+    f.paths = total;
     std::vector<uint32_t> still;
     for (auto& p : plan) {
         Job& j = jobs_[p.first];
-        j.done += p.second;
-        const bool finished = j.done >= j.target;
-        if (finished || j.cancel) {
-            if (finished) {
-                const uint64_t px = (uint64_t)j.desc.width * j.desc.height;
-                j.image.resize(px);
-                j.accum.resize(4 * px);
-                ATX_TRY(exec_->read_image(j.slot, j.image.data(), px));
-                ATX_TRY(exec_->read_accumulation(j.slot, j.accum.data(), px));
-                j.state = ATX_JOB_DONE;
-                ++st_.completed;
-            } else {
-                j.state = ATX_JOB_CANCELLED;
-                ++st_.cancelled;
-            }
-            j.t_done = now();
-            ATX_TRY(exec_->remove(j.slot));
-            cv_done_.notify_all();
-        } else {
+        j.queued += p.second;
+        f.frames.push_back({p.first, p.second, j.epoch});
+        if (j.queued < j.target) {
             still.push_back(p.first);
+            continue;
         }
+        // final pass: read the results back after it
+        const uint64_t px = (uint64_t)j.desc.width * j.desc.height;
+        j.result_bytes = px * (sizeof(uint32_t) + 4 * sizeof(float));
+        void* buf = exec_->host_alloc(j.result_bytes);
+        if (!buf) return fail(ATX_ERR_OUT_OF_MEMORY, "server: no host memory for a %llu-pixel result",
+                              (unsigned long long)px);
+        j.image = static_cast<uint32_t*>(buf);
+        j.accum = reinterpret_cast<float*>(j.image + px);
+        ATX_TRY(exec_->enqueue_read(j.slot, j.image, j.accum, px));
+        ATX_TRY(exec_->set_spp(j.slot, 0));   // resident until the read-back is done, idle meanwhile
+        j.draining = true;
+        f.finishing.push_back(p.first);
     }
+    ATX_TRY(exec_->commit(&f.ticket));
     active_.swap(still);
+    flights_.push_back(std::move(f));
+    *queued = true;
     return ATX_OK;
+}
+
+// Waits for the oldest queued pass and settles its jobs.
+atx_status Server::finish_oldest()
+{
+    uint64_t ticket;
+    {
+        std::lock_guard<std::mutex> lock(mu_);
+        ticket = flights_.front().ticket;
+    }
+    double ms = 0.0;
+    const atx_status s = exec_->wait(ticket, &ms);   // without the lock: submitters keep going
+    std::lock_guard<std::mutex> lock(mu_);
+    if (s != ATX_OK) return s;
+    Flight f = std::move(flights_.front());
+    flights_.pop_front();
+    st_.busy_s += ms * 1e-3;
+    ++st_.passes;
+    st_.paths += f.paths;
+    for (const auto& e : f.frames) {
+        auto it = jobs_.find(e.job);
+        if (it != jobs_.end() && it->second.epoch == e.epoch) it->second.done += e.frames;
+    }
+    for (uint32_t jid : f.finishing) {
+        Job& j = jobs_[jid];
+        ATX_TRY(exec_->remove(j.slot));
+        j.draining = false;
+        j.state = ATX_JOB_DONE;
+        j.t_done = now();
+        ++st_.completed;
+    }
+    cv_done_.notify_all();
+    return ATX_OK;
+}
+
+void Server::fail_all_locked(atx_status s)
+{
+    worker_error_ = s;
+    std::snprintf(worker_msg_, sizeof(worker_msg_), "%s", last_error_message());
+    auto fail_job = [&](uint32_t jid) {
+        Job& j = jobs_[jid];
+        if (j.state != ATX_JOB_ACTIVE) return;
+        j.state = ATX_JOB_FAILED;
+        j.t_done = now();
+        j.draining = false;
+        exec_->remove(j.slot);
+        ++st_.failed;
+    };
+    for (uint32_t jid : active_) fail_job(jid);
+    for (const Flight& f : flights_)
+        for (const auto& e : f.frames) fail_job(e.job);
+    active_.clear();
+    flights_.clear();
+    cv_done_.notify_all();
 }
 
 void Server::loop()
 {
     for (;;) {
+        bool queued = false;
         {
             std::unique_lock<std::mutex> lock(mu_);
-            cv_work_.wait(lock, [&] { return stop_ || !pending_.empty() || !active_.empty(); });
+            cv_work_.wait(lock, [&] { return stop_ || !pending_.empty() || !active_.empty() || !flights_.empty(); });
             if (stop_) break;
             admit_locked();
-            if (active_.empty()) {
+            if (flights_.size() < kPassesInFlight) {
+                const atx_status s = queue_pass_locked(&queued);
+                if (s != ATX_OK) {
+                    fail_all_locked(s);
+                    continue;
+                }
+            }
+            if (!queued && flights_.empty()) {
                 // nothing fits yet and nothing runs: wait for a submission or cancel
                 if (!pending_.empty()) cv_work_.wait_for(lock, std::chrono::milliseconds(5));
                 continue;
             }
+            if (queued && flights_.size() < kPassesInFlight) continue;   // queue the next one first
         }
-        const atx_status s = run_pass();
+        const atx_status s = finish_oldest();
         if (s != ATX_OK) {
             std::lock_guard<std::mutex> lock(mu_);
-            worker_error_ = s;
-            std::snprintf(worker_msg_, sizeof(worker_msg_), "%s", last_error_message());
-            for (uint32_t jid : active_) {
-                Job& j = jobs_[jid];
-                j.state = ATX_JOB_FAILED;
-                j.t_done = now();
-                exec_->remove(j.slot);
-                ++st_.failed;
-            }
-            active_.clear();
-            cv_done_.notify_all();
+            fail_all_locked(s);
         }
     }
+    // let queued passes finish (their read-backs write into job buffers), then
     // cancel whatever is left
+    while (true) {
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            if (flights_.empty()) break;
+        }
+        if (finish_oldest() != ATX_OK) {
+            std::lock_guard<std::mutex> lock(mu_);
+            flights_.clear();
+            break;
+        }
+    }
     std::lock_guard<std::mutex> lock(mu_);
     for (uint32_t jid : pending_) jobs_[jid].state = ATX_JOB_CANCELLED;
     for (uint32_t jid : active_) jobs_[jid].state = ATX_JOB_CANCELLED;
@@ -369,9 +606,11 @@ atx_status Server::read_image(uint32_t id, uint32_t* host, uint64_t n)
     std::lock_guard<std::mutex> lock(mu_);
     auto it = jobs_.find(id);
     if (it == jobs_.end()) return fail(ATX_ERR_NOT_FOUND, "server: no job %u", id);
-    if (it->second.state != ATX_JOB_DONE) return fail(ATX_ERR_BUSY, "server: job %u not done", id);
-    if (!host || n > it->second.image.size()) return fail(ATX_ERR_INVALID_ARG, "server_read_image: bad buffer");
-    std::memcpy(host, it->second.image.data(), n * sizeof(uint32_t));
+    const Job& j = it->second;
+    if (j.state != ATX_JOB_DONE) return fail(ATX_ERR_BUSY, "server: job %u not done", id);
+    if (!host || n > (uint64_t)j.desc.width * j.desc.height)
+        return fail(ATX_ERR_INVALID_ARG, "server_read_image: bad buffer");
+    std::memcpy(host, j.image, n * sizeof(uint32_t));
     return ATX_OK;
 }
 
@@ -380,10 +619,11 @@ atx_status Server::read_accumulation(uint32_t id, float* host, uint64_t n)
     std::lock_guard<std::mutex> lock(mu_);
     auto it = jobs_.find(id);
     if (it == jobs_.end()) return fail(ATX_ERR_NOT_FOUND, "server: no job %u", id);
-    if (it->second.state != ATX_JOB_DONE) return fail(ATX_ERR_BUSY, "server: job %u not done", id);
-    if (!host || 4 * n > it->second.accum.size())
+    const Job& j = it->second;
+    if (j.state != ATX_JOB_DONE) return fail(ATX_ERR_BUSY, "server: job %u not done", id);
+    if (!host || n > (uint64_t)j.desc.width * j.desc.height)
         return fail(ATX_ERR_INVALID_ARG, "server_read_accumulation: bad buffer");
-    std::memcpy(host, it->second.accum.data(), 4 * n * sizeof(float));
+    std::memcpy(host, j.accum, 4 * n * sizeof(float));
     return ATX_OK;
 }
 
@@ -400,9 +640,30 @@ atx_status Server::cancel(uint32_t id)
         ++st_.cancelled;
         cv_done_.notify_all();
         cv_work_.notify_all();
-    } else if (j.state == ATX_JOB_ACTIVE) {
-        j.cancel = true;   // retired by the worker after the current pass
+    } else if (j.state == ATX_JOB_ACTIVE && !j.draining) {
+        j.cancel = true;   // retired by the worker before its next pass
+        cv_work_.notify_all();
     }
+    return ATX_OK;
+}
+
+atx_status Server::set_camera(uint32_t id, const atx_camera& c)
+{
+    if (!finite3(c.position) || !finite3(c.direction))
+        return fail(ATX_ERR_INVALID_ARG, "server_set_camera: camera is not finite");
+    std::lock_guard<std::mutex> lock(mu_);
+    auto it = jobs_.find(id);
+    if (it == jobs_.end()) return fail(ATX_ERR_NOT_FOUND, "server: no job %u", id);
+    Job& j = it->second;
+    if (j.state == ATX_JOB_QUEUED) {
+        j.desc.camera = c;
+        return ATX_OK;
+    }
+    if (j.state != ATX_JOB_ACTIVE || j.draining)
+        return fail(ATX_ERR_BUSY, "server_set_camera: job %u is finishing or finished", id);
+    j.desc.camera = c;
+    j.restart = true;
+    cv_work_.notify_all();
     return ATX_OK;
 }
 
@@ -412,6 +673,7 @@ atx_status Server::release(uint32_t id)
     auto it = jobs_.find(id);
     if (it == jobs_.end()) return fail(ATX_ERR_NOT_FOUND, "server: no job %u", id);
     if (it->second.state < ATX_JOB_DONE) return fail(ATX_ERR_BUSY, "server: job %u still running", id);
+    free_results(it->second);
     jobs_.erase(it);
     return ATX_OK;
 }
@@ -421,7 +683,9 @@ atx_status Server::stats(atx_server_stats* out)
     std::lock_guard<std::mutex> lock(mu_);
     *out = st_;
     out->device_bytes = exec_->device_bytes();
-    out->active = (uint32_t)active_.size();
+    size_t draining = 0;   // resident until their final pass and read-back finish
+    for (const Flight& f : flights_) draining += f.finishing.size();
+    out->active = (uint32_t)(active_.size() + draining);
     out->queued = (uint32_t)pending_.size();
     return ATX_OK;
 }

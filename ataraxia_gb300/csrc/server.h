@@ -1,6 +1,6 @@
 // Render server: continuous batching of progressive render jobs over the
-// batched renderer (batch_host.h), or over a host-only simulated
-// executor for scheduling tests on machines without a GPU.
+// batched renderer (batch_host.h), or over a host-only simulated executor for
+// scheduling tests on machines without a GPU.
 #pragma once
 
 #include <chrono>
@@ -18,18 +18,30 @@
 
 namespace atx {
 
-// What the server needs from the device: resident scenes and batched passes.
+// What the server needs from the device: resident scenes and batched passes,
+// queued asynchronously.  A pass, the read-backs queued after it and the
+// completion marker of commit() run in order; wait(ticket) returns when
+// everything up to that marker has finished.
 class Executor {
 public:
     virtual ~Executor() = default;
     virtual atx_status init() = 0;
+    // Makes a scene resident; its uploads do not wait for queued passes.
     virtual atx_status add(const atx_batch_scene& d, uint64_t bytes, uint32_t* slot) = 0;
+    // Frees a slot after the work already queued (passes, read-backs).
     virtual atx_status remove(uint32_t slot) = 0;
     virtual atx_status set_spp(uint32_t slot, uint32_t spp) = 0;
-    virtual atx_status run_pass() = 0;   // returns when the pass has finished
-    virtual atx_status read_image(uint32_t slot, uint32_t* host, uint64_t n) = 0;
-    virtual atx_status read_accumulation(uint32_t slot, float* host, uint64_t n) = 0;
+    virtual atx_status set_camera(uint32_t slot, const atx_camera& c) = 0;
+    virtual atx_status enqueue_pass() = 0;
+    virtual atx_status enqueue_read(uint32_t slot, uint32_t* image, float* accum, uint64_t n) = 0;
+    virtual atx_status commit(uint64_t* ticket) = 0;
+    // Blocks until the ticket's marker is reached; device time since the
+    // previous commit (the pass and its read-backs).
+    virtual atx_status wait(uint64_t ticket, double* device_ms) = 0;
     virtual uint64_t device_bytes() const = 0;
+    // Host buffers for results (page-locked where that makes copies async).
+    virtual void* host_alloc(uint64_t bytes) = 0;
+    virtual void host_free(void* p, uint64_t bytes) = 0;
 };
 
 std::unique_ptr<Executor> make_batch_executor(const atx_config& cfg);
@@ -47,6 +59,7 @@ public:
     atx_status read_image(uint32_t id, uint32_t* host, uint64_t n);
     atx_status read_accumulation(uint32_t id, float* host, uint64_t n);
     atx_status cancel(uint32_t id);
+    atx_status set_camera(uint32_t id, const atx_camera& c);
     atx_status release(uint32_t id);
     atx_status stats(atx_server_stats* out);
     double now() const;
@@ -62,17 +75,38 @@ private:
         std::vector<atx_light> lights;
         atx_batch_scene desc{};
         uint32_t target = 0;
-        uint32_t done = 0;
-        uint32_t slot = 0;          // executor scene id while active
+        uint32_t queued = 0;        // frames in passes queued so far
+        uint32_t done = 0;          // frames finished on the device
+        uint32_t slot = 0;          // executor scene id while resident
         uint64_t bytes = 0;
         double t_submit = 0, t_admit = 0, t_done = 0;
-        std::vector<uint32_t> image;
-        std::vector<float> accum;
+        uint32_t* image = nullptr;  // results, host buffers from the executor
+        float* accum = nullptr;
+        uint64_t result_bytes = 0;
         bool cancel = false;
+        bool restart = false;       // camera changed: restart when its queued passes finish
+        bool draining = false;      // final pass queued, read-back pending
+        uint32_t epoch = 0;         // bumped by a camera change; older frames in flight do not count
+    };
+    // A queued pass: its marker, the frames it adds per job and the jobs whose
+    // final read-back follows it.
+    struct Flight {
+        uint64_t ticket = 0;
+        uint64_t paths = 0;
+        struct Part {
+            uint32_t job, frames, epoch;
+        };
+        std::vector<Part> frames;
+        std::vector<uint32_t> finishing;
     };
     void loop();
     void admit_locked();
-    atx_status run_pass();
+    // Plans and queues one pass over the active jobs (lock held); false if
+    // there was nothing to render.
+    atx_status queue_pass_locked(bool* queued);
+    atx_status finish_oldest();
+    void fail_all_locked(atx_status s);
+    void free_results(Job& j);
 
     atx_server_config cfg_;
     std::unique_ptr<Executor> exec_;
@@ -85,6 +119,7 @@ private:
     std::unordered_map<uint32_t, Job> jobs_;
     std::deque<uint32_t> pending_;
     std::vector<uint32_t> active_;
+    std::deque<Flight> flights_;
     atx_server_stats st_{};
     atx_status worker_error_ = ATX_OK;
     char worker_msg_[256] = "";

@@ -93,8 +93,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_extend(SceneView sc, CameraView
     if (SMEM) stage_spheres(sc, s_sph);
     const float4* sph = SMEM ? s_sph : sc.sph;
 
-    const uint32_t* qin = ws.q[bounce & 1];
-    uint32_t* qout = ws.q[(bounce + 1) & 1];
+    // select, not index: a runtime index into the parameter's array would
+    // copy the whole WaveState to local memory
+    const uint32_t* qin = (bounce & 1) ? ws.q[1] : ws.q[0];
+    uint32_t* qout = (bounce & 1) ? ws.q[0] : ws.q[1];
     const bool last = bounce + 1 >= job.max_bounces;
     const uint32_t stride = gridDim.x * blockDim.x;
 
@@ -218,6 +220,18 @@ __global__ void __launch_bounds__(kThreads, 4) k_extend(SceneView sc, CameraView
     }
 }
 
+// Adds the light a shadow ray carries to its path (Renderer.cu:356-368).
+__device__ __forceinline__ void shadow_light(const WaveState& ws, uint32_t idx, float4 sd)
+{
+    const float4 c = ws.sh_c[idx];
+    const uint32_t pid = __float_as_uint(sd.w);
+    float4 col = ws.col[pid];
+    col.x = col.x + c.x;
+    col.y = col.y + c.y;
+    col.z = col.z + c.z;
+    ws.col[pid] = col;
+}
+
 template <int IS>
 __global__ void __launch_bounds__(kThreads) k_shadow(SceneView sc, WaveState ws, int bounce)
 {
@@ -228,18 +242,79 @@ __global__ void __launch_bounds__(kThreads) k_shadow(SceneView sc, WaveState ws,
     if (SMEM) stage_spheres(sc, s_sph);
     const float4* sph = SMEM ? s_sph : sc.sph;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += stride) {
-        const float4 so = ws.sh_o[idx];
-        const float4 sd = ws.sh_d[idx];
-        if (!scene_occluded<IS>(sc, sph, mk3(so.x, so.y, so.z), mk3(sd.x, sd.y, sd.z), so.w)) {
-            const float4 c = ws.sh_c[idx];
-            const uint32_t pid = __float_as_uint(sd.w);
-            float4 col = ws.col[pid];
-            col.x = col.x + c.x;
-            col.y = col.y + c.y;
-            col.z = col.z + c.z;
-            ws.col[pid] = col;
+    const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+
+    if (IS == kIsBvh || sc.n_sph == 0u) {
+        for (uint32_t idx = first; idx < n; idx += stride) {
+            const float4 so = ws.sh_o[idx];
+            const float4 sd = ws.sh_d[idx];
+            if (!scene_occluded<IS>(sc, sph, mk3(so.x, so.y, so.z), mk3(sd.x, sd.y, sd.z), so.w))
+                shadow_light(ws, idx, sd);
         }
+        return;
+    }
+
+    // Brute force, any hit.  Rays stop at their first occluder, so lanes of a
+    // warp finish at different times; instead of idling until the slowest lane
+    // is done, a lane that finishes loads its next ray at once and tests it
+    // from the warp's current 32-sphere chunk on, wrapping around.  Every
+    // iteration the whole warp tests the same chunk (one broadcast read per
+    // sphere) and each lane counts the chunks its ray has left.  An any-hit
+    // query does not depend on the order in which spheres are tested.
+    // Each lane also holds its next ray, loaded when the current one starts,
+    // so a lane that moves on does not stall the warp on a memory load.
+    const uint32_t nchunks = (sc.n_sph + 31u) / 32u;
+    const uint32_t tail = sc.n_sph - (nchunks - 1u) * 32u;   // spheres in the last chunk
+    uint32_t idx = 0u, left = 0u, chunk = 0u;
+    float3 o = mk3(0.f, 0.f, 0.f), d = o;
+    float a = 0.0f, dist2 = 0.0f;
+    float4 sd = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool live = false;   // lane holds a ray
+    uint32_t nidx = first;
+    float4 nso = sd, nsd = sd;
+    if (nidx < n) {
+        nso = ws.sh_o[nidx];
+        nsd = ws.sh_d[nidx];
+    }
+    for (;;) {   // ends: every iteration retires a ray or takes a chunk off one
+        if (!live && nidx < n) {
+            idx = nidx;
+            sd = nsd;
+            o = mk3(nso.x, nso.y, nso.z);
+            d = mk3(nsd.x, nsd.y, nsd.z);
+            a = dot3(d, d);
+            dist2 = nso.w;
+            left = nchunks;
+            live = true;
+            nidx += stride;
+            if (nidx < n) {
+                nso = ws.sh_o[nidx];
+                nsd = ws.sh_d[nidx];
+            }
+        }
+        if (!__any_sync(kFull, live)) break;
+        if (live) {
+            const uint32_t base = chunk * 32u;
+            uint32_t mask = (chunk + 1u < nchunks || tail == 32u)
+                                ? candidate_bits<SMEM, 32>(sph, base, o, d, a, 32u)
+                                : candidate_bits<SMEM, 31>(sph, base, o, d, a, tail);
+            bool hit = false;
+            while (mask) {
+                const uint32_t k = (uint32_t)__clz(mask);
+                mask &= ~(0x80000000u >> k);
+                float t;
+                if (sphere_t(SMEM ? sph[base + k] : __ldg(&sph[base + k]), o, d, a, t) && t > 0.0f &&
+                    t * t < dist2) {
+                    hit = true;
+                    break;
+                }
+            }
+            if (hit || --left == 0u) {
+                if (!hit) shadow_light(ws, idx, sd);   // Renderer.cu:353-369: unoccluded
+                live = false;
+            }
+        }
+        chunk = (chunk + 1u == nchunks) ? 0u : chunk + 1u;
     }
 }
 

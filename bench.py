@@ -432,7 +432,7 @@ def _pct(v, q):
     return round(float(np.percentile(np.asarray(v), q)), 4) if v else None
 
 
-def serve_batched(jobs, duration, args):
+def serve_batched(jobs, duration, args, policy="arrival"):
     """Poisson arrivals into the continuous-batching server for `duration` seconds.  A driver thread
     submits each job at its arrival time (BUSY = rejected once max_pending jobs wait); the main thread
     collects finished jobs and releases them.  Latency = done time - intended arrival time."""
@@ -441,8 +441,8 @@ def serve_batched(jobs, duration, args):
     import ataraxia_gb300 as atx
 
     s = atx.Server(hbm_budget_bytes=int(args.hbm_budget_gb * 1e9), max_active_jobs=args.max_active,
-                   pass_spp=args.pass_spp, max_pending=args.max_pending,
-                   host_executor=getattr(args, "host_executor", False))
+                   pass_spp=args.pass_spp, max_pending=args.max_pending, max_pass_paths=args.max_pass_paths,
+                   host_executor=getattr(args, "host_executor", False), policy=policy)
     lock = threading.Lock()
     outstanding = {}   # job id -> (intended arrival on the server clock, paths)
     rejected = [0]
@@ -560,7 +560,9 @@ def run_serve(args, dist: Dist):
            "pool_scenes": len(pool), "rates": {}}
     for rate in [float(x) for x in args.rates.split(",")]:
         jobs = scenes.config4(seed=4, rate=rate, duration_s=args.serve_seconds, pool=pool)
-        res = {"batched": serve_batched(jobs, args.serve_seconds, args)}
+        res = {}
+        for pol in ("arrival", "smallest") if args.policy == "both" else (args.policy,):
+            res["batched_" + pol] = serve_batched(jobs, args.serve_seconds, args, pol)
         if not args.no_fifo:
             res["fifo"] = serve_fifo(jobs, args.serve_seconds, args.max_pending)
         out["rates"][str(rate)] = res
@@ -652,6 +654,9 @@ def main(argv=None) -> int:
     ap.add_argument("--max-pending", type=int, default=4096, help="serve mode: queue bound (then BUSY)")
     ap.add_argument("--pool", type=int, default=512, help="serve mode: scenes in the job pool")
     ap.add_argument("--no-fifo", action="store_true", help="serve mode: skip the FIFO baseline")
+    ap.add_argument("--policy", default="both", choices=["arrival", "smallest", "both"],
+                    help="serve mode: admission order of the batching server")
+    ap.add_argument("--max-pass-paths", type=int, default=0, help="serve mode: bound on paths per pass (0 = default)")
     ap.add_argument("--lanes", type=int, default=0, help="batch mode: concurrent lanes (0 = library default)")
     ap.add_argument("--lane-wave", type=int, default=0, help="batch mode: path state per lane, Mi paths")
     ap.add_argument("--width", type=int, default=0, help="render mode: override the viewport width")

@@ -290,11 +290,13 @@ ATX_API atx_status atx_batch_get_tuning(atx_batch* b, atx_batch_tuning* tuning);
 
 /* A render server: jobs (a scene and a target sample count) are submitted
  * from any thread and rendered progressively by a worker thread that runs
- * batched passes (continuous batching).  A job is admitted, in arrival order,
- * when an active slot is free and its device memory (scene tables, LBVH,
- * accumulator, image) fits the HBM budget; its scene, frame index and
- * accumulator stay resident until it reaches its target, when its image and
- * accumulator are copied to host memory and its device memory is released.
+ * batched passes (continuous batching).  A job is admitted (in arrival order,
+ * or smallest first) when an active slot is free and its device memory (scene
+ * tables, LBVH, accumulator, image) fits the HBM budget; its scene, frame
+ * index and accumulator stay resident until it reaches its target, when its
+ * image and accumulator are copied to host memory and its device memory is
+ * released.  The worker queues the next pass, its uploads and read-backs
+ * while the current one runs, so the GPU does not wait for the host.
  * No counterpart in the reference (an interactive single-scene viewer). */
 typedef struct atx_server atx_server;
 
@@ -306,7 +308,11 @@ typedef struct atx_server_config {
     uint32_t max_pending;       /* queued jobs before submit returns ATX_ERR_BUSY (0 = unbounded) */
     uint32_t host_fail_pass;    /* with ATX_FLAG_HOST_EXECUTOR: pass number at which the simulated device
                                    reports an error (fault injection on the host; 0 = never) */
+    uint32_t policy;            /* ATX_ADMIT_ARRIVAL or ATX_ADMIT_SMALLEST */
 } atx_server_config;
+
+#define ATX_ADMIT_ARRIVAL 0u    /* admit queued jobs in arrival order */
+#define ATX_ADMIT_SMALLEST 1u   /* admit the queued job with the fewest pixel-samples first */
 
 typedef enum atx_job_state {
     ATX_JOB_QUEUED = 0,
@@ -328,7 +334,7 @@ typedef struct atx_job_info {
 typedef struct atx_server_stats {
     uint64_t submitted, admitted, completed, cancelled, failed, rejected;
     uint64_t passes, paths;
-    double busy_s;              /* wall time spent in passes */
+    double busy_s;              /* device time of the passes (with their read-backs) */
     uint64_t device_bytes;
     uint32_t active, queued;
 } atx_server_stats;
@@ -345,6 +351,10 @@ ATX_API atx_status atx_server_wait(atx_server* s, uint32_t job, uint32_t timeout
 ATX_API atx_status atx_server_read_image(atx_server* s, uint32_t job, uint32_t* host_rgba8, uint64_t n_pixels);
 ATX_API atx_status atx_server_read_accumulation(atx_server* s, uint32_t job, float* host_rgba, uint64_t n_pixels);
 ATX_API atx_status atx_server_cancel(atx_server* s, uint32_t job);
+/* New camera for a queued or active job: its accumulation restarts from frame
+ * 1 and it renders its full target again (main.cpp:24-29 resets the frame
+ * index when the camera moves). */
+ATX_API atx_status atx_server_set_camera(atx_server* s, uint32_t job, const atx_camera* camera);
 /* Forgets a finished or cancelled job and its host copies. */
 ATX_API atx_status atx_server_release(atx_server* s, uint32_t job);
 ATX_API atx_status atx_server_get_stats(atx_server* s, atx_server_stats* stats);

@@ -30,23 +30,24 @@ def alone(sc, spp, frames_before=0):
         return r.get_accumulation().reshape(-1, 4).copy(), r.get_image().reshape(-1).copy()
 
 
-def test_mix_equals_alone_two_passes():
+def test_mix_equals_alone_three_passes():
     mix = small_mix()
     with Batch() as b:
         ids = [b.add_synthetic(sc) for sc in mix]
         for i, sc in zip(ids, mix):
             b.set_spp(i, sc.spp)
-        b.run()
-        b.run()                       # second pass continues each accumulation
+        b.run()                       # a new shape: launched directly
+        b.run()                       # continues each accumulation (no clear): another new shape
+        b.run()                       # same shape as the last: replayed from the captured graph
         for i, sc in zip(ids, mix):
             acc, img = b.get_accumulation(i), b.get_image(i)
-            ref_acc, ref_img = alone(sc, sc.spp, frames_before=sc.spp)
+            ref_acc, ref_img = alone(sc, sc.spp, frames_before=2 * sc.spp)
             assert bit_mismatches(acc, ref_acc) == 0, sc.name
             assert np.array_equal(img, ref_img), sc.name
-            assert b.frame_index(i) == 1 + 2 * sc.spp
+            assert b.frame_index(i) == 1 + 3 * sc.spp
         st = b.stats()
-        assert st["passes"] == 2 and st["graph_launches"] >= 1
-        assert st["paths"] == 2 * sum(sc.width * sc.height * sc.spp for sc in mix)
+        assert st["passes"] == 3 and st["graph_launches"] == 1
+        assert st["paths"] == 3 * sum(sc.width * sc.height * sc.spp for sc in mix)
 
 
 def test_batch_matches_oracle_and_lbvh_scene(po):

@@ -90,3 +90,30 @@ def N_bytes(sc):
     tables = 24 * n + 48 * len(sc.materials) + 32 * len(sc.lights) + 8 * 256
     bvh = 200 * n if n >= 1024 else 0
     return tables + bvh + 20 * px + 512
+
+
+def test_camera_change_while_queued_and_while_active():
+    jobs = mix(2, scale=8, seed=11)
+    (sa, ta), (sb, tb) = jobs
+    moved = lambda sc: scenes.SyntheticScene(**{**sc.__dict__,
+                                                "camera_position": tuple(p + 0.7 for p in sc.camera_position)})
+    cam = lambda sc: Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction)
+    with Server(pass_spp=1, max_active_jobs=1) as s:
+        a = s.submit(sa, 64)
+        b = s.submit(sb, tb)
+        s.set_camera(b, cam(moved(sb)))            # still queued behind a: takes the new camera as is
+        while s.poll(a)["frames_done"] < 2:
+            time.sleep(0.001)
+        restarted = True
+        try:
+            s.set_camera(a, cam(moved(sa)))        # active: restarts from frame 1
+        except Exception:
+            restarted = False                      # finished already (a fast GPU): nothing to check
+        s.wait(a, 60000)
+        s.wait(b, 60000)
+        ref_b, _ = alone(moved(sb), tb)
+        assert bit_mismatches(s.accumulation(b), ref_b) == 0
+        if restarted:
+            ref_a, _ = alone(moved(sa), 64)
+            assert s.poll(a)["frames_done"] == 64
+            assert bit_mismatches(s.accumulation(a), ref_a) == 0

@@ -145,3 +145,34 @@ def test_concurrent_submitters_and_pass_slicing():
         assert st["completed"] == 40 and st["submitted"] == 40
         # pass slices were scaled down: never more than max_pass_paths per pass (or one frame per job)
         assert st["paths"] <= st["passes"] * max(32 * 16 * 6, 32 * 16 * 64)
+
+
+def test_smallest_first_policy():
+    """With one slot busy, queued jobs are admitted smallest first (arrival order by default)."""
+    order = {}
+    for policy in ("arrival", "smallest"):
+        with Server(host_executor=True, max_active_jobs=1, pass_spp=64, policy=policy) as s:
+            blocker = s.submit(job_scene(512, 512), 64)          # holds the slot for ~17 ms
+            big = s.submit(job_scene(256, 256), 64)
+            small = s.submit(job_scene(16, 16), 4)
+            for j in (blocker, big, small):
+                s.wait(j, 10000)
+            order[policy] = s.poll(small)["done_s"] < s.poll(big)["done_s"]
+    assert order == {"arrival": False, "smallest": True}
+
+
+def test_camera_change_restarts_job():
+    sc = job_scene(512, 512)                     # 0.26 ms of simulated device time per frame
+    with Server(host_executor=True, pass_spp=1) as s:
+        j = s.submit(sc, 40)
+        while s.poll(j)["frames_done"] < 5:
+            time.sleep(0.0005)
+        cam = Camera(sc.fov, sc.near, sc.far, (1.0, 2.0, 3.0), sc.camera_direction)
+        s.set_camera(j, cam)
+        s.wait(j, 10000)
+        info = s.poll(j)
+        assert info["state"] == "done" and info["frames_done"] == 40
+        assert np.all(s.image(j) == 40)          # every frame of the result is from after the change
+        with pytest.raises(AtxError) as e:
+            s.set_camera(j, cam)                 # finished: nothing to restart
+        assert e.value.status == 5
