@@ -11,7 +11,7 @@ namespace atx {
 namespace {
 constexpr uint32_t kDefaultLanes = 8;
 constexpr uint32_t kMaxLanes = 64;
-constexpr uint32_t kDefaultLaneWavePaths = 8u << 20;   // 8 Mi paths (about 1.1 GB of path state) per lane
+constexpr uint32_t kDefaultLaneWavePaths = 16u << 20;  // 16 Mi paths (about 2.2 GB of path state) per lane
 constexpr uint32_t kDefaultBvhThreshold = 1024;
 
 // Relative device time of one pass of a scene: paths x (1 + B/2) rays, each

@@ -24,6 +24,7 @@ constexpr uint32_t kDefaultPassSpp = 16;
 constexpr uint64_t kDefaultPassPaths = 1ull << 30;
 constexpr uint32_t kDefaultBvhThreshold = 1024;
 constexpr size_t kPassesInFlight = 2;                 // the one running and the next
+constexpr uint64_t kMinSlicePaths = 4ull << 20;       // a job's slice fills at least a few-Mi-path wave
 constexpr uint64_t kPinnedCacheBytes = 4ull << 30;    // result buffers kept for reuse
 
 uint64_t up256(uint64_t x) { return (x + 255u) & ~uint64_t(255u); }
@@ -252,6 +253,7 @@ std::unique_ptr<Executor> make_host_executor(uint32_t fail_pass) { return std::m
 Server::Server(const atx_server_config& cfg) : cfg_(cfg)
 {
     if (!cfg_.max_active_jobs) cfg_.max_active_jobs = kDefaultActive;
+    auto_slice_ = cfg_.pass_spp == 0;   // explicit pass_spp: slices of exactly that many frames
     if (!cfg_.pass_spp) cfg_.pass_spp = kDefaultPassSpp;
     if (!cfg_.max_pass_paths) cfg_.max_pass_paths = kDefaultPassPaths;
     exec_ = (cfg_.base.flags & ATX_FLAG_HOST_EXECUTOR) ? make_host_executor(cfg_.host_fail_pass)
@@ -408,12 +410,18 @@ atx_status Server::queue_pass_locked(bool* queued)
     }
     active_.swap(keep);
 
-    // slices: up to pass_spp frames per job, scaled down so a pass stays bounded
+    // slices: pass_spp frames per job (by default, more for small images so
+    // that every slice is at least kMinSlicePaths: a small wave is mostly
+    // launch latency and tail), scaled down so a pass stays within
+    // max_pass_paths
     std::vector<std::pair<uint32_t, uint32_t>> plan;   // job, frames this pass
     uint64_t total = 0;
     for (uint32_t jid : active_) {
         const Job& j = jobs_[jid];
-        const uint32_t q = std::min(j.target - j.queued, cfg_.pass_spp);
+        const uint64_t px = (uint64_t)j.desc.width * j.desc.height;
+        const uint64_t want =
+            auto_slice_ ? std::max<uint64_t>(cfg_.pass_spp, (kMinSlicePaths + px - 1) / px) : cfg_.pass_spp;
+        const uint32_t q = (uint32_t)std::min<uint64_t>(j.target - j.queued, want);
         plan.emplace_back(jid, q);
         total += (uint64_t)j.desc.width * j.desc.height * q;
     }

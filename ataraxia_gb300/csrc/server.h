@@ -109,6 +109,7 @@ private:
     void free_results(Job& j);
 
     atx_server_config cfg_;
+    bool auto_slice_ = true;
     std::unique_ptr<Executor> exec_;
     std::chrono::steady_clock::time_point t0_;
     std::thread worker_;

@@ -1,6 +1,7 @@
-// Device-side tracing shared by the wavefront kernels (wavefront.cu) and the
-// batched persistent kernel (batch.cu): primary directions, the brute-force
-// nearest / any hit over a sphere table and their dispatch to the LBVH.
+// Device-side tracing used by the wavefront kernels (wavefront.cu) and the
+// allocation-free entry point (noalloc.cu): primary directions, the
+// brute-force nearest / any hit over a sphere table and their dispatch to the
+// LBVH.
 #pragma once
 
 #include <cstdint>

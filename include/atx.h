@@ -257,7 +257,7 @@ typedef struct atx_batch_stats {
 /* Tuning knobs (0 = keep the current value). */
 typedef struct atx_batch_tuning {
     uint32_t lanes;             /* concurrent streams, each with its own path state (default 8) */
-    uint32_t lane_wave_paths;   /* path-state capacity of one lane, paths (default 8 Mi = 1.1 GB) */
+    uint32_t lane_wave_paths;   /* path-state capacity of one lane, paths (default 16 Mi = 2.2 GB) */
     uint32_t threads;           /* threads per CTA of the wavefront kernels (0 = per-kernel default) */
     uint32_t bvh_threshold;     /* sphere count from which a scene uses its LBVH */
     uint32_t bvh_leaf_size;
@@ -303,8 +303,8 @@ typedef struct atx_server atx_server;
 typedef struct atx_server_config {
     atx_config base;            /* device, hbm_budget_bytes (0 = unlimited), bvh settings, flags */
     uint32_t max_active_jobs;   /* jobs rendered together (0 = 64) */
-    uint32_t pass_spp;          /* frames per job per pass (0 = 16) */
-    uint64_t max_pass_paths;    /* bound on pixel-samples per pass, scaling slices down (0 = 2^28) */
+    uint32_t pass_spp;          /* frames per job per pass (0 = 16, raised for small images to 4 Mi paths per slice) */
+    uint64_t max_pass_paths;    /* bound on pixel-samples per pass, scaling slices down (0 = 2^30) */
     uint32_t max_pending;       /* queued jobs before submit returns ATX_ERR_BUSY (0 = unbounded) */
     uint32_t host_fail_pass;    /* with ATX_FLAG_HOST_EXECUTOR: pass number at which the simulated device
                                    reports an error (fault injection on the host; 0 = never) */
