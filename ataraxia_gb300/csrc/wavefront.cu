@@ -1,15 +1,11 @@
 // Wavefront path tracer for sm_103a: the reference's per-pixel loop
 // (Renderer.cu:287-387) split into queue-driven stages.
 //
-//   k_primary        nearest hit of each pixel's primary ray (Camera.cpp:
-//                    161-195), once per pixel: the primary ray depends only on
-//                    the pixel, so its samples share the hit.
-//   k_intersect      bounce b > 0: nearest hit of each extension-queue ray over
-//                    the sphere table staged in shared memory (or the LBVH).
-//   k_extend<FIRST>  bounce b: shading of the hit (the shared primary hit at
-//                    b = 0, k_intersect's at b > 0), light pick and the shadow
-//                    ray, Russian roulette and the next direction.  Survivors
-//                    go to the next extension queue, shadow rays to the shadow
+//   k_extend<FIRST>  bounce b: (FIRST: generate the primary ray, Camera.cpp:
+//                    161-195) nearest hit over the sphere table staged in
+//                    shared memory, shading, light pick and the shadow ray,
+//                    Russian roulette and the next direction.  Survivors go to
+//                    the next extension queue, shadow rays to the shadow
 //                    queue, both through warp-aggregated atomics.
 //   k_shadow         any-hit over the shadow queue of bounce b; unoccluded
 //                    rays add their contribution to the path colour.
@@ -84,40 +80,10 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
 
 // SHARED (first bounce only): take the nearest hit from k_primary's per-pixel
 // record instead of tracing the primary ray again.
-// Where k_extend takes a path's nearest hit from: traced here, the pixel's
-// shared primary hit (bounce 0), or the hit buffer k_intersect filled.
-enum : int { kHitTrace = 0, kHitPrimary = 1, kHitBuffer = 2 };
-
-// Bounce b > 0, nearest hit only: one extension-queue entry per thread; the
-// result goes to ws.hit for k_extend.  Kept apart from the shading so this
-// loop runs with the registers it needs (full occupancy) instead of the
-// shading code's.
-template <int IS>
-__global__ void __launch_bounds__(kThreads) k_intersect(SceneView sc, WaveState ws, int bounce)
-{
-    constexpr bool SMEM = IS == kIsSmem;
-    extern __shared__ float4 s_sph[];
-    const uint32_t n = ws.counters[2 * bounce];
-    if (blockIdx.x * blockDim.x >= n) return;
-    if (SMEM) stage_spheres(sc, s_sph);
-    const float4* sph = SMEM ? s_sph : sc.sph;
-    const uint32_t* qin = (bounce & 1) ? ws.q[1] : ws.q[0];
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += stride) {
-        const uint32_t pid = qin[idx];
-        const float4 ro = ws.ray_o[pid];
-        const float4 rd = ws.ray_d[pid];
-        float t = 0.0f;
-        const int32_t hit = scene_nearest<IS>(sc, sph, mk3(ro.x, ro.y, ro.z), mk3(rd.x, rd.y, rd.z), t);
-        ws.hit[idx] = make_uint2(__float_as_uint(t), (uint32_t)hit);
-    }
-}
-
-template <bool FIRST, int IS, int HIT>
+template <bool FIRST, int IS, bool SHARED>
 __global__ void __launch_bounds__(kThreads, 4) k_extend(SceneView sc, CameraView cam, WaveState ws, WaveJob job,
                                                         int bounce)
 {
-    constexpr bool SHARED = HIT == kHitPrimary;
     constexpr bool SMEM = IS == kIsSmem;
     extern __shared__ float4 s_sph[];
     const uint32_t n = !FIRST ? ws.counters[2 * bounce]
@@ -166,14 +132,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_extend(SceneView sc, CameraView
 
             float tmin;
             int32_t hit;
-            if (HIT == kHitPrimary) {
+            if (SHARED) {
                 const uint2 pr = ws.prim[pid / job.spp];
                 tmin = __uint_as_float(pr.x);
                 hit = (int32_t)pr.y;
-            } else if (HIT == kHitBuffer) {
-                const uint2 h = ws.hit[idx];
-                tmin = __uint_as_float(h.x);
-                hit = (int32_t)h.y;
             } else {
                 hit = scene_nearest<IS>(sc, sph, o, d, tmin);
             }
@@ -455,21 +417,19 @@ void with_mode(int mode, F&& f)
 }
 
 template <int IS>
-cudaError_t occupancy(int threads, size_t bytes, int* isx, int* ext, int* sh, int* pr)
+cudaError_t occupancy(int threads, size_t bytes, int* ext, int* sh, int* pr)
 {
     if (bytes > 48 * 1024) {
         const int b = (int)bytes;
         const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-        cudaError_t e = cudaFuncSetAttribute(k_extend<true, IS, kHitTrace>, a, b);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_intersect<IS>, a, b);
+        cudaError_t e = cudaFuncSetAttribute(k_extend<true, IS, false>, a, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_extend<false, IS, false>, a, b);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_primary<IS>, a, b);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shadow<IS>, a, b);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace<IS>, a, b);
         if (e != cudaSuccess) return e;
     }
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(isx, k_intersect<IS>, threads, bytes);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ext, k_extend<false, kIsGlobal, kHitBuffer>, threads, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ext, k_extend<false, IS, false>, threads, bytes);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(sh, k_shadow<IS>, threads, bytes);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(pr, k_primary<IS>, threads, bytes);
     return e;
@@ -485,11 +445,10 @@ cudaError_t plan_launch(const SceneView& sc, int device, int threads, LaunchShap
     if (e != cudaSuccess) return e;
     const int mode = isect_mode(sc);
     const size_t bytes = mode == kIsSmem ? (size_t)sc.n_sph * sizeof(float4) : 0;
-    int isx = 0, ext = 0, sh = 0, pr = 0;
-    with_mode(mode, [&](auto m) { e = occupancy<decltype(m)::value>(threads, bytes, &isx, &ext, &sh, &pr); });
+    int ext = 0, sh = 0, pr = 0;
+    with_mode(mode, [&](auto m) { e = occupancy<decltype(m)::value>(threads, bytes, &ext, &sh, &pr); });
     if (e != cudaSuccess) return e;
     out->threads = threads;
-    out->blocks_intersect = sms * (isx > 0 ? isx : 1);
     out->blocks_extend = sms * (ext > 0 ? ext : 1);
     out->blocks_shadow = sms * (sh > 0 ? sh : 1);
     out->blocks_primary = sms * (pr > 0 ? pr : 1);
@@ -523,24 +482,20 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
                 ++nl;
                 // no sphere table needed: the nearest hit comes from k_primary
                 begin(kFamExtend);
-                k_extend<true, kIsGlobal, kHitPrimary><<<g0, shape.threads, 0, stream>>>(sc, cam, ws, job, 0);
+                k_extend<true, kIsGlobal, true><<<g0, shape.threads, 0, stream>>>(sc, cam, ws, job, 0);
                 end(kFamExtend);
             } else {
                 begin(kFamExtend);
-                k_extend<true, IS, kHitTrace><<<g0, shape.threads, sm, stream>>>(sc, cam, ws, job, 0);
+                k_extend<true, IS, false><<<g0, shape.threads, sm, stream>>>(sc, cam, ws, job, 0);
                 end(kFamExtend);
             }
             ++nl;
             for (int b = 0; b < bounces; ++b) {
                 if (b > 0) {
                     begin(kFamExtend);
-                    k_intersect<IS><<<shape.blocks_intersect, shape.threads, sm, stream>>>(sc, ws, b);
+                    k_extend<false, IS, false><<<shape.blocks_extend, shape.threads, sm, stream>>>(sc, cam, ws, job, b);
                     end(kFamExtend);
-                    begin(kFamExtend);
-                    k_extend<false, kIsGlobal, kHitBuffer>
-                        <<<shape.blocks_extend, shape.threads, 0, stream>>>(sc, cam, ws, job, b);
-                    end(kFamExtend);
-                    nl += 2;
+                    ++nl;
                 }
                 begin(kFamShadow);
                 k_shadow<IS><<<shape.blocks_shadow, shape.threads, sm, stream>>>(sc, ws, b);

@@ -94,7 +94,6 @@ struct WaveState {
     unsigned long long* totals;   // [0] extension rays after bounce 0, [1] shadow rays (running sums)
     uint2* prim;                  // per pixel of the wave: primary hit (t bits, sphere id), shared by its samples
     uint32_t* hitq;               // wave pixels whose primary ray hits (only those get first-bounce paths)
-    uint2* hit;                   // bounce b > 0: nearest hit (t bits, sphere id) of extension-queue entry idx
     uint32_t capacity;
 };
 
@@ -126,7 +125,6 @@ public:
 };
 
 struct LaunchShape {
-    int blocks_intersect;
     int blocks_extend;
     int blocks_shadow;
     int blocks_primary;
