@@ -40,6 +40,7 @@ Batch::~Batch()
         for (Lane& l : lanes_) {
             l.wave.buf.reset();
             if (l.done) cudaEventDestroy(l.done);
+            if (l.mark) cudaEventDestroy(l.mark);
             if (l.stream) cudaStreamDestroy(l.stream);
         }
         totals_.reset();
@@ -198,7 +199,7 @@ atx_status Batch::set_camera(uint32_t id, const atx_camera& c)
 atx_status Batch::set_tuning(const atx_batch_tuning& t)
 {
     ATX_CUDA(cudaSetDevice(cfg_.device));
-    if (t.lanes) tuning_.lanes = std::min(t.lanes, kMaxLanes);
+    if (t.lanes) tuning_.lanes = std::min(t.lanes, kMaxLanes);   // <= 64: lane sets are 64-bit masks
     if (t.lane_wave_paths && t.lane_wave_paths != tuning_.lane_wave_paths) {
         tuning_.lane_wave_paths = std::max<uint32_t>(t.lane_wave_paths, 1u << 16);
         release_scratch();
@@ -219,6 +220,7 @@ atx_status Batch::ensure_lanes(uint32_t n)
         Lane l;
         ATX_CUDA(cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking));
         ATX_CUDA(cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming));
+        ATX_CUDA(cudaEventCreateWithFlags(&l.mark, cudaEventDisableTiming));
         lanes_.push_back(std::move(l));
     }
     return ATX_OK;
@@ -227,43 +229,50 @@ atx_status Batch::ensure_lanes(uint32_t n)
 atx_status Batch::run(cudaEvent_t done)
 {
     ATX_CUDA(cudaSetDevice(cfg_.device));
-    struct Work {
+    // Work items: a scene's pass, split into pixel ranges when it is larger
+    // than one lane's wave so that a big scene spreads over several lanes
+    // (ranges of pixels are independent: their accumulator rows are disjoint).
+    struct Part {
         uint32_t id;
         double cost;
-        uint32_t frame0;
+        uint64_t pix_begin, pix_end;
     };
-    std::vector<Work> work;
+    const uint32_t max_lanes = std::max<uint32_t>(tuning_.lanes, 1u);
+    std::vector<Part> parts;
     uint64_t paths = 0;
     for (uint32_t i = 0; i < slots_.size(); ++i) {
         Slot* s = slots_[i].get();
         if (!s || s->spp_next == 0) continue;
-        const uint64_t p = (uint64_t)s->w * s->h * s->spp_next;
-        work.push_back({i, pass_cost(s->scene.view, p, s->settings.max_bounces), 0});
+        const uint64_t px = (uint64_t)s->w * s->h;
+        const uint64_t p = px * s->spp_next;
         paths += p;
+        const uint64_t want = (p + tuning_.lane_wave_paths - 1) / tuning_.lane_wave_paths;
+        const uint32_t n = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>({want, max_lanes, px}));
+        const double c = pass_cost(s->scene.view, p, s->settings.max_bounces) / n;
+        for (uint32_t k = 0; k < n; ++k) parts.push_back({i, c, px * k / n, px * (k + 1) / n});
     }
     ++st_.passes;
     st_.waves_last_pass = 0;
-    if (work.empty()) {
+    if (parts.empty()) {
         if (done) ATX_CUDA(cudaEventRecord(done, stream_));
         return ATX_OK;
     }
-    ATX_CUDA(cudaStreamWaitEvent(stream_, uploaded_, 0));   // scenes added since the last pass
 
     // longest first onto the least-loaded lane
-    std::stable_sort(work.begin(), work.end(), [](const Work& a, const Work& b) { return a.cost > b.cost; });
-    const uint32_t nl = std::min<uint32_t>(std::max<uint32_t>(tuning_.lanes, 1u), (uint32_t)work.size());
+    std::stable_sort(parts.begin(), parts.end(), [](const Part& a, const Part& b) { return a.cost > b.cost; });
+    const uint32_t nl = std::min<uint32_t>(max_lanes, (uint32_t)parts.size());
     ATX_TRY(ensure_lanes(nl));
     std::vector<std::vector<uint32_t>> plan(nl);
     std::vector<double> load(nl, 0.0);
-    for (uint32_t k = 0; k < work.size(); ++k) {
+    for (uint32_t k = 0; k < parts.size(); ++k) {
         const uint32_t lane = (uint32_t)(std::min_element(load.begin(), load.end()) - load.begin());
         plan[lane].push_back(k);
-        load[lane] += work[k].cost;
+        load[lane] += parts[k].cost;
     }
     // path state: one buffer per lane, deep enough for its deepest scene
     for (uint32_t l = 0; l < nl; ++l) {
         int32_t maxb = 0;
-        for (uint32_t k : plan[l]) maxb = std::max(maxb, slots_[work[k].id]->settings.max_bounces);
+        for (uint32_t k : plan[l]) maxb = std::max(maxb, slots_[parts[k].id]->settings.max_bounces);
         Lane& ln = lanes_[l];
         if (ln.wave.view.capacity < tuning_.lane_wave_paths || ln.wave.bounces < (uint32_t)maxb) drop_graph();
         ATX_TRY(ln.wave.ensure(tuning_.lane_wave_paths, (uint32_t)maxb, &scratch_));
@@ -271,29 +280,40 @@ atx_status Batch::run(cudaEvent_t done)
     }
     // frame bookkeeping (Renderer.cu:175-182, 245-248): this pass renders
     // frames [frame0, frame0 + spp) of each scene
-    for (Work& w : work) {
-        Slot* s = slots_[w.id].get();
+    std::vector<uint32_t> frame0(slots_.size(), 0u);
+    for (uint32_t i = 0; i < slots_.size(); ++i) {
+        Slot* s = slots_[i].get();
+        if (!s || s->spp_next == 0) continue;
         if (!s->settings.accumulation) s->frame = 1;
-        w.frame0 = s->frame;
+        frame0[i] = s->frame;
         s->frame = s->settings.accumulation ? s->frame + s->spp_next : 1u;
     }
+    // lanes each scene's parts run on this pass
+    std::vector<uint64_t> now_lanes(slots_.size(), 0u);
+    for (uint32_t l = 0; l < nl; ++l)
+        for (uint32_t k : plan[l]) now_lanes[parts[k].id] |= 1ull << l;
 
-    // The graph's shape: lanes, their scenes in order, whether each clears its
-    // accumulator, its waves and bounces.  A pass of the same shape as the
-    // last one replays the graph with updated kernel arguments; a pass of a
-    // new shape (scenes come and go in a server) is launched directly, since
-    // capturing and instantiating a graph used once costs more host time.
+    // The graph's shape: lanes, their parts in order, whether each clears its
+    // accumulator rows, its waves and bounces.  A pass of the same shape as
+    // the last one replays the graph with updated kernel arguments; a pass of
+    // a new shape (scenes come and go in a server) is launched directly,
+    // since capturing and instantiating a graph used once costs more host time.
+    auto part_waves = [&](const Part& q, uint32_t cap) {
+        const Slot* s = slots_[q.id].get();
+        const WavePlan wp = plan_waves(q.pix_end - q.pix_begin, s->spp_next, cap);
+        return ((q.pix_end - q.pix_begin + wp.pixels_per_wave - 1) / wp.pixels_per_wave) *
+               ((s->spp_next + wp.spp_per_wave - 1) / wp.spp_per_wave);
+    };
     std::vector<uint64_t> sig;
     for (uint32_t l = 0; l < nl; ++l) {
         sig.push_back(0xffffffff00000000ull | l);
         for (uint32_t k : plan[l]) {
-            const Slot* s = slots_[work[k].id].get();
-            const uint64_t px = (uint64_t)s->w * s->h;
-            const WavePlan wp = plan_waves(px, s->spp_next, lanes_[l].wave.view.capacity);
-            sig.push_back(work[k].id);
-            sig.push_back(((uint64_t)(work[k].frame0 == 1) << 63) | ((uint64_t)(uint32_t)s->settings.max_bounces << 32) |
-                          (((px + wp.pixels_per_wave - 1) / wp.pixels_per_wave) *
-                           ((s->spp_next + wp.spp_per_wave - 1) / wp.spp_per_wave)));
+            const Part& q = parts[k];
+            const Slot* s = slots_[q.id].get();
+            sig.push_back(((uint64_t)q.id << 32) | (q.pix_begin & 0xffffffffu));
+            sig.push_back(((uint64_t)(frame0[q.id] == 1) << 63) |
+                          ((uint64_t)(uint32_t)s->settings.max_bounces << 32) |
+                          part_waves(q, lanes_[l].wave.view.capacity));
         }
     }
     const bool graphs = !(cfg_.flags & ATX_FLAG_NO_GRAPHS) && sig == last_sig_;
@@ -301,25 +321,43 @@ atx_status Batch::run(cudaEvent_t done)
     if (!graphs) drop_graph();
     uint32_t launches = 0, waves = 0;
     uint64_t prim = 0;
+    // direct launch: a lane that takes over a scene, or part of one, from
+    // other lanes waits for their queued work (the scene's last pass); a lane
+    // continues with its own scenes in stream order
+    std::vector<uint64_t> waits(nl, 0u);   // per lane: lanes whose marks it waits for
+    if (!graphs) {
+        for (uint32_t l = 0; l < nl; ++l)
+            for (uint32_t k : plan[l]) waits[l] |= slots_[parts[k].id]->lanes & ~(1ull << l);
+        for (Lane& ln : lanes_) ATX_CUDA(cudaEventRecord(ln.mark, ln.stream));
+    }
+    // A graph pass forks from the batch stream (a barrier); so does a direct
+    // pass after a graph pass, whose kernels ran on the batch stream.
+    const bool fork = graphs || last_graph_;
+    if (fork) ATX_CUDA(cudaStreamWaitEvent(stream_, uploaded_, 0));   // scenes added since the last pass
     auto enqueue = [&]() -> atx_status {
-        ATX_CUDA(cudaEventRecord(fork_, stream_));
+        if (fork) ATX_CUDA(cudaEventRecord(fork_, stream_));
         for (uint32_t l = 0; l < nl; ++l) {
             Lane& ln = lanes_[l];
-            ATX_CUDA(cudaStreamWaitEvent(ln.stream, fork_, 0));
+            if (fork) {
+                ATX_CUDA(cudaStreamWaitEvent(ln.stream, fork_, 0));
+            } else {
+                ATX_CUDA(cudaStreamWaitEvent(ln.stream, uploaded_, 0));
+                for (uint32_t from = 0; from < (uint32_t)lanes_.size() && from < 64u; ++from)
+                    if (waits[l] >> from & 1u) ATX_CUDA(cudaStreamWaitEvent(ln.stream, lanes_[from].mark, 0));
+            }
             for (uint32_t k : plan[l]) {
-                Slot* s = slots_[work[k].id].get();
-                const uint64_t px = (uint64_t)s->w * s->h;
-                if (work[k].frame0 == 1) {
-                    ATX_CUDA(enqueue_clear_accum(s->accum.as<float4>(), px, ln.stream));
+                const Part& q = parts[k];
+                Slot* s = slots_[q.id].get();
+                if (frame0[q.id] == 1) {
+                    ATX_CUDA(enqueue_clear_accum(s->accum.as<float4>() + q.pix_begin, q.pix_end - q.pix_begin,
+                                                 ln.stream));
                     ++launches;
                 }
-                const WavePlan wp = plan_waves(px, s->spp_next, ln.wave.view.capacity);
-                waves += (uint32_t)(((px + wp.pixels_per_wave - 1) / wp.pixels_per_wave) *
-                                    ((s->spp_next + wp.spp_per_wave - 1) / wp.spp_per_wave));
-                ATX_TRY(enqueue_frames(s->scene.view, s->cam, ln.wave, s->shape, work[k].frame0, s->spp_next,
+                waves += (uint32_t)part_waves(q, ln.wave.view.capacity);
+                ATX_TRY(enqueue_frames(s->scene.view, s->cam, ln.wave, s->shape, frame0[q.id], s->spp_next,
                                        s->settings.max_bounces, s->settings.sky_light ? 1 : 0, s->accum.as<float4>(),
                                        s->image.as<uint32_t>(), ln.wave.view.capacity, ln.stream, &launches, nullptr,
-                                       &prim));
+                                       &prim, q.pix_begin, q.pix_end));
             }
             ATX_CUDA(cudaEventRecord(ln.done, ln.stream));
             ATX_CUDA(cudaStreamWaitEvent(stream_, ln.done, 0));
@@ -363,6 +401,9 @@ atx_status Batch::run(cudaEvent_t done)
         ATX_TRY(enqueue());
         ATX_CUDA(cudaEventRecord(ev1_, stream_));
     }
+    for (uint32_t i = 0; i < slots_.size(); ++i)
+        if (slots_[i] && now_lanes[i]) slots_[i]->lanes = now_lanes[i];
+    last_graph_ = graphs;
     if (done) ATX_CUDA(cudaEventRecord(done, stream_));
     timed_ = true;
     st_.paths += paths;

@@ -14,7 +14,10 @@
 // A pass with the same shape as the previous one (same scenes on the same
 // lanes, same waves) is captured as one CUDA graph (fork, every lane's
 // kernels, join) and replayed, the instantiated graph's kernel arguments
-// updated in place; a pass of a new shape is launched directly.
+// updated in place.  A pass of a new shape is launched directly and without
+// the fork: each lane continues with its part as soon as it has finished its
+// part of the previous pass (a scene that changes lanes waits for its old
+// lane), so passes overlap instead of meeting at a barrier.
 #pragma once
 
 #include <cstdint>
@@ -68,10 +71,12 @@ private:
         uint32_t w = 0, h = 0;
         uint32_t frame = 1;
         uint32_t spp_next = 0;
+        uint64_t lanes = 0;         // lanes its parts ran on in its last pass (bit l = lane l)
     };
     struct Lane {
         cudaStream_t stream = nullptr;
-        cudaEvent_t done = nullptr;
+        cudaEvent_t done = nullptr;   // after the lane's part of a pass
+        cudaEvent_t mark = nullptr;   // everything queued on the lane before a pass (scenes moving off it)
         WaveStore wave;
     };
     Slot* slot(uint32_t id);
@@ -96,6 +101,7 @@ private:
 
     cudaGraphExec_t graph_ = nullptr;
     std::vector<uint64_t> last_sig_;   // shape of the last pass
+    bool last_graph_ = false;           // the last pass ran as a graph on the batch stream
 
     atx_batch_stats st_{};
     uint64_t primary_rays_ = 0;

@@ -52,63 +52,123 @@ __device__ __forceinline__ float3 safe_inv(float3 d)
     return mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
 }
 
+// Candidate bits of the leaf cluster [first, first + cnt) (cnt <= 32): bit k
+// set unless sphere first + k certainly misses, with the brute-force loop's
+// filter and arithmetic (trace.cuh candidate_bits), so candidates are decided
+// by the same exact test.
+__device__ __forceinline__ uint32_t leaf_candidates(const BvhView& b, uint32_t first, uint32_t cnt, float3 o,
+                                                    float3 d, float a)
+{
+    uint32_t mask = 0u;
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const float4 s = __ldg(&b.leaf_sph[first + k]);
+        const float ox = o.x - s.x, oy = o.y - s.y, oz = o.z - s.z;
+        const float bb = __fmaf_rn(oz, d.z, __fmaf_rn(oy, d.y, ox * d.x));
+        const float cc = __fmaf_rn(oz, oz, __fmaf_rn(oy, oy, __fmaf_rn(ox, ox, -s.w)));
+        const float disc = __fmaf_rn(bb, bb, -(a * cc));
+        mask |= (__float_as_uint(fmaxf(bb, -disc)) >> 31) << k;
+    }
+    return mask;
+}
+
+__device__ __forceinline__ void leaf_nearest(const BvhView& b, uint32_t first, uint32_t cnt, float3 o, float3 d,
+                                             float a, float& tm, int32_t& best)
+{
+    uint32_t mask = leaf_candidates(b, first, cnt, o, d, a);
+    while (mask) {
+        const uint32_t k = (uint32_t)(__ffs(mask) - 1);
+        mask &= mask - 1u;
+        float t;
+        if (sphere_t(__ldg(&b.leaf_sph[first + k]), o, d, a, t) && t > 0.0f) {
+            const int32_t id = (int32_t)__ldg(&b.leaf_id[first + k]);
+            if (t < tm || (t == tm && best >= 0 && id < best)) {
+                tm = t;
+                best = id;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ bool leaf_occluded(const BvhView& b, uint32_t first, uint32_t cnt, float3 o, float3 d,
+                                              float a, float dist2)
+{
+    uint32_t mask = leaf_candidates(b, first, cnt, o, d, a);
+    while (mask) {
+        const uint32_t k = (uint32_t)(__ffs(mask) - 1);
+        mask &= mask - 1u;
+        float t;
+        if (sphere_t(__ldg(&b.leaf_sph[first + k]), o, d, a, t) && t > 0.0f && t * t < dist2) return true;
+    }
+    return false;
+}
+
+// A child of a child-pair node: (ref, count) decoded and bounds-checked.
+// Returns 1 for a leaf cluster (first, cnt set), 2 for an internal node,
+// 0 for a malformed reference (skipped).
+__device__ __forceinline__ int bvh_child(const BvhView& b, uint32_t ref, uint32_t count, uint32_t& first,
+                                         uint32_t& cnt)
+{
+    if (count) {
+        if (ref >= b.n_leaves || count > 32u) return 0;
+        first = ref;
+        cnt = min(count, b.n_leaves - ref);
+        return 1;
+    }
+    return ref < b.n_leaves - 1u ? 2 : 0;
+}
+
 __device__ __forceinline__ int32_t bvh_nearest(const SceneView& sc, float3 o, float3 d, float& tmin)
 {
     const BvhView& b = sc.bvh;
     const float a = dot3(d, d);
-    const float3 inv_d = safe_inv(d);
     float tm = kFltMax;
     int32_t best = -1;
-    const uint32_t n_int = b.n_leaves - 1u;
+    if (b.n_leaves < 2 || b.n_leaves <= b.leaf_size) {   // the whole tree is one cluster
+        leaf_nearest(b, 0u, min(b.n_leaves, 32u), o, d, a, tm, best);
+        tmin = tm;
+        return best;
+    }
+    const float3 inv_d = safe_inv(d);
+    const float inf = __int_as_float(0x7f800000);
     uint32_t stack[kBvhStack];
     int sp = 0;
     stack[sp++] = b.root;
-    // a tree visits each of its 2n-1 nodes at most once; the cap only guards
-    // against a malformed tree
+    // every internal node is pushed at most once; the cap only guards against
+    // a malformed tree
     uint32_t budget = 2u * b.n_leaves + 8u;
     while (sp > 0 && budget-- > 0u) {
         const uint32_t node = stack[--sp];
-        if (node >= n_int + b.n_leaves) continue;
-        uint32_t first, last;
-        if (node >= n_int) {
-            first = last = node - n_int;
-        } else {
-            const uint2 r = __ldg(&b.node_range[node]);
-            first = r.x;
-            last = r.y < b.n_leaves ? r.y : b.n_leaves - 1u;   // never read past the leaves
-        }
-        if (last - first + 1u <= b.leaf_size || node >= n_int) {
-            for (uint32_t k = first; k <= last; ++k) {
-                float t;
-                if (sphere_t(__ldg(&b.leaf_sph[k]), o, d, a, t) && t > 0.0f) {
-                    const int32_t id = (int32_t)__ldg(&b.leaf_id[k]);
-                    if (t < tm || (t == tm && best >= 0 && id < best)) {
-                        tm = t;
-                        best = id;
-                    }
-                }
-            }
-            continue;
-        }
-        const float4 cl = __ldg(&b.node_ctr[node]);
-        const float4 hl = __ldg(&b.node_half[node]);
-        const uint32_t left = __float_as_uint(cl.w);
-        const uint32_t right = __float_as_uint(hl.w);
-        if (left >= n_int + b.n_leaves || right >= n_int + b.n_leaves) continue;   // malformed: skip
-        const float4 c0 = __ldg(&b.node_ctr[left]), h0 = __ldg(&b.node_half[left]);
-        const float4 c1 = __ldg(&b.node_ctr[right]), h1 = __ldg(&b.node_half[right]);
+        if (node >= b.n_leaves - 1u) continue;
+        const float4* p = b.pair + 4 * (size_t)node;
+        const float4 c0 = __ldg(p), h0 = __ldg(p + 1), c1 = __ldg(p + 2), h1 = __ldg(p + 3);
         const float t0 = bvh_box_enter(c0, h0, o, inv_d, tm);
         const float t1 = bvh_box_enter(c1, h1, o, inv_d, tm);
-        const bool v0 = t0 < __int_as_float(0x7f800000);
-        const bool v1 = t1 < __int_as_float(0x7f800000);
-        if (v0 && v1) {
+        uint32_t f0 = 0, n0 = 0, f1 = 0, n1 = 0;
+        int k0 = t0 < inf ? bvh_child(b, __float_as_uint(c0.w), __float_as_uint(h0.w), f0, n0) : 0;
+        int k1 = t1 < inf ? bvh_child(b, __float_as_uint(c1.w), __float_as_uint(h1.w), f1, n1) : 0;
+        // leaf clusters at once, nearer first; internal children onto the stack
+        if (k0 == 1 && k1 == 1 && t1 < t0) {
+            leaf_nearest(b, f1, n1, o, d, a, tm, best);
+            leaf_nearest(b, f0, n0, o, d, a, tm, best);
+            k0 = k1 = 0;
+        }
+        if (k0 == 1) {
+            leaf_nearest(b, f0, n0, o, d, a, tm, best);
+            k0 = 0;
+        }
+        if (k1 == 1) {
+            leaf_nearest(b, f1, n1, o, d, a, tm, best);
+            k1 = 0;
+        }
+        const uint32_t r0 = __float_as_uint(c0.w), r1 = __float_as_uint(c1.w);
+        if (k0 == 2 && k1 == 2) {
             // push the farther child first so the nearer one is popped next
             if (sp + 2 > kBvhStack) break;
-            if (t0 <= t1) { stack[sp++] = right; stack[sp++] = left; }
-            else          { stack[sp++] = left;  stack[sp++] = right; }
-        } else if (v0 || v1) {
+            if (t0 <= t1) { stack[sp++] = r1; stack[sp++] = r0; }
+            else          { stack[sp++] = r0; stack[sp++] = r1; }
+        } else if (k0 == 2 || k1 == 2) {
             if (sp + 1 > kBvhStack) break;
-            stack[sp++] = v0 ? left : right;
+            stack[sp++] = k0 == 2 ? r0 : r1;
         }
     }
     tmin = tm;
@@ -119,46 +179,30 @@ __device__ __forceinline__ bool bvh_occluded(const SceneView& sc, float3 o, floa
 {
     const BvhView& b = sc.bvh;
     const float a = dot3(d, d);
+    if (b.n_leaves < 2 || b.n_leaves <= b.leaf_size) return leaf_occluded(b, 0u, min(b.n_leaves, 32u), o, d, a, dist2);
     const float3 inv_d = safe_inv(d);
+    const float inf = __int_as_float(0x7f800000);
     // any accepted t has t*t < dist2, so t < sqrt(dist2) (1 + 2^-22)
     const float limit = sqrtf(dist2) * 1.0000003f;
-    const uint32_t n_int = b.n_leaves - 1u;
     uint32_t stack[kBvhStack];
     int sp = 0;
     stack[sp++] = b.root;
-    // a tree visits each of its 2n-1 nodes at most once; the cap only guards
-    // against a malformed tree
     uint32_t budget = 2u * b.n_leaves + 8u;
     while (sp > 0 && budget-- > 0u) {
         const uint32_t node = stack[--sp];
-        if (node >= n_int + b.n_leaves) continue;
-        uint32_t first, last;
-        if (node >= n_int) {
-            first = last = node - n_int;
-        } else {
-            const uint2 r = __ldg(&b.node_range[node]);
-            first = r.x;
-            last = r.y < b.n_leaves ? r.y : b.n_leaves - 1u;   // never read past the leaves
-        }
-        if (last - first + 1u <= b.leaf_size || node >= n_int) {
-            for (uint32_t k = first; k <= last; ++k) {
-                float t;
-                if (sphere_t(__ldg(&b.leaf_sph[k]), o, d, a, t) && t > 0.0f && t * t < dist2) return true;
-            }
-            continue;
-        }
-        const float4 cl = __ldg(&b.node_ctr[node]);
-        const float4 hl = __ldg(&b.node_half[node]);
-        const uint32_t left = __float_as_uint(cl.w);
-        const uint32_t right = __float_as_uint(hl.w);
-        if (left >= n_int + b.n_leaves || right >= n_int + b.n_leaves) continue;   // malformed: skip
-        const float4 c0 = __ldg(&b.node_ctr[left]), h0 = __ldg(&b.node_half[left]);
-        const float4 c1 = __ldg(&b.node_ctr[right]), h1 = __ldg(&b.node_half[right]);
-        const bool v0 = bvh_box_enter(c0, h0, o, inv_d, limit) < __int_as_float(0x7f800000);
-        const bool v1 = bvh_box_enter(c1, h1, o, inv_d, limit) < __int_as_float(0x7f800000);
+        if (node >= b.n_leaves - 1u) continue;
+        const float4* p = b.pair + 4 * (size_t)node;
+        const float4 c0 = __ldg(p), h0 = __ldg(p + 1), c1 = __ldg(p + 2), h1 = __ldg(p + 3);
+        uint32_t f0 = 0, n0 = 0, f1 = 0, n1 = 0;
+        const int k0 = bvh_box_enter(c0, h0, o, inv_d, limit) < inf
+                           ? bvh_child(b, __float_as_uint(c0.w), __float_as_uint(h0.w), f0, n0) : 0;
+        const int k1 = bvh_box_enter(c1, h1, o, inv_d, limit) < inf
+                           ? bvh_child(b, __float_as_uint(c1.w), __float_as_uint(h1.w), f1, n1) : 0;
+        if (k0 == 1 && leaf_occluded(b, f0, n0, o, d, a, dist2)) return true;
+        if (k1 == 1 && leaf_occluded(b, f1, n1, o, d, a, dist2)) return true;
         if (sp + 2 > kBvhStack) break;
-        if (v0) stack[sp++] = left;
-        if (v1) stack[sp++] = right;
+        if (k0 == 2) stack[sp++] = __float_as_uint(c0.w);
+        if (k1 == 2) stack[sp++] = __float_as_uint(c1.w);
     }
     return false;
 }

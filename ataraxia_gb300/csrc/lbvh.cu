@@ -12,6 +12,8 @@
 //      over (code, sorted position), which makes every key distinct
 //   5. bottom-up boxes: each leaf thread climbs, the second arrival at a node
 //      forms the union of its children's boxes
+//   6. child-pair nodes for traversal (both children's boxes in one line,
+//      subtrees of at most leaf_size spheres collapsed into leaf clusters)
 #include <cstdint>
 
 #include "lbvh.h"
@@ -251,6 +253,42 @@ __global__ void k_refit(int n, float4* node_ctr, float4* node_half, const uint32
     }
 }
 
+// Child-pair nodes for traversal: internal node i stores both children's boxes
+// in four float4 rows (one 64-byte line), so a traversal step is one load
+// level: [4i] = (centre of child 0, ref 0), [4i+1] = (half extent of child 0,
+// count 0), [4i+2], [4i+3] the same for child 1.  A child whose subtree holds
+// at most leaf_size spheres (a single sphere included) is a leaf cluster:
+// ref = its first sorted sphere, count = its sphere count; otherwise ref = its
+// internal node index and count = 0.
+__global__ void k_pack_pairs(int n, uint32_t leaf_size, const float4* node_ctr, const float4* node_half,
+                             const uint2* range, float4* pair)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const uint32_t child[2] = {__float_as_uint(node_ctr[i].w), __float_as_uint(node_half[i].w)};
+    for (int k = 0; k < 2; ++k) {
+        const uint32_t c = child[k];
+        uint32_t ref, cnt;
+        if (c >= (uint32_t)(n - 1)) {
+            ref = c - (uint32_t)(n - 1);
+            cnt = 1u;
+        } else {
+            const uint2 r = range[c];
+            const uint32_t size = r.y - r.x + 1u;
+            if (size <= leaf_size) {
+                ref = r.x;
+                cnt = size;
+            } else {
+                ref = c;
+                cnt = 0u;
+            }
+        }
+        const float4 ctr = node_ctr[c], half = node_half[c];
+        pair[4 * i + 2 * k] = make_float4(ctr.x, ctr.y, ctr.z, __uint_as_float(ref));
+        pair[4 * i + 2 * k + 1] = make_float4(half.x, half.y, half.z, __uint_as_float(cnt));
+    }
+}
+
 }  // namespace
 
 namespace {
@@ -262,6 +300,7 @@ struct Parts {
     float4* node_ctr;
     float4* node_half;
     uint2* range;
+    float4* pair;
     float4* leaf_sph;
     uint32_t* leaf_id;
     uint32_t *k0, *v0, *k1, *v1;
@@ -284,6 +323,7 @@ uint64_t carve(char* base, uint32_t n, Parts* q)
     q->node_ctr = static_cast<float4*>(take(2 * nn * sizeof(float4)));
     q->node_half = static_cast<float4*>(take(2 * nn * sizeof(float4)));
     q->range = static_cast<uint2*>(take(nn * sizeof(uint2)));
+    q->pair = static_cast<float4*>(take(4 * nn * sizeof(float4)));
     q->leaf_sph = static_cast<float4*>(take(nn * sizeof(float4)));
     q->leaf_id = static_cast<uint32_t*>(take(nn * sizeof(uint32_t)));
     q->k0 = static_cast<uint32_t*>(take(nn * sizeof(uint32_t)));
@@ -349,16 +389,19 @@ cudaError_t lbvh_build(const float4* sph, const float* radius, uint32_t n, uint3
         const int gi = (int)((n - 1 + kT - 1) / kT);
         k_tree<<<gi, kT, 0, stream>>>(k0, (int)n, node_ctr, node_half, range, parent);
         k_refit<<<g, kT, 0, stream>>>((int)n, node_ctr, node_half, parent, visits);
+        const uint32_t ls = leaf_size ? (leaf_size < 32u ? leaf_size : 32u) : 1u;   // clusters fit a 32-bit mask
+        k_pack_pairs<<<gi, kT, 0, stream>>>((int)n, ls, node_ctr, node_half, range, q.pair);
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     out->node_ctr = node_ctr;
     out->node_half = node_half;
     out->node_range = range;
+    out->pair = q.pair;
     out->leaf_sph = leaf_sph;
     out->leaf_id = leaf_id;
     out->n_leaves = n;
-    out->leaf_size = leaf_size ? leaf_size : 1;
+    out->leaf_size = leaf_size ? (leaf_size < 32u ? leaf_size : 32u) : 1u;
     out->root = 0;
     return cudaSuccess;
 }

@@ -373,6 +373,8 @@ def run_batch_compare(args, dist: Dist):
     dev = dist.local_rank
     torch.cuda.set_device(dev)
     mix = scenes.config3(count=args.mix_scenes)
+    if args.max_pass_spp:   # slices of at most this many frames per scene and pass, as a server makes
+        mix = [scenes.SyntheticScene(**{**sc.__dict__, "spp": min(sc.spp, args.max_pass_spp)}) for sc in mix]
     paths = sum(s.width * s.height * s.spp for s in mix)
 
     # plain: one renderer, one launch per scene
@@ -658,6 +660,7 @@ def main(argv=None) -> int:
                     help="serve mode: admission order of the batching server")
     ap.add_argument("--max-pass-paths", type=int, default=0, help="serve mode: bound on paths per pass (0 = default)")
     ap.add_argument("--lanes", type=int, default=0, help="batch mode: concurrent lanes (0 = library default)")
+    ap.add_argument("--max-pass-spp", type=int, default=0, help="batch mode: cap each scene's frames per pass")
     ap.add_argument("--lane-wave", type=int, default=0, help="batch mode: path state per lane, Mi paths")
     ap.add_argument("--width", type=int, default=0, help="render mode: override the viewport width")
     ap.add_argument("--height", type=int, default=0, help="render mode: override the viewport height")
