@@ -109,12 +109,14 @@ atx_status Batch::add_scene(const atx_batch_scene& d, uint32_t* id)
     s->scene.order = &order_;
     s->accum.use_stream_order(&order_);
     s->image.use_stream_order(&order_);
+    s->prim.use_stream_order(&order_);
     // on the upload stream: a pass running on the batch stream is not waited for
     ATX_TRY(s->scene.upload(d.spheres, d.n_spheres, d.materials, d.n_materials, d.lights, d.n_lights, &budget_,
                             up_stream_));
     const uint64_t px = (uint64_t)d.width * d.height;
     ATX_TRY(s->accum.ensure(px * sizeof(float4), &budget_, "batch accumulator"));
     ATX_TRY(s->image.ensure(px * sizeof(uint32_t), &budget_, "batch image"));
+    ATX_TRY(s->prim.ensure(px * sizeof(uint2), &budget_, "batch primary hits"));
     ATX_CUDA(cudaEventRecord(uploaded_, up_stream_));
     ATX_CUDA(plan_launch(s->scene.view, cfg_.device, (int)tuning_.threads, &s->shape));
     s->w = d.width;
@@ -193,6 +195,7 @@ atx_status Batch::set_camera(uint32_t id, const atx_camera& c)
     camera_matrices(c, s->w, s->h, nullptr, s->cam.inv_view, nullptr, s->cam.inv_proj);
     std::memcpy(s->cam.pos, c.position, sizeof(s->cam.pos));
     s->frame = 1;   // a moved camera restarts the accumulation (main.cpp:24-29)
+    s->prim_valid = false;
     return ATX_OK;
 }
 
@@ -357,7 +360,7 @@ atx_status Batch::run(cudaEvent_t done)
                 ATX_TRY(enqueue_frames(s->scene.view, s->cam, ln.wave, s->shape, frame0[q.id], s->spp_next,
                                        s->settings.max_bounces, s->settings.sky_light ? 1 : 0, s->accum.as<float4>(),
                                        s->image.as<uint32_t>(), ln.wave.view.capacity, ln.stream, &launches, nullptr,
-                                       &prim, q.pix_begin, q.pix_end));
+                                       &prim, q.pix_begin, q.pix_end, s->prim.as<uint2>(), s->prim_valid));
             }
             ATX_CUDA(cudaEventRecord(ln.done, ln.stream));
             ATX_CUDA(cudaStreamWaitEvent(stream_, ln.done, 0));
@@ -402,7 +405,10 @@ atx_status Batch::run(cudaEvent_t done)
         ATX_CUDA(cudaEventRecord(ev1_, stream_));
     }
     for (uint32_t i = 0; i < slots_.size(); ++i)
-        if (slots_[i] && now_lanes[i]) slots_[i]->lanes = now_lanes[i];
+        if (slots_[i] && now_lanes[i]) {
+            slots_[i]->lanes = now_lanes[i];
+            slots_[i]->prim_valid = true;   // this pass traced every pixel's primary hit
+        }
     last_graph_ = graphs;
     if (done) ATX_CUDA(cudaEventRecord(done, stream_));
     timed_ = true;

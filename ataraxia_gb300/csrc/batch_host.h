@@ -64,6 +64,8 @@ private:
     struct Slot {
         SceneStore scene;
         DeviceBuffer accum, image;
+        DeviceBuffer prim;          // per-pixel primary hits, traced once per camera (8 B/pixel)
+        bool prim_valid = false;
         atx_camera desc{};
         CameraView cam{};
         LaunchShape shape{};

@@ -204,6 +204,8 @@ extern "C" ATX_API atx_status atx_render_noalloc(const atx_sphere* spheres, uint
             job.max_bounces = settings->max_bounces;
             job.sky = settings->sky_light ? 1 : 0;
             job.pack_frame = (s0 + job.spp >= spp && image) ? last_frame : 0u;
+            job.prim_cache = nullptr;
+            job.prim_cached = 0;
             ATX_CUDA(enqueue_wave(sc, cam, ws, job, shape, acc, image, st, &launches, nullptr));
         }
     }

@@ -210,7 +210,8 @@ atx_status EventTimer::collect(atx_kernel_times* t)
 atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore& ws, const LaunchShape& shape,
                           uint32_t frame0, uint32_t spp, int32_t max_bounces, int32_t sky, float4* accum,
                           uint32_t* image, uint32_t capacity, cudaStream_t stream, uint32_t* launches,
-                          KernelTimer* timer, uint64_t* primary_rays, uint64_t pix_begin, uint64_t pix_end)
+                          KernelTimer* timer, uint64_t* primary_rays, uint64_t pix_begin, uint64_t pix_end,
+                          uint2* prim_cache, bool prim_cached)
 {
     const uint64_t all = (uint64_t)cam.width * cam.height;
     const uint64_t pend = std::min(pix_end, all);
@@ -219,6 +220,7 @@ atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore&
     const uint32_t last_frame = frame0 + spp - 1;
     for (uint64_t p0 = pbeg; p0 < pend; p0 += plan.pixels_per_wave) {
         const uint32_t np = (uint32_t)std::min<uint64_t>(plan.pixels_per_wave, pend - p0);
+        bool filled = prim_cached;   // primary hits of these pixels already traced
         for (uint32_t s0 = 0; s0 < spp; s0 += plan.spp_per_wave) {
             WaveJob job;
             job.pixel0 = (uint32_t)p0;
@@ -228,9 +230,15 @@ atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore&
             job.max_bounces = max_bounces;
             job.sky = sky;
             job.pack_frame = (s0 + job.spp >= spp && image) ? last_frame : 0u;
+            job.prim_cache = prim_cache;
+            // later sample chunks of the same pixels reuse the hits the first traced
+            // (in the cache, or in the wave's own per-pixel rows, which only k_primary writes)
+            job.prim_cached = filled ? 1 : 0;
             ATX_CUDA(enqueue_wave(sc, cam, ws.view, job, shape, accum, image, stream, launches, timer));
-            // primary rays traced: once per pixel when its samples share the hit
-            if (primary_rays && max_bounces > 0) *primary_rays += job.spp > 1 ? np : (uint64_t)np * job.spp;
+            if (wave_shares_primary(job)) filled = true;
+            // primary rays traced: once per pixel when its samples share the hit, none when cached
+            if (primary_rays && max_bounces > 0 && !job.prim_cached)
+                *primary_rays += wave_shares_primary(job) ? np : (uint64_t)np * job.spp;
         }
     }
     return ATX_OK;

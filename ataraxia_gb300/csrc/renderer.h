@@ -48,12 +48,14 @@ struct WavePlan {
 WavePlan plan_waves(uint64_t pixels, uint32_t spp, uint32_t capacity);
 
 // Enqueues frames [frame0, frame0 + spp) for pixels [pix_begin, pix_end) of
-// the view (default: all of them).
+// the view (default: all of them).  prim_cache (W*H entries, optional) keeps
+// the primary hits across calls: traced into it unless prim_cached says it
+// already holds them for this scene and camera.
 atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore& ws, const LaunchShape& shape,
                           uint32_t frame0, uint32_t spp, int32_t max_bounces, int32_t sky, float4* accum,
                           uint32_t* image, uint32_t capacity, cudaStream_t stream, uint32_t* launches,
                           KernelTimer* timer = nullptr, uint64_t* primary_rays = nullptr, uint64_t pix_begin = 0,
-                          uint64_t pix_end = ~uint64_t(0));
+                          uint64_t pix_end = ~uint64_t(0), uint2* prim_cache = nullptr, bool prim_cached = false);
 
 // Records a pair of CUDA events around each kernel and sums their durations
 // per kernel family when collected.

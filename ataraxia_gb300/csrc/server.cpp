@@ -290,7 +290,7 @@ uint64_t Server::job_bytes(const atx_batch_scene& s, uint32_t bvh_threshold)
     uint64_t b = up256(16 * n) + up256(4 * n) + up256(4 * n) + up256(48ull * s.n_materials) + up256(32ull * s.n_lights);
     if (n >= (bvh_threshold ? bvh_threshold : kDefaultBvhThreshold) && n > 1) b += up256(lbvh_bytes((uint32_t)n));
     const uint64_t px = (uint64_t)s.width * s.height;
-    b += up256(16 * px) + up256(4 * px);
+    b += up256(16 * px) + up256(4 * px) + up256(8 * px);   // accumulator, image, primary hits
     return b;
 }
 

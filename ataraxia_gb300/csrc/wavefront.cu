@@ -56,20 +56,26 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
     extern __shared__ float4 s_sph[];
     const uint32_t n = job.n_pixels;
     if (blockIdx.x * blockDim.x >= n) return;
-    if (SMEM) stage_spheres(sc, s_sph);
+    const bool cached = job.prim_cached != 0;   // uniform: only the hit queue is built
+    if (SMEM && !cached) stage_spheres(sc, s_sph);
     const float4* sph = SMEM ? s_sph : sc.sph;
     const float3 o = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t* hits = &ws.counters[2 * ((uint32_t)job.max_bounces + 1u)];
+    uint2* prim = job.prim_cache ? job.prim_cache + job.pixel0 : ws.prim;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {   // warp-uniform trip count
         const uint32_t j = base + threadIdx.x;
         int32_t id = -1;
         if (j < n) {
-            const uint32_t p = job.pixel0 + j;
-            const float3 d = primary_dir(cam, p % cam.width, p / cam.width);
-            float t;
-            id = scene_nearest<IS>(sc, sph, o, d, t);
-            ws.prim[j] = make_uint2(__float_as_uint(t), (uint32_t)id);
+            if (cached) {
+                id = (int32_t)prim[j].y;
+            } else {
+                const uint32_t p = job.pixel0 + j;
+                const float3 d = primary_dir(cam, p % cam.width, p / cam.width);
+                float t;
+                id = scene_nearest<IS>(sc, sph, o, d, t);
+                prim[j] = make_uint2(__float_as_uint(t), (uint32_t)id);
+            }
         }
         // pixels whose primary ray hits get first-bounce paths; the others'
         // samples are closed-form (accumulated by k_accumulate)
@@ -133,7 +139,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_extend(SceneView sc, CameraView
             float tmin;
             int32_t hit;
             if (SHARED) {
-                const uint2 pr = ws.prim[pid / job.spp];
+                const uint2 pr = job.prim_cache ? job.prim_cache[job.pixel0 + pid / job.spp] : ws.prim[pid / job.spp];
                 tmin = __uint_as_float(pr.x);
                 hit = (int32_t)pr.y;
             } else {
@@ -332,12 +338,13 @@ __global__ void __launch_bounds__(kThreads) k_accumulate(WaveState ws, WaveJob j
         atomicAdd(&ws.totals[1], sh);
     }
     // a sample whose shared primary ray missed has colour 0 + sky * 1 (Renderer.cu:311-316)
-    const bool shared = job.spp > 1 && job.max_bounces > 0;
+    const bool shared = wave_shares_primary(job);
+    const uint2* prim = job.prim_cache ? job.prim_cache + job.pixel0 : ws.prim;
     const float4 miss = job.sky ? make_float4(0.6f, 0.7f, 0.9f, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < job.n_pixels; j += stride) {
         const uint32_t p = job.pixel0 + j;
         float4 a = accum[p];
-        const bool missed = shared && (int32_t)ws.prim[j].y < 0;
+        const bool missed = shared && (int32_t)prim[j].y < 0;
         for (uint32_t s = 0; s < job.spp; ++s) {
             float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
             if (missed) c = miss;
@@ -471,7 +478,7 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
         cudaError_t e = cudaMemsetAsync(ws.counters, 0, sizeof(uint32_t) * wave_counter_words(bounces), stream);
         if (e != cudaSuccess) return e;
         const int g0 = grid_for(paths, shape.threads, shape.blocks_extend);
-        const bool share = job.spp > 1;
+        const bool share = wave_shares_primary(job);
         with_mode(shape.mode, [&](auto m) {
             constexpr int IS = decltype(m)::value;
             if (share) {

@@ -112,7 +112,20 @@ struct WaveJob {
     int32_t max_bounces;
     int32_t sky;
     uint32_t pack_frame;      // when non-zero, pack the RGBA8 image at this frame index after accumulating
+    // Per-pixel primary hits of the whole image (indexed by pixel), kept by the
+    // caller across launches of the same scene and camera; nullptr: the wave's
+    // own ws.prim (indexed by wave pixel).  prim_cached: prim_cache already
+    // holds this view's hits, so they are not traced again.
+    uint2* prim_cache;
+    int32_t prim_cached;
 };
+
+// Whether a wave shares each pixel's primary hit among its samples (the hit is
+// traced once, by k_primary, or comes from the cache).
+__host__ __device__ inline bool wave_shares_primary(const WaveJob& j)
+{
+    return j.max_bounces > 0 && (j.spp > 1 || j.prim_cache != nullptr);
+}
 
 // Kernel families timed by KernelTimer.
 enum KernelFamily { kFamExtend = 0, kFamShadow = 1, kFamAccumulate = 2, kFamOther = 3, kFamCount = 4 };

@@ -292,8 +292,9 @@ ATX_API atx_status atx_batch_get_tuning(atx_batch* b, atx_batch_tuning* tuning);
  * from any thread and rendered progressively by a worker thread that runs
  * batched passes (continuous batching).  A job is admitted (in arrival order,
  * or smallest first) when an active slot is free and its device memory (scene
- * tables, LBVH, accumulator, image) fits the HBM budget; its scene, frame
- * index and accumulator stay resident until it reaches its target, when its
+ * tables, LBVH, accumulator, image, per-pixel primary hits) fits the HBM
+ * budget; its scene, frame index, accumulator and primary hits (traced once
+ * per camera) stay resident until it reaches its target, when its
  * image and accumulator are copied to host memory and its device memory is
  * released.  The worker queues the next pass, its uploads and read-backs
  * while the current one runs, so the GPU does not wait for the host.
