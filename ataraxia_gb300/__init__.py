@@ -516,8 +516,10 @@ class Batch:
         N.check(N.lib().atx_batch_get_stats(self._h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in N.BatchStats._fields_}
 
-    def set_tuning(self, lanes=0, lane_wave_paths=0, threads=0, bvh_threshold=0, bvh_leaf_size=0):
-        t = N.BatchTuning(lanes, lane_wave_paths, threads, bvh_threshold, bvh_leaf_size, (C.c_uint32 * 3)())
+    def set_tuning(self, lanes=0, lane_wave_paths=0, threads=0, bvh_threshold=0, bvh_leaf_size=0,
+                   primary_cache=None):
+        pc = 0 if primary_cache is None else (1 if primary_cache else 2)
+        t = N.BatchTuning(lanes, lane_wave_paths, threads, bvh_threshold, bvh_leaf_size, pc, (C.c_uint32 * 2)())
         N.check(N.lib().atx_batch_set_tuning(self._h, C.byref(t)))
 
     def tuning(self) -> dict:

@@ -93,7 +93,8 @@ class BatchStats(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("lanes", C.c_uint32), ("lane_wave_paths", C.c_uint32), ("threads", C.c_uint32),
-                ("bvh_threshold", C.c_uint32), ("bvh_leaf_size", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("bvh_threshold", C.c_uint32), ("bvh_leaf_size", C.c_uint32), ("primary_cache", C.c_uint32),
+                ("reserved", C.c_uint32 * 2)]
 
 
 class ServerConfig(C.Structure):

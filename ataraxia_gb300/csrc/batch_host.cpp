@@ -87,6 +87,7 @@ atx_status Batch::init()
     tuning_.threads = cfg_.threads;
     tuning_.bvh_threshold = cfg_.bvh_threshold ? cfg_.bvh_threshold : kDefaultBvhThreshold;
     tuning_.bvh_leaf_size = cfg_.bvh_leaf_size;
+    tuning_.primary_cache = 1;
     return ATX_OK;
 }
 
@@ -211,6 +212,11 @@ atx_status Batch::set_tuning(const atx_batch_tuning& t)
         tuning_.threads = std::min<uint32_t>(1024, std::max<uint32_t>(32, t.threads & ~31u));
         for (auto& p : slots_)
             if (p) ATX_CUDA(plan_launch(p->scene.view, cfg_.device, (int)tuning_.threads, &p->shape));
+    }
+    if (t.primary_cache) {
+        tuning_.primary_cache = t.primary_cache == 1 ? 1u : 2u;
+        for (auto& p : slots_)
+            if (p) p->prim_valid = false;
     }
     if (t.bvh_threshold) tuning_.bvh_threshold = t.bvh_threshold;   // scenes added from now on
     if (t.bvh_leaf_size) tuning_.bvh_leaf_size = t.bvh_leaf_size;
@@ -360,7 +366,8 @@ atx_status Batch::run(cudaEvent_t done)
                 ATX_TRY(enqueue_frames(s->scene.view, s->cam, ln.wave, s->shape, frame0[q.id], s->spp_next,
                                        s->settings.max_bounces, s->settings.sky_light ? 1 : 0, s->accum.as<float4>(),
                                        s->image.as<uint32_t>(), ln.wave.view.capacity, ln.stream, &launches, nullptr,
-                                       &prim, q.pix_begin, q.pix_end, s->prim.as<uint2>(), s->prim_valid));
+                                       &prim, q.pix_begin, q.pix_end, s->prim.as<uint2>(),
+                                       s->prim_valid && tuning_.primary_cache == 1));
             }
             ATX_CUDA(cudaEventRecord(ln.done, ln.stream));
             ATX_CUDA(cudaStreamWaitEvent(stream_, ln.done, 0));

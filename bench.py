@@ -415,14 +415,28 @@ def run_batch_compare(args, dist: Dist):
     wall = time.perf_counter() - t0
     s1 = b.stats()
     tun = b.tuning()
+    # the same passes with every scene's primary hits traced again each pass
+    b.set_tuning(primary_cache=False)
+    for _ in range(2):
+        b.run()
+    b.synchronize()
+    nc_ms = []
+    for _ in range(args.steps):
+        b.run()
+        b.synchronize()
+        nc_ms.append(b.stats()["last_pass_ms"])
     b.close()
     batched_ms = statistics.mean(pass_ms)
+    nocache_ms = statistics.mean(nc_ms)
     return {"mode": "batch", "scenes": len(mix), "paths_per_pass": paths,
             "plain_ms_per_pass": round(plain_ms, 3), "plain_mpaths_s": round(paths / (plain_ms * 1e-3) / 1e6, 1),
             "batched_ms_per_pass": round(batched_ms, 3),
             "batched_mpaths_s": round(paths / (batched_ms * 1e-3) / 1e6, 1),
             "batched_wall_mpaths_s": round(args.steps * paths / wall / 1e6, 1),
-            "speedup": round(plain_ms / batched_ms, 3), "graph_launches": s1["graph_launches"] - s0["graph_launches"],
+            "speedup": round(plain_ms / batched_ms, 3),
+            "batched_retrace_primary_mpaths_s": round(paths / (nocache_ms * 1e-3) / 1e6, 1),
+            "speedup_retrace_primary": round(plain_ms / nocache_ms, 3),
+            "graph_launches": s1["graph_launches"] - s0["graph_launches"],
             "rays_per_path": round(((s1["extension_rays"] - s0["extension_rays"]) +
                                     (s1["shadow_rays"] - s0["shadow_rays"])) / (args.steps * paths), 3),
             "tuning": tun}

@@ -261,7 +261,8 @@ typedef struct atx_batch_tuning {
     uint32_t threads;           /* threads per CTA of the wavefront kernels (0 = per-kernel default) */
     uint32_t bvh_threshold;     /* sphere count from which a scene uses its LBVH */
     uint32_t bvh_leaf_size;
-    uint32_t reserved[3];
+    uint32_t primary_cache;     /* 1 (default): keep each scene's primary hits across passes; 2: trace them every pass */
+    uint32_t reserved[2];
 } atx_batch_tuning;
 
 ATX_API atx_status atx_batch_create(const atx_config* config, atx_batch** out);

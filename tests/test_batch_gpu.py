@@ -111,12 +111,13 @@ def test_accumulation_off_in_batch():
         assert bit_mismatches(b.get_accumulation(i), ref) == 0
 
 
-@pytest.mark.parametrize("lanes,wave", [(1, 1 << 16), (3, 1 << 17), (16, 1 << 20)])
-def test_tunings_do_not_change_results(lanes, wave):
-    """Lane count and path-state size (down to several waves per scene) leave results unchanged."""
+@pytest.mark.parametrize("lanes,wave,cache", [(1, 1 << 16, True), (3, 1 << 17, False), (16, 1 << 20, True)])
+def test_tunings_do_not_change_results(lanes, wave, cache):
+    """Lane count, path-state size (down to several waves and pixel-range parts per scene) and the
+    primary-hit cache leave results unchanged."""
     mix = small_mix(3)
     with Batch() as b:
-        b.set_tuning(lanes=lanes, lane_wave_paths=wave)
+        b.set_tuning(lanes=lanes, lane_wave_paths=wave, primary_cache=cache)
         ids = [b.add_synthetic(sc) for sc in mix]
         for i, sc in zip(ids, mix):
             b.set_spp(i, 3)
