@@ -522,6 +522,13 @@ class Batch:
         t = N.BatchTuning(lanes, lane_wave_paths, threads, bvh_threshold, bvh_leaf_size, pc, (C.c_uint32 * 2)())
         N.check(N.lib().atx_batch_set_tuning(self._h, C.byref(t)))
 
+    def autotune(self, passes: int = 2) -> dict:
+        """Times lane / path-state settings on the current scenes (all at frame 1) and keeps the fastest
+        (atx_batch_autotune); the scenes are back at frame 1 afterwards."""
+        t = N.BatchTuning()
+        N.check(N.lib().atx_batch_autotune(self._h, passes, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in N.BatchTuning._fields_ if k != "reserved"}
+
     def tuning(self) -> dict:
         t = N.BatchTuning()
         N.check(N.lib().atx_batch_get_tuning(self._h, C.byref(t)))

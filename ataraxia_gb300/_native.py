@@ -176,6 +176,7 @@ SIGNATURES = {
     "atx_batch_get_stats": (_ST, [_P, C.POINTER(BatchStats)]),
     "atx_batch_set_tuning": (_ST, [_P, C.POINTER(BatchTuning)]),
     "atx_batch_set_camera": (_ST, [_P, _U32, C.POINTER(CameraDesc)]),
+    "atx_batch_autotune": (_ST, [_P, _U32, C.POINTER(BatchTuning)]),
     "atx_batch_get_tuning": (_ST, [_P, C.POINTER(BatchTuning)]),
     "atx_server_create": (_ST, [C.POINTER(ServerConfig), C.POINTER(_P)]),
     "atx_server_destroy": (_ST, [_P]),

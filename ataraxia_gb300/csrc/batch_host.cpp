@@ -12,7 +12,7 @@ namespace {
 constexpr uint32_t kDefaultLanes = 8;
 constexpr uint32_t kMaxLanes = 64;
 constexpr uint32_t kDefaultLaneWavePaths = 16u << 20;  // 16 Mi paths (about 2.2 GB of path state) per lane
-constexpr uint32_t kDefaultBvhThreshold = 1024;
+constexpr uint32_t kDefaultBvhThreshold = 512;   // fastest of 256-1024 on the 64-scene mix
 
 // Relative device time of one pass of a scene: paths x (1 + B/2) rays, each
 // N brute-force tests or an LBVH walk, plus a fixed cost per dependent launch
@@ -220,6 +220,45 @@ atx_status Batch::set_tuning(const atx_batch_tuning& t)
     }
     if (t.bvh_threshold) tuning_.bvh_threshold = t.bvh_threshold;   // scenes added from now on
     if (t.bvh_leaf_size) tuning_.bvh_leaf_size = t.bvh_leaf_size;
+    return ATX_OK;
+}
+
+atx_status Batch::autotune(uint32_t passes, atx_batch_tuning* chosen)
+{
+    for (auto& p : slots_)
+        if (p && p->frame != 1) return fail(ATX_ERR_INVALID_ARG, "batch_autotune: scenes must be at frame 1");
+    if (!passes) passes = 2;
+    // lanes x path state per lane (Mi paths); at 132 B per path the largest is ~36 GB
+    const uint32_t cand[][2] = {{4, 32}, {8, 16}, {8, 32}, {16, 8}, {16, 16}};
+    double best = 1e300;
+    atx_batch_tuning pick = tuning_;
+    auto reset_frames = [&]() {
+        for (auto& p : slots_)
+            if (p) p->frame = 1;
+    };
+    for (const auto& c : cand) {
+        atx_batch_tuning t{};
+        t.lanes = c[0];
+        t.lane_wave_paths = c[1] << 20;
+        ATX_TRY(set_tuning(t));
+        ATX_TRY(run());   // a new shape, then its graph capture
+        ATX_TRY(run());
+        double ms = 0.0;
+        for (uint32_t k = 0; k < passes; ++k) {
+            ATX_TRY(run());
+            atx_batch_stats st;
+            ATX_TRY(stats(&st));   // synchronises
+            ms += st.last_pass_ms;
+        }
+        reset_frames();
+        if (ms < best) {
+            best = ms;
+            pick = tuning_;
+        }
+    }
+    ATX_TRY(set_tuning(pick));
+    reset_frames();
+    if (chosen) *chosen = tuning_;
     return ATX_OK;
 }
 

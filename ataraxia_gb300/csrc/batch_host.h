@@ -53,6 +53,7 @@ public:
     atx_status read_async(uint32_t id, uint32_t* image, float* accum, uint64_t n);
     atx_status stats(atx_batch_stats* out);
     atx_status set_tuning(const atx_batch_tuning& t);
+    atx_status autotune(uint32_t passes, atx_batch_tuning* chosen);
     atx_batch_tuning tuning() const { return tuning_; }
     // Device bytes held by resident scenes (charged to the configured budget).
     uint64_t scene_bytes() const { return budget_.used(); }

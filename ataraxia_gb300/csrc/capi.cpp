@@ -706,6 +706,11 @@ ATX_API atx_status atx_batch_get_tuning(atx_batch* b, atx_batch_tuning* t)
     });
 }
 
+ATX_API atx_status atx_batch_autotune(atx_batch* b, uint32_t passes, atx_batch_tuning* chosen)
+{
+    return guarded([&]() -> atx_status { NEEDB(b); return b->impl.autotune(passes, chosen); });
+}
+
 }  // extern "C"
 
 // ------------------------------------------------------------------ serving

@@ -12,7 +12,7 @@ namespace atx {
 
 namespace {
 constexpr uint32_t kDefaultWavePaths = 64u << 20;  // at most 64 Mi paths (8.7 GB of state) per wave
-constexpr uint32_t kDefaultBvhThreshold = 1024;
+constexpr uint32_t kDefaultBvhThreshold = 512;   // fastest of 256-1024 on the 64-scene mix
 constexpr uint32_t kDefaultBvhLeaf = 16;   // fastest of 1..32 on the 65,536-sphere scene
 constexpr uint32_t kMaxBounces = 4096;
 }  // namespace
@@ -252,13 +252,15 @@ Renderer::~Renderer()
 {
     if (cudaSetDevice(cfg_.device) == cudaSuccess) {
         if (stream_) cudaStreamSynchronize(stream_);
-        if (stream2_) cudaStreamSynchronize(stream2_);
+        for (int l = 1; l < kLanes; ++l)
+            if (lane_stream_[l]) cudaStreamSynchronize(lane_stream_[l]);
         scene_ = SceneStore();
-        wave_[0].buf.reset();
-        wave_[1].buf.reset();
+        for (WaveStore& w : wave_) w.buf.reset();
         if (fork_) cudaEventDestroy(fork_);
-        if (join_) cudaEventDestroy(join_);
-        if (stream2_) cudaStreamDestroy(stream2_);
+        for (int l = 1; l < kLanes; ++l) {
+            if (join_[l]) cudaEventDestroy(join_[l]);
+            if (lane_stream_[l]) cudaStreamDestroy(lane_stream_[l]);
+        }
         accum_.reset();
         image_.reset();
         totals_.reset();
@@ -286,9 +288,12 @@ atx_status Renderer::init()
         return fail(ATX_ERR_INVALID_ARG, "device %d out of range (%d visible)", cfg_.device, count);
     ATX_TRY(activate());
     ATX_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
-    ATX_CUDA(cudaStreamCreateWithFlags(&stream2_, cudaStreamNonBlocking));
+    lane_stream_[0] = stream_;
+    for (int l = 1; l < kLanes; ++l) {
+        ATX_CUDA(cudaStreamCreateWithFlags(&lane_stream_[l], cudaStreamNonBlocking));
+        ATX_CUDA(cudaEventCreateWithFlags(&join_[l], cudaEventDisableTiming));
+    }
     ATX_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
-    ATX_CUDA(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
     ATX_CUDA(cudaEventCreate(&ev_start_));
     ATX_CUDA(cudaEventCreate(&ev_stop_));
     ATX_TRY(totals_.ensure(2 * sizeof(unsigned long long), &budget_, "ray totals"));
@@ -384,16 +389,17 @@ atx_status Renderer::render(uint32_t spp)
     ATX_TRY(refresh_camera());
     ATX_TRY(ensure_shape());
     // One wave per lane when it fits: fewer, fuller kernels (the state is
-    // allocated for this launch's paths, rounded up to 1 Mi, and kept).  Two
+    // allocated for this launch's paths, rounded up to 1 Mi, and kept).  All
     // lanes unless the caller fixed the wave size, kernels are being timed
-    // one by one, or the launch is too small to fill two.
+    // one by one, or the launch is too small to fill them.
     const uint64_t px = (uint64_t)width_ * height_;
     const bool profile = (cfg_.flags & ATX_FLAG_PROFILE_KERNELS) != 0;
-    const uint32_t lanes = (cfg_.wave_paths || profile || px < 2 || px * spp < (8ull << 20)) ? 1u : 2u;
-    const uint64_t half = (px + 1) / 2;
+    const uint32_t lanes =
+        (cfg_.wave_paths || profile || px < (uint64_t)kLanes || px * spp < (4ull << 20) * kLanes) ? 1u : kLanes;
+    const uint64_t lane_px = (px + lanes - 1) / lanes;
     uint32_t capacity = cfg_.wave_paths;
     if (!capacity) {
-        const uint64_t lane_paths = (lanes == 2 ? half : px) * spp;
+        const uint64_t lane_paths = lane_px * spp;
         const uint64_t want = (lane_paths + (1u << 20) - 1) & ~uint64_t((1u << 20) - 1);
         capacity = (uint32_t)std::min<uint64_t>(want, kDefaultWavePaths);
     }
@@ -416,19 +422,19 @@ atx_status Renderer::render(uint32_t spp)
     }
     uint64_t primary_rays = 0;
     const int32_t sky = settings_.sky_light ? 1 : 0;
-    if (lanes == 1) {
-        ATX_TRY(enqueue_frames(scene_.view, camv_, wave_[0], shape_, f0, spp, bounces, sky, accum_.as<float4>(),
-                               image_.as<uint32_t>(), capacity, stream_, &launches, timer, &primary_rays));
-    } else {
+    if (lanes > 1) {
         ATX_CUDA(cudaEventRecord(fork_, stream_));
-        ATX_CUDA(cudaStreamWaitEvent(stream2_, fork_, 0));
-        ATX_TRY(enqueue_frames(scene_.view, camv_, wave_[0], shape_, f0, spp, bounces, sky, accum_.as<float4>(),
-                               image_.as<uint32_t>(), capacity, stream_, &launches, nullptr, &primary_rays, 0, half));
-        ATX_TRY(enqueue_frames(scene_.view, camv_, wave_[1], shape_, f0, spp, bounces, sky, accum_.as<float4>(),
-                               image_.as<uint32_t>(), capacity, stream2_, &launches, nullptr, &primary_rays, half,
-                               px));
-        ATX_CUDA(cudaEventRecord(join_, stream2_));
-        ATX_CUDA(cudaStreamWaitEvent(stream_, join_, 0));
+        for (uint32_t l = 1; l < lanes; ++l) ATX_CUDA(cudaStreamWaitEvent(lane_stream_[l], fork_, 0));
+    }
+    for (uint32_t l = 0; l < lanes; ++l) {
+        const uint64_t b = std::min(px, l * lane_px), e = std::min(px, (l + 1) * lane_px);
+        ATX_TRY(enqueue_frames(scene_.view, camv_, wave_[l], shape_, f0, spp, bounces, sky, accum_.as<float4>(),
+                               image_.as<uint32_t>(), capacity, lane_stream_[l], &launches, l == 0 ? timer : nullptr,
+                               &primary_rays, b, e));
+    }
+    for (uint32_t l = 1; l < lanes; ++l) {
+        ATX_CUDA(cudaEventRecord(join_[l], lane_stream_[l]));
+        ATX_CUDA(cudaStreamWaitEvent(stream_, join_[l], 0));
     }
     ATX_CUDA(cudaEventRecord(ev_stop_, stream_));
     timed_ = true;

@@ -126,12 +126,14 @@ private:
     bool cam_dirty_ = true;
 
     SceneStore scene_;
-    // Two lanes: a launch's pixels are split in halves rendered on two
-    // streams with their own path state, so one half's last, sparse bounces
-    // overlap the other half's work instead of leaving SMs idle.
-    WaveStore wave_[2];
-    cudaStream_t stream2_ = nullptr;
-    cudaEvent_t fork_ = nullptr, join_ = nullptr;
+    // Lanes: a launch's pixels are split into kLanes ranges rendered on as
+    // many streams with their own path state, so one range's last, sparse
+    // bounces overlap the others' work instead of leaving SMs idle.  Lane 0
+    // is the renderer's stream.
+    static constexpr int kLanes = 2;
+    WaveStore wave_[kLanes];
+    cudaStream_t lane_stream_[kLanes] = {};
+    cudaEvent_t fork_ = nullptr, join_[kLanes] = {};
     DeviceBuffer accum_, image_, totals_;
     LaunchShape shape_{};
     bool shape_valid_ = false;

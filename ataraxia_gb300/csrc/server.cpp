@@ -22,7 +22,7 @@ namespace {
 constexpr uint32_t kDefaultActive = 64;
 constexpr uint32_t kDefaultPassSpp = 16;
 constexpr uint64_t kDefaultPassPaths = 1ull << 30;
-constexpr uint32_t kDefaultBvhThreshold = 1024;
+constexpr uint32_t kDefaultBvhThreshold = 512;   // fastest of 256-1024 on the 64-scene mix
 constexpr size_t kPassesInFlight = 2;                 // the one running and the next
 constexpr uint64_t kMinSlicePaths = 4ull << 20;       // a job's slice fills at least a few-Mi-path wave
 constexpr uint64_t kPinnedCacheBytes = 4ull << 30;    // result buffers kept for reuse

@@ -378,7 +378,7 @@ def run_batch_compare(args, dist: Dist):
     paths = sum(s.width * s.height * s.spp for s in mix)
 
     # plain: one renderer, one launch per scene
-    r = atx.Renderer(device=dev)
+    r = atx.Renderer(device=dev, bvh_threshold=args.bvh_threshold, bvh_leaf_size=args.bvh_leaf)
     stream = torch.cuda.ExternalStream(r.stream, device=dev)
     plain_ms = 0.0
     for rep in range(2):                       # rep 0 warms up (allocations, BVH builds)
@@ -396,12 +396,14 @@ def run_batch_compare(args, dist: Dist):
                 plain_ms += e0.elapsed_time(e1)
     r.close()
 
-    b = atx.Batch(device=dev)
+    b = atx.Batch(device=dev, bvh_threshold=args.bvh_threshold, bvh_leaf_size=args.bvh_leaf)
     if args.lanes or args.lane_wave:
         b.set_tuning(lanes=args.lanes, lane_wave_paths=args.lane_wave << 20)
     ids = [b.add_synthetic(sc) for sc in mix]
     for i, sc in zip(ids, mix):
         b.set_spp(i, sc.spp)
+    if args.autotune:
+        b.autotune()
     for _ in range(args.warmup):
         b.run()
     b.synchronize()
@@ -675,6 +677,7 @@ def main(argv=None) -> int:
     ap.add_argument("--max-pass-paths", type=int, default=0, help="serve mode: bound on paths per pass (0 = default)")
     ap.add_argument("--lanes", type=int, default=0, help="batch mode: concurrent lanes (0 = library default)")
     ap.add_argument("--max-pass-spp", type=int, default=0, help="batch mode: cap each scene's frames per pass")
+    ap.add_argument("--autotune", action="store_true", help="batch mode: pick lanes / path state by timing first")
     ap.add_argument("--lane-wave", type=int, default=0, help="batch mode: path state per lane, Mi paths")
     ap.add_argument("--width", type=int, default=0, help="render mode: override the viewport width")
     ap.add_argument("--height", type=int, default=0, help="render mode: override the viewport height")

@@ -142,3 +142,23 @@ def test_set_camera_restarts_accumulation():
         moved = scenes.SyntheticScene(**{**sc.__dict__, "camera_position": cam.position})
         ref, _ = alone(moved, 2)
         assert bit_mismatches(b.get_accumulation(i), ref) == 0
+
+
+def test_autotune_leaves_no_trace():
+    """Autotuning renders the scenes under several settings, then puts them back at frame 1: the
+    passes after it equal rendering each scene alone."""
+    mix = small_mix(4)
+    with Batch() as b:
+        ids = [b.add_synthetic(sc) for sc in mix]
+        for i, sc in zip(ids, mix):
+            b.set_spp(i, 2)
+        chosen = b.autotune(passes=1)
+        assert chosen["lanes"] in (4, 8, 16) and chosen["lane_wave_paths"] >= 8 << 20
+        assert all(b.frame_index(i) == 1 for i in ids)
+        b.run()
+        for i, sc in zip(ids, mix):
+            ref, _ = alone(sc, 2)
+            assert bit_mismatches(b.get_accumulation(i), ref) == 0
+        b.run()
+        with pytest.raises(Exception):
+            b.autotune()                       # scenes have rendered frames now

@@ -88,8 +88,8 @@ def N_bytes(sc):
     n = len(sc.spheres)
     px = sc.width * sc.height
     tables = 24 * n + 48 * len(sc.materials) + 32 * len(sc.lights) + 8 * 256
-    bvh = 200 * n if n >= 1024 else 0
-    return tables + bvh + 20 * px + 512
+    bvh = 200 * n if n >= 512 else 0
+    return tables + bvh + 28 * px + 512
 
 
 def test_camera_change_while_queued_and_while_active():
