@@ -130,7 +130,7 @@ private:
     // many streams with their own path state, so one range's last, sparse
     // bounces overlap the others' work instead of leaving SMs idle.  Lane 0
     // is the renderer's stream.
-    static constexpr int kLanes = 2;
+    static constexpr int kLanes = 4;
     WaveStore wave_[kLanes];
     cudaStream_t lane_stream_[kLanes] = {};
     cudaEvent_t fork_ = nullptr, join_[kLanes] = {};
