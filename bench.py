@@ -275,18 +275,21 @@ def run_ours(args, dist: Dist):
         "peak_source": "measured FFMA throughput (atx_measure_fp32_peak, this process); MEASURED_PEAKS.json "
                        "has no FP32 figure",
         "traffic": None,
-        "flop_per_launch": round(ext_flops / max(1, kt["extend_launches"])),
-        "avg_launch_ms": round(kt["extend_ms"] / max(1, kt["extend_launches"]), 4),
+        "launch": "one atx_render of the workload: all its k_primary and k_extend kernels",
+        "flop_per_launch": round(ext_flops / prof_steps),
+        "avg_launch_ms": round(kt["extend_ms"] / prof_steps, 4),
+        "kernel_launches_per_launch": round(kt["extend_launches"] / prof_steps, 1),
         "share_of_kernel_time": round(kt["extend_ms"] / total_kernel_ms, 4) if total_kernel_ms else None,
         "kernel_ms_per_step": {k: round(kt[k] / prof_steps, 3) for k in
                                ("extend_ms", "shadow_ms", "accumulate_ms", "other_ms")},
     }
-    traffic_file = ROOT / "profiles" / "k_extend_config1_traffic.json"
+    # DRAM bytes of the same kernels per atx_render, from an ncu capture summarised in profiles/
+    traffic_file = ROOT / "profiles" / "extension_traffic_medium_scene.txt"
     if traffic_file.exists():
-        try:
-            roofline["traffic"] = json.loads(traffic_file.read_text()).get("bytes_per_launch")
-        except ValueError:
-            pass
+        for line in traffic_file.read_text().splitlines():
+            if line.startswith("dram_bytes_per_launch:"):
+                roofline["traffic"] = int(line.split(":", 1)[1])
+                roofline["traffic_source"] = "profiles/extension_traffic_medium_scene.txt (ncu)"
 
     ref_kernel = None
     if dist.world == 1 and not args.no_ref_kernel:
