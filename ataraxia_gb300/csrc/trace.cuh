@@ -36,6 +36,47 @@ __device__ __forceinline__ float3 primary_dir(const CameraView& cam, uint32_t x,
     return normalize3(mk3(dv[0], dv[1], dv[2]));
 }
 
+// The shared-memory sphere table in pair layout: spheres 2j and 2j+1 share
+// the float4s at 2j and 2j+1, {-x0, -x1, -y0, -y1} and {-z0, -z1, -w0, -w1}
+// (w = r^2).  One packed f32x2 instruction then does an operation for both
+// spheres, with the same IEEE rounding per component as the scalar one, and
+// the negated centres let a packed add form o - c exactly (x + (-y) is x - y).
+// For an odd count the last pair repeats its sphere; its second half is never
+// a candidate (candidate_bits masks it).
+__device__ __forceinline__ void stage_spheres(const SceneView& sc, float4* s)
+{
+    const uint32_t n = sc.n_sph, np = (n + 1u) >> 1;
+    for (uint32_t j = threadIdx.x; j < np; j += blockDim.x) {
+        const float4 p = __ldg(&sc.sph[2u * j]);
+        const float4 q = 2u * j + 1u < n ? __ldg(&sc.sph[2u * j + 1u]) : p;
+        s[2u * j] = make_float4(-p.x, -q.x, -p.y, -q.y);
+        s[2u * j + 1u] = make_float4(-p.z, -q.z, -p.w, -q.w);
+    }
+    __syncthreads();
+}
+
+// Bytes of the pair-layout table for n spheres.
+__host__ __device__ constexpr size_t smem_table_bytes(uint32_t n)
+{
+    return (size_t)((n + 1u) & ~1u) * 16u;
+}
+
+// Sphere i (x, y, z, r^2) of the pair-layout table.
+__device__ __forceinline__ float4 smem_sphere(const float4* s, uint32_t i)
+{
+    const float4 p = s[i & ~1u], q = s[i | 1u];
+    const bool odd = (i & 1u) != 0u;
+    return make_float4(-(odd ? p.y : p.x), -(odd ? p.w : p.z), -(odd ? q.y : q.x), -(odd ? q.w : q.z));
+}
+
+// Sphere i of a kernel's table: the shared-memory pair layout or the plain
+// global array.
+template <bool SMEM>
+__device__ __forceinline__ float4 table_sphere(const float4* __restrict__ sph, uint32_t i)
+{
+    return SMEM ? smem_sphere(sph, i) : __ldg(&sph[i]);
+}
+
 // Candidate bits of up to 32 spheres starting at base.  A sphere can only be
 // accepted when its discriminant is >= 0 (else the reference skips it) and its
 // half-b term is < 0: with b >= 0 the root -(b + sqrt(disc)) / a is <= 0 and
@@ -46,15 +87,41 @@ __device__ __forceinline__ float3 primary_dir(const CameraView& cam, uint32_t x,
 // branches, which keeps the square root and the IEEE division out of the inner
 // loop.  Each sphere shifts its bit in from the right (one funnel shift), so
 // sphere base+k ends at bit 31-k: the highest set bit is the lowest index.
+// CNT is 32 for a full chunk, 31 for a partial one of cnt spheres.
 template <bool SMEM, int CNT>
 __device__ __forceinline__ uint32_t candidate_bits(const float4* __restrict__ sph, uint32_t base, float3 o, float3 d,
                                                    float a, uint32_t cnt)
 {
     uint32_t mask = 0u;
+    if (SMEM) {
+        // pair layout, base even: b, c and the discriminant of two spheres
+        // per packed instruction, in the order of the scalar branch below
+        const float2 ox = make_float2(o.x, o.x), oy = make_float2(o.y, o.y), oz = make_float2(o.z, o.z);
+        const float2 dx = make_float2(d.x, d.x), dy = make_float2(d.y, d.y), dz = make_float2(d.z, d.z);
+        const float2 na = make_float2(-a, -a);
+        const uint32_t np = CNT == 32 ? 16u : (cnt + 1u) >> 1;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            if (CNT == 32 || (uint32_t)k < np) {
+                const float4 p = sph[base + 2u * k], q = sph[base + 2u * k + 1u];
+                const float2 vx = __fadd2_rn(ox, make_float2(p.x, p.y));
+                const float2 vy = __fadd2_rn(oy, make_float2(p.z, p.w));
+                const float2 vz = __fadd2_rn(oz, make_float2(q.x, q.y));
+                const float2 b = __ffma2_rn(vz, dz, __ffma2_rn(vy, dy, __fmul2_rn(vx, dx)));
+                const float2 cc = __ffma2_rn(vz, vz, __ffma2_rn(vy, vy, __ffma2_rn(vx, vx, make_float2(q.z, q.w))));
+                const float2 disc = __ffma2_rn(b, b, __fmul2_rn(na, cc));
+                mask = __funnelshift_l(__float_as_uint(fmaxf(b.x, -disc.x)), mask, 1);
+                mask = __funnelshift_l(__float_as_uint(fmaxf(b.y, -disc.y)), mask, 1);
+            }
+        }
+        // align the first sphere to bit 31 and drop an odd count's repeat
+        if (CNT != 32) mask = (mask << (32u - 2u * np)) & ~(0xffffffffu >> cnt);
+        return mask;
+    }
 #pragma unroll
     for (int k = 0; k < CNT; ++k) {
         if (CNT == 32 || (uint32_t)k < cnt) {
-            const float4 s = SMEM ? sph[base + k] : __ldg(&sph[base + k]);
+            const float4 s = __ldg(&sph[base + k]);
             const float ox = o.x - s.x, oy = o.y - s.y, oz = o.z - s.z;
             const float b = __fmaf_rn(oz, d.z, __fmaf_rn(oy, d.y, ox * d.x));
             const float cc = __fmaf_rn(oz, oz, __fmaf_rn(oy, oy, __fmaf_rn(ox, ox, -s.w)));
@@ -83,7 +150,7 @@ __device__ __forceinline__ int32_t nearest_brute(const float4* __restrict__ sph,
             mask &= ~(0x80000000u >> k);
             const uint32_t i = base + k;
             float t;
-            if (sphere_t(SMEM ? sph[i] : __ldg(&sph[i]), o, d, a, t) && t > 0.0f && t < tm) {
+            if (sphere_t(table_sphere<SMEM>(sph, i), o, d, a, t) && t > 0.0f && t < tm) {
                 tm = t;
                 best = (int32_t)i;
             }
@@ -111,7 +178,7 @@ __device__ __forceinline__ bool occluded_brute(const float4* __restrict__ sph, u
             mask &= ~(0x80000000u >> k);
             const uint32_t i = base + k;
             float t;
-            if (sphere_t(SMEM ? sph[i] : __ldg(&sph[i]), o, d, a, t) && t > 0.0f && t * t < dist2) return true;
+            if (sphere_t(table_sphere<SMEM>(sph, i), o, d, a, t) && t > 0.0f && t * t < dist2) return true;
         }
     }
     return false;
@@ -132,12 +199,5 @@ __device__ __forceinline__ bool scene_occluded(const SceneView& sc, const float4
     if (IS == kIsBvh) return bvh_occluded(sc, o, d, dist2);
     return occluded_brute<IS == kIsSmem>(sph, sc.n_sph, o, d, dist2);
 }
-
-__device__ __forceinline__ void stage_spheres(const SceneView& sc, float4* s_sph)
-{
-    for (uint32_t i = threadIdx.x; i < sc.n_sph; i += blockDim.x) s_sph[i] = __ldg(&sc.sph[i]);
-    __syncthreads();
-}
-
 
 }  // namespace atx

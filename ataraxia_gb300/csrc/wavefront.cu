@@ -30,11 +30,11 @@ namespace {
 
 constexpr uint32_t kFull = 0xffffffffu;
 constexpr int kThreads = 256;
-// k_extend's block: its shading code sets the register count.  6 blocks of
-// 192 threads per SM (56 registers, 56% occupancy) beat 4 of 256 (64
-// registers, 50%) by 0.8% on the medium scene.
-constexpr int kExtendThreads = 192;
-constexpr int kExtendBlocksPerSm = 6;
+// k_extend's block: its shading code sets the register count.  4 blocks of
+// 256 threads per SM (64 registers, no spills in the shared-memory variant)
+// beat 6 of 192 (56 registers, 44 bytes spilled) by 0.6% on the medium scene.
+constexpr int kExtendThreads = 256;
+constexpr int kExtendBlocksPerSm = 4;
 
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
                     touch = true;
                 }
             } else {
-                const float4 s = SMEM ? sph[hit] : __ldg(&sc.sph[hit]);
+                const float4 s = table_sphere<SMEM>(sph, (uint32_t)hit);
                 float3 pos, nrm;
                 ray_hit(s, o, d, tmin, pos, nrm);
                 const int32_t mi = __ldg(&sc.sph_mat[hit]);
@@ -243,7 +243,7 @@ __device__ __forceinline__ bool own_occludes(const SceneView& sc, const float4* 
                                              float3 o, float3 d, float dist2)
 {
     if (own >= sc.n_sph) return false;
-    const float4 s = smem ? sph[own] : __ldg(&sc.sph[own]);
+    const float4 s = smem ? smem_sphere(sph, own) : __ldg(&sc.sph[own]);
     float t;
     return sphere_t(s, o, d, dot3(d, d), t) && t > 0.0f && t * t < dist2;
 }
@@ -260,8 +260,13 @@ __device__ __forceinline__ void shadow_light(const WaveState& ws, uint32_t idx, 
     ws.col[pid] = col;
 }
 
+// k_shadow's blocks per SM: the shared-memory variant fits 40 registers
+// without spilling (6 blocks of 256 threads); the others take up to 64 (4).
 template <int IS>
-__global__ void __launch_bounds__(kThreads) k_shadow(SceneView sc, WaveState ws, int bounce)
+constexpr int kShadowBlocksPerSm = IS == kIsSmem ? 6 : 4;
+
+template <int IS>
+__global__ void __launch_bounds__(kThreads, kShadowBlocksPerSm<IS>) k_shadow(SceneView sc, WaveState ws, int bounce)
 {
     constexpr bool SMEM = IS == kIsSmem;
     extern __shared__ float4 s_sph[];
@@ -333,7 +338,7 @@ __global__ void __launch_bounds__(kThreads) k_shadow(SceneView sc, WaveState ws,
                 const uint32_t k = (uint32_t)__clz(mask);
                 mask &= ~(0x80000000u >> k);
                 float t;
-                if (sphere_t(SMEM ? sph[base + k] : __ldg(&sph[base + k]), o, d, a, t) && t > 0.0f &&
+                if (sphere_t(table_sphere<SMEM>(sph, base + k), o, d, a, t) && t > 0.0f &&
                     t * t < dist2) {
                     hit = true;
                     break;
@@ -427,7 +432,7 @@ constexpr size_t kSmemSphereCap = 96 * 1024;  // 6144 spheres staged per CTA
 int isect_mode(const SceneView& sc)
 {
     if (sc.use_bvh) return kIsBvh;
-    if (sc.n_sph > 0 && (size_t)sc.n_sph * sizeof(float4) <= kSmemSphereCap) return kIsSmem;
+    if (sc.n_sph > 0 && smem_table_bytes(sc.n_sph) <= kSmemSphereCap) return kIsSmem;
     return kIsGlobal;
 }
 
@@ -475,7 +480,7 @@ cudaError_t plan_launch(const SceneView& sc, int device, int threads, LaunchShap
     cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) return e;
     const int mode = isect_mode(sc);
-    const size_t bytes = mode == kIsSmem ? (size_t)sc.n_sph * sizeof(float4) : 0;
+    const size_t bytes = mode == kIsSmem ? smem_table_bytes(sc.n_sph) : 0;
     int ext = 0, sh = 0, pr = 0;
     with_mode(mode, [&](auto m) { e = occupancy<decltype(m)::value>(threads, bytes, &ext, &sh, &pr); });
     if (e != cudaSuccess) return e;
@@ -555,7 +560,7 @@ cudaError_t enqueue_trace_nearest(const SceneView& sc, const float* origins, con
     if (n == 0) return cudaSuccess;
     const int g = grid_for(n, kThreads, 4096);
     const int mode = isect_mode(sc);
-    const size_t bytes = mode == kIsSmem ? (size_t)sc.n_sph * sizeof(float4) : 0;
+    const size_t bytes = mode == kIsSmem ? smem_table_bytes(sc.n_sph) : 0;
     cudaError_t e = cudaSuccess;
     with_mode(mode, [&](auto m) {
         constexpr int IS = decltype(m)::value;
