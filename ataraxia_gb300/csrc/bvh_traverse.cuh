@@ -52,10 +52,11 @@ __device__ __forceinline__ float3 safe_inv(float3 d)
     return mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
 }
 
-// Candidate bits of the leaf cluster [first, first + cnt) (cnt <= 32): bit k
-// set unless sphere first + k certainly misses, with the brute-force loop's
-// filter and arithmetic (trace.cuh candidate_bits), so candidates are decided
-// by the same exact test.
+// Candidate bits of the leaf cluster [first, first + cnt) (1 <= cnt <= 32):
+// bit k set unless sphere first + k certainly misses, with the brute-force
+// loop's filter and arithmetic (trace.cuh candidate_bits: the sign of
+// h = fma(b, -|b|, -(a*c)), clear for every sphere the exact test can
+// accept), so candidates are decided by the same exact test.
 __device__ __forceinline__ uint32_t leaf_candidates(const BvhView& b, uint32_t first, uint32_t cnt, float3 o,
                                                     float3 d, float a)
 {
@@ -65,10 +66,10 @@ __device__ __forceinline__ uint32_t leaf_candidates(const BvhView& b, uint32_t f
         const float ox = o.x - s.x, oy = o.y - s.y, oz = o.z - s.z;
         const float bb = __fmaf_rn(oz, d.z, __fmaf_rn(oy, d.y, ox * d.x));
         const float cc = __fmaf_rn(oz, oz, __fmaf_rn(oy, oy, __fmaf_rn(ox, ox, -s.w)));
-        const float disc = __fmaf_rn(bb, bb, -(a * cc));
-        mask |= (__float_as_uint(fmaxf(bb, -disc)) >> 31) << k;
+        const float h = __fmaf_rn(bb, -fabsf(bb), -(a * cc));
+        mask = __funnelshift_l(__float_as_uint(h), mask, 1);   // sphere k at bit cnt-1-k
     }
-    return mask;
+    return __brev(~mask << (32u - cnt));   // sphere k at bit k
 }
 
 __device__ __forceinline__ void leaf_nearest(const BvhView& b, uint32_t first, uint32_t cnt, float3 o, float3 d,

@@ -77,15 +77,19 @@ __device__ __forceinline__ float4 table_sphere(const float4* __restrict__ sph, u
     return SMEM ? smem_sphere(sph, i) : __ldg(&sph[i]);
 }
 
-// Candidate bits of up to 32 spheres starting at base.  A sphere can only be
-// accepted when its discriminant is >= 0 (else the reference skips it) and its
-// half-b term is < 0: with b >= 0 the root -(b + sqrt(disc)) / a is <= 0 and
-// fails t > 0.  The bit is the sign of max(b, -disc), a superset of those
-// cases (disc is never -0, being b*b - a*c with b*b >= +0; max(b, -disc) = +0
-// only when b = +0, which is never accepted); candidates are then decided by
-// the exact test, so results equal the plain loop's.  The cheap pass has no
-// branches, which keeps the square root and the IEEE division out of the inner
-// loop.  Each sphere shifts its bit in from the right (one funnel shift), so
+// Candidate bits of up to 32 spheres starting at base.  The exact test
+// (sphere_t) accepts a sphere only when its discriminant disc = b*b - a*c is
+// >= 0 and its half-b term b is < 0: with b >= 0 the root -(b + sqrt(disc))/a
+// is <= 0 and fails t > 0.  The filter computes h = fma(b, -|b|, -(a*c)) and
+// marks a sphere when h's sign bit is clear.  For b < 0, -|b| = b, so h is the
+// exact test's discriminant (same operations, same rounding) and the sphere is
+// marked exactly when disc >= 0, +0 included.  For b >= 0, h = -b*b - a*c,
+// marked only when c <= 0 (origin inside or on the sphere): a few extra
+// candidates, which the exact test then rejects.  So candidates are a
+// superset of the accepted spheres and results equal the plain loop's.  The
+// cheap pass has no branches, which keeps the square root and the IEEE
+// division out of the inner loop.  Each sphere shifts h's sign bit in from the
+// right (one funnel shift) and the word is inverted once at the end, so
 // sphere base+k ends at bit 31-k: the highest set bit is the lowest index.
 // CNT is 32 for a full chunk, 31 for a partial one of cnt spheres.
 template <bool SMEM, int CNT>
@@ -94,8 +98,8 @@ __device__ __forceinline__ uint32_t candidate_bits(const float4* __restrict__ sp
 {
     uint32_t mask = 0u;
     if (SMEM) {
-        // pair layout, base even: b, c and the discriminant of two spheres
-        // per packed instruction, in the order of the scalar branch below
+        // pair layout, base even: b, c and h of two spheres per packed
+        // instruction, in the order of the scalar branch below
         const float2 ox = make_float2(o.x, o.x), oy = make_float2(o.y, o.y), oz = make_float2(o.z, o.z);
         const float2 dx = make_float2(d.x, d.x), dy = make_float2(d.y, d.y), dz = make_float2(d.z, d.z);
         const float2 na = make_float2(-a, -a);
@@ -109,11 +113,12 @@ __device__ __forceinline__ uint32_t candidate_bits(const float4* __restrict__ sp
                 const float2 vz = __fadd2_rn(oz, make_float2(q.x, q.y));
                 const float2 b = __ffma2_rn(vz, dz, __ffma2_rn(vy, dy, __fmul2_rn(vx, dx)));
                 const float2 cc = __ffma2_rn(vz, vz, __ffma2_rn(vy, vy, __ffma2_rn(vx, vx, make_float2(q.z, q.w))));
-                const float2 disc = __ffma2_rn(b, b, __fmul2_rn(na, cc));
-                mask = __funnelshift_l(__float_as_uint(fmaxf(b.x, -disc.x)), mask, 1);
-                mask = __funnelshift_l(__float_as_uint(fmaxf(b.y, -disc.y)), mask, 1);
+                const float2 h = __ffma2_rn(b, make_float2(-fabsf(b.x), -fabsf(b.y)), __fmul2_rn(na, cc));
+                mask = __funnelshift_l(__float_as_uint(h.x), mask, 1);
+                mask = __funnelshift_l(__float_as_uint(h.y), mask, 1);
             }
         }
+        mask = ~mask;
         // align the first sphere to bit 31 and drop an odd count's repeat
         if (CNT != 32) mask = (mask << (32u - 2u * np)) & ~(0xffffffffu >> cnt);
         return mask;
@@ -125,10 +130,11 @@ __device__ __forceinline__ uint32_t candidate_bits(const float4* __restrict__ sp
             const float ox = o.x - s.x, oy = o.y - s.y, oz = o.z - s.z;
             const float b = __fmaf_rn(oz, d.z, __fmaf_rn(oy, d.y, ox * d.x));
             const float cc = __fmaf_rn(oz, oz, __fmaf_rn(oy, oy, __fmaf_rn(ox, ox, -s.w)));
-            const float disc = __fmaf_rn(b, b, -(a * cc));
-            mask = __funnelshift_l(__float_as_uint(fmaxf(b, -disc)), mask, 1);
+            const float h = __fmaf_rn(b, -fabsf(b), -(a * cc));
+            mask = __funnelshift_l(__float_as_uint(h), mask, 1);
         }
     }
+    mask = ~mask;
     if (CNT != 32) mask <<= (32u - cnt);   // align the first sphere to bit 31
     return mask;
 }
