@@ -139,8 +139,7 @@ extern "C" ATX_API atx_status atx_render_noalloc(const atx_sphere* spheres, uint
     DevLight* lts = reinterpret_cast<DevLight*>(take((uint64_t)kMaxLights * sizeof(DevLight)));
     uint32_t* counters = reinterpret_cast<uint32_t*>(take(wave_counter_words(kMaxBounces) * sizeof(uint32_t)));
     const uint64_t used = (uint64_t)(p - base);
-    const uint64_t per_path = 7 * sizeof(float4) + 3 * sizeof(uint32_t) + sizeof(uint2);
-    const uint32_t capacity = (uint32_t)((kScratchBytes - used - 13 * 256) / per_path);
+    const uint32_t capacity = (uint32_t)((kScratchBytes - used - (kWaveArrays + 1) * 256) / kWaveBytesPerPath);
     WaveState ws{};
     ws.ray_o = reinterpret_cast<float4*>(take((uint64_t)capacity * sizeof(float4)));
     ws.ray_d = reinterpret_cast<float4*>(take((uint64_t)capacity * sizeof(float4)));
@@ -153,6 +152,7 @@ extern "C" ATX_API atx_status atx_render_noalloc(const atx_sphere* spheres, uint
     ws.q[1] = reinterpret_cast<uint32_t*>(take((uint64_t)capacity * sizeof(uint32_t)));
     ws.prim = reinterpret_cast<uint2*>(take((uint64_t)capacity * sizeof(uint2)));
     ws.hitq = reinterpret_cast<uint32_t*>(take((uint64_t)capacity * sizeof(uint32_t)));
+    ws.vis = reinterpret_cast<uint32_t*>(take((uint64_t)capacity * sizeof(uint32_t)));
     ws.counters = counters;
     ws.totals = nullptr;
     ws.capacity = capacity;

@@ -101,8 +101,8 @@ atx_status SceneStore::upload(const atx_sphere* s, uint32_t n, const atx_materia
 uint64_t WaveStore::bytes_for(uint32_t capacity, uint32_t max_bounces)
 {
     const uint64_t c = capacity;
-    return c * (7 * sizeof(float4) + 3 * sizeof(uint32_t) + sizeof(uint2)) +
-           wave_counter_words((int)max_bounces) * sizeof(uint32_t) + 16 + 13 * 256;
+    return c * kWaveBytesPerPath + wave_counter_words((int)max_bounces) * sizeof(uint32_t) + 16 +
+           (kWaveArrays + 1) * 256;
 }
 
 atx_status WaveStore::ensure(uint32_t capacity, uint32_t max_bounces, Budget* budget)
@@ -130,6 +130,7 @@ atx_status WaveStore::ensure(uint32_t capacity, uint32_t max_bounces, Budget* bu
     view.q[1] = reinterpret_cast<uint32_t*>(take(c * sizeof(uint32_t)));
     view.prim = reinterpret_cast<uint2*>(take(c * sizeof(uint2)));
     view.hitq = reinterpret_cast<uint32_t*>(take(c * sizeof(uint32_t)));
+    view.vis = reinterpret_cast<uint32_t*>(take(c * sizeof(uint32_t)));
     view.counters = reinterpret_cast<uint32_t*>(take(wave_counter_words((int)b) * sizeof(uint32_t)));
     view.capacity = cap;
     bounces = b;

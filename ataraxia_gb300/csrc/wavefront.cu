@@ -53,7 +53,24 @@ __device__ __forceinline__ uint32_t warp_push(uint32_t* counter, bool pred)
     return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
 }
 
+// Renderer.cu:339-348: light li's parameter row, the unit direction L from pos
+// to the light and the squared distance.  One function for the first bounce
+// and the per-(pixel, light) shadow rays, so both compute the same floats.
+__device__ __forceinline__ float4 light_dir(const SceneView& sc, uint32_t li, float3 pos, float3& L, float& dist2)
+{
+    const float4* lrow = reinterpret_cast<const float4*>(sc.lights + li);
+    const float4 l0 = __ldg(lrow), l1 = __ldg(lrow + 1);
+    L = sub3(mk3(l0.x, l0.y, l0.z), pos);
+    dist2 = dot3(L, L);
+    L = muls3(L, 1.0f / sqrtf(dist2));
+    return l1;
+}
+
 // Primary nearest hit once per pixel of the wave (shared by its samples).
+// With per-(pixel, light) shadow rays (wave_light_vis) it also clears the
+// pixel's visibility word and queues, as bounce 0's shadow rays, one ray per
+// distinct light its samples pick (record: origin and squared distance, L and
+// the wave pixel, the light index and the hit sphere).
 template <int IS>
 __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView cam, WaveState ws, WaveJob job)
 {
@@ -68,16 +85,21 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t* hits = &ws.counters[2 * ((uint32_t)job.max_bounces + 1u)];
     uint2* prim = job.prim_cache ? job.prim_cache + job.pixel0 : ws.prim;
+    const bool vis = wave_light_vis(job, sc.n_lights);   // uniform
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {   // warp-uniform trip count
         const uint32_t j = base + threadIdx.x;
         int32_t id = -1;
+        float t = 0.0f;
+        float3 d = o;
         if (j < n) {
+            const uint32_t p = job.pixel0 + j;
             if (cached) {
-                id = (int32_t)prim[j].y;
+                const uint2 pr = prim[j];
+                id = (int32_t)pr.y;
+                t = __uint_as_float(pr.x);
+                if (vis && id >= 0) d = primary_dir(cam, p % cam.width, p / cam.width);
             } else {
-                const uint32_t p = job.pixel0 + j;
-                const float3 d = primary_dir(cam, p % cam.width, p / cam.width);
-                float t;
+                d = primary_dir(cam, p % cam.width, p / cam.width);
                 id = scene_nearest<IS>(sc, sph, o, d, t);
                 prim[j] = make_uint2(__float_as_uint(t), (uint32_t)id);
             }
@@ -86,6 +108,31 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
         // samples are closed-form (accumulated by k_accumulate)
         const uint32_t slot = warp_push(hits, id >= 0);
         if (id >= 0) ws.hitq[slot] = j;
+        if (!vis) continue;
+
+        uint32_t lights = 0u;   // distinct lights the pixel's samples pick (Renderer.cu:339)
+        float3 pos = o, nrm = o;
+        if (j < n) ws.vis[j] = 0u;
+        if (id >= 0) {
+            ray_hit(__ldg(&sc.sph[id]), o, d, t, pos, nrm);
+            const uint32_t p = job.pixel0 + j;
+            for (uint32_t s = 0; s < job.spp; ++s) lights |= 1u << (pcg_hash(p * (job.frame0 + s)) % sc.n_lights);
+        }
+        const float3 so = add3(pos, muls3(nrm, kOffset));
+        while (__any_sync(kFull, lights != 0u)) {
+            const bool has = lights != 0u;
+            const uint32_t li = has ? (uint32_t)(__ffs(lights) - 1) : 0u;
+            lights &= lights - 1u;
+            const uint32_t ss = warp_push(&ws.counters[1], has);
+            if (has) {
+                float3 L;
+                float dist2;
+                light_dir(sc, li, pos, L, dist2);
+                ws.sh_o[ss] = make_float4(so.x, so.y, so.z, dist2);
+                ws.sh_d[ss] = make_float4(L.x, L.y, L.z, __uint_as_float(j));
+                ws.sh_c[ss] = make_float4(__uint_as_float(li), 0.0f, 0.0f, __uint_as_float((uint32_t)id));
+            }
+        }
     }
 }
 
@@ -110,18 +157,21 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
     uint32_t* qout = (bounce & 1) ? ws.q[0] : ws.q[1];
     const bool last = bounce + 1 >= job.max_bounces;
     const uint32_t stride = gridDim.x * blockDim.x;
+    // first bounce with per-(pixel, light) shadow rays: the light of a sample
+    // is added here when k_shadow found it visible from the pixel's hit
+    const bool vis = FIRST && SHARED && wave_light_vis(job, sc.n_lights);
 
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t idx = base + threadIdx.x;
-        bool push_next = false, push_sh = false;
-        uint32_t pid = 0u, seed = 0u;
-        float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o;
+        bool push_next = false, push_sh = false, lit = false;
+        uint32_t pid = 0u, seed = 0u, j = 0u;
+        float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o, lc = o;
         float4 sho = make_float4(0.f, 0.f, 0.f, 0.f), shd = sho, shc = sho;
 
         if (idx < n) {
             if (FIRST) {
                 // SHARED: idx enumerates (hit pixel, sample); path ids stay pixel-major
-                const uint32_t j = SHARED ? ws.hitq[idx / job.spp] : idx / job.spp;
+                j = SHARED ? ws.hitq[idx / job.spp] : idx / job.spp;
                 const uint32_t s = idx % job.spp;
                 pid = j * job.spp + s;
                 const uint32_t p = job.pixel0 + j;
@@ -178,19 +228,22 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
 
                 if (sc.n_lights > 0u) {  // Renderer.cu:338-369
                     const uint32_t li = pcg_hash(seed) % sc.n_lights;
-                    const float4* lrow = reinterpret_cast<const float4*>(sc.lights + li);
-                    const float4 l0 = __ldg(lrow), l1 = __ldg(lrow + 1);
-                    float3 L = sub3(mk3(l0.x, l0.y, l0.z), pos);
-                    const float dist2 = dot3(L, L);
-                    L = muls3(L, 1.0f / sqrtf(dist2));
-                    const float3 so = add3(pos, muls3(nrm, kOffset));
+                    float3 L;
+                    float dist2;
+                    const float4 l1 = light_dir(sc, li, pos, L, dist2);
                     const float3 f = cook_torrance(albedo, base, metallic, rough, nrm, neg3(d), L);
                     const float3 c = mul3(mul3(mk3(l1.x, l1.y, l1.z), f), thr);
-                    sho = make_float4(so.x, so.y, so.z, dist2);
-                    shd = make_float4(L.x, L.y, L.z, __uint_as_float(pid));
-                    // w: the sphere the shadow ray leaves from, tested first by k_shadow
-                    shc = make_float4(c.x, c.y, c.z, __uint_as_float((uint32_t)hit));
-                    push_sh = true;
+                    if (vis) {
+                        lit = ((ws.vis[j] >> li) & 1u) != 0u;
+                        lc = c;
+                    } else {
+                        const float3 so = add3(pos, muls3(nrm, kOffset));
+                        sho = make_float4(so.x, so.y, so.z, dist2);
+                        shd = make_float4(L.x, L.y, L.z, __uint_as_float(pid));
+                        // w: the sphere the shadow ray leaves from, tested first by k_shadow
+                        shc = make_float4(c.x, c.y, c.z, __uint_as_float((uint32_t)hit));
+                        push_sh = true;
+                    }
                 }
 
                 if (!last) {  // Renderer.cu:371-384
@@ -205,7 +258,8 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
                 }
             }
             if (FIRST) {
-                const float3 c = add3(mk3(0.f, 0.f, 0.f), add);
+                float3 c = add3(mk3(0.f, 0.f, 0.f), add);
+                if (lit) c = add3(c, lc);   // as k_shadow adds it: after the emission
                 ws.col[pid] = make_float4(c.x, c.y, c.z, 0.0f);
             } else if (touch) {
                 float4 c = ws.col[pid];
@@ -248,9 +302,15 @@ __device__ __forceinline__ bool own_occludes(const SceneView& sc, const float4* 
     return sphere_t(s, o, d, dot3(d, d), t) && t > 0.0f && t * t < dist2;
 }
 
-// Adds the light a shadow ray carries to its path (Renderer.cu:356-368).
+// Adds the light a shadow ray carries to its path (Renderer.cu:356-368), or,
+// for a per-(pixel, light) ray (VIS), marks the light visible from the pixel.
+template <bool VIS>
 __device__ __forceinline__ void shadow_light(const WaveState& ws, uint32_t idx, float4 sd)
 {
+    if (VIS) {
+        atomicOr(&ws.vis[__float_as_uint(sd.w)], 1u << __float_as_uint(ws.sh_c[idx].x));
+        return;
+    }
     const float4 c = ws.sh_c[idx];
     const uint32_t pid = __float_as_uint(sd.w);
     float4 col = ws.col[pid];
@@ -265,7 +325,7 @@ __device__ __forceinline__ void shadow_light(const WaveState& ws, uint32_t idx, 
 template <int IS>
 constexpr int kShadowBlocksPerSm = IS == kIsSmem ? 6 : 4;
 
-template <int IS>
+template <int IS, bool VIS>
 __global__ void __launch_bounds__(kThreads, kShadowBlocksPerSm<IS>) k_shadow(SceneView sc, WaveState ws, int bounce)
 {
     constexpr bool SMEM = IS == kIsSmem;
@@ -284,7 +344,7 @@ __global__ void __launch_bounds__(kThreads, kShadowBlocksPerSm<IS>) k_shadow(Sce
             const float3 o = mk3(so.x, so.y, so.z), d = mk3(sd.x, sd.y, sd.z);
             if (!own_occludes(sc, sph, SMEM, __float_as_uint(ws.sh_c[idx].w), o, d, so.w) &&
                 !scene_occluded<IS>(sc, sph, o, d, so.w))
-                shadow_light(ws, idx, sd);
+                shadow_light<VIS>(ws, idx, sd);
         }
         return;
     }
@@ -345,7 +405,7 @@ __global__ void __launch_bounds__(kThreads, kShadowBlocksPerSm<IS>) k_shadow(Sce
                 }
             }
             if (hit || --left == 0u) {
-                if (!hit) shadow_light(ws, idx, sd);   // Renderer.cu:353-369: unoccluded
+                if (!hit) shadow_light<VIS>(ws, idx, sd);   // Renderer.cu:353-369: unoccluded
                 live = false;
             }
         }
@@ -461,12 +521,13 @@ cudaError_t occupancy(int threads, size_t bytes, int* ext, int* sh, int* pr)
         cudaError_t e = cudaFuncSetAttribute(k_extend<true, IS, false>, a, b);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_extend<false, IS, false>, a, b);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_primary<IS>, a, b);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shadow<IS>, a, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shadow<IS, false>, a, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shadow<IS, true>, a, b);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace<IS>, a, b);
         if (e != cudaSuccess) return e;
     }
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ext, k_extend<false, IS, false>, kExtendThreads, bytes);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(sh, k_shadow<IS>, threads, bytes);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(sh, k_shadow<IS, false>, threads, bytes);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(pr, k_primary<IS>, threads, bytes);
     return e;
 }
@@ -508,6 +569,7 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
         if (e != cudaSuccess) return e;
         const int g0 = grid_for(paths, kExtendThreads, shape.blocks_extend);
         const bool share = wave_shares_primary(job);
+        const bool vis = wave_light_vis(job, sc.n_lights);
         with_mode(shape.mode, [&](auto m) {
             constexpr int IS = decltype(m)::value;
             if (share) {
@@ -516,6 +578,12 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
                 k_primary<IS><<<gp, shape.threads, sm, stream>>>(sc, cam, ws, job);
                 end(kFamExtend);
                 ++nl;
+                if (vis) {   // bounce 0's shadow rays, one per (pixel, light), before the shading
+                    begin(kFamShadow);
+                    k_shadow<IS, true><<<shape.blocks_shadow, shape.threads, sm, stream>>>(sc, ws, 0);
+                    end(kFamShadow);
+                    ++nl;
+                }
                 // no sphere table needed: the nearest hit comes from k_primary
                 begin(kFamExtend);
                 k_extend<true, kIsGlobal, true><<<g0, kExtendThreads, 0, stream>>>(sc, cam, ws, job, 0);
@@ -533,8 +601,9 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
                     end(kFamExtend);
                     ++nl;
                 }
+                if (vis && b == 0) continue;
                 begin(kFamShadow);
-                k_shadow<IS><<<shape.blocks_shadow, shape.threads, sm, stream>>>(sc, ws, b);
+                k_shadow<IS, false><<<shape.blocks_shadow, shape.threads, sm, stream>>>(sc, ws, b);
                 end(kFamShadow);
                 ++nl;
             }

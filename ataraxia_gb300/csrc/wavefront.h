@@ -95,8 +95,15 @@ struct WaveState {
     unsigned long long* totals;   // [0] extension rays after bounce 0, [1] shadow rays (running sums)
     uint2* prim;                  // per pixel of the wave: primary hit (t bits, sphere id), shared by its samples
     uint32_t* hitq;               // wave pixels whose primary ray hits (only those get first-bounce paths)
+    uint32_t* vis;                // per pixel of the wave: bit l set when light l is visible from the primary hit
     uint32_t capacity;
 };
+
+// Path state per path slot: ray_o, ray_d, thr, col, sh_o, sh_d, sh_c (float4),
+// q[0], q[1], hitq, vis (uint32) and prim (uint2); kWaveArrays arrays, each
+// aligned to 256 bytes.
+constexpr uint64_t kWaveBytesPerPath = 7 * 16 + 4 * 4 + 8;
+constexpr uint64_t kWaveArrays = 12;
 
 // Counter slots after the per-bounce pairs: [2*(max_bounces+1)] = hit pixels.
 inline size_t wave_counter_words(int max_bounces) { return 2 * ((size_t)(max_bounces > 0 ? max_bounces : 0) + 1) + 2; }
@@ -125,6 +132,18 @@ struct WaveJob {
 __host__ __device__ inline bool wave_shares_primary(const WaveJob& j)
 {
     return j.max_bounces > 0 && (j.spp > 1 || j.prim_cache != nullptr);
+}
+
+// Whether the first bounce's shadow rays are traced once per (pixel, light)
+// instead of once per sample.  A pixel's samples share the primary hit, so
+// samples that pick the same light (Renderer.cu:339, PcgHash(seed) % lights)
+// cast the same shadow ray: k_primary queues one ray per distinct light the
+// pixel's samples pick, k_shadow records the visible ones in ws.vis, and the
+// first bounce adds the light of a sample whose light is visible.  Needs the
+// light set to fit one 32-bit word.
+__host__ __device__ inline bool wave_light_vis(const WaveJob& j, uint32_t n_lights)
+{
+    return wave_shares_primary(j) && n_lights > 0u && n_lights <= 32u;
 }
 
 // Kernel families timed by KernelTimer.

@@ -155,6 +155,23 @@ def test_sky_light_and_emission(po):
     assert bit_mismatches(acc, ref) == 0
 
 
+@pytest.mark.parametrize("n_lights,spp", [(32, 8), (33, 8), (5, 1), (31, 40)])
+def test_first_bounce_light_visibility_per_pixel(po, n_lights, spp):
+    # up to 32 lights a pixel's samples share one shadow ray per distinct light
+    # at the first bounce; above that every sample casts its own
+    sc = scenes.config1().with_resolution(72, 40)
+    rng = np.random.default_rng(n_lights)
+    lights = np.zeros(n_lights, dtype=scenes.LIGHT_DTYPE)
+    lights["position"] = rng.normal(0.0, 25.0, (n_lights, 3))
+    lights["color"] = rng.uniform(0.5, 1.0, (n_lights, 3))
+    lights["intensity"] = rng.uniform(20.0, 200.0, n_lights)
+    sc = scenes.SyntheticScene(**{**sc.__dict__, "lights": lights})
+    acc, img = gpu_render(sc, spp)
+    ref, _, _ = oracle_render(sc, spp)
+    assert bit_mismatches(acc, ref) == 0
+    assert np.array_equal(img, po.pack_rgba8(ref, spp))
+
+
 def test_empty_scene_no_lights_and_bad_material_ids(po):
     sc = scenes.config0().with_resolution(40, 20)
     empty = scenes.SyntheticScene(**{**sc.__dict__, "spheres": sc.spheres[:0]})
