@@ -7,6 +7,7 @@
 #include <cstring>
 
 #include "lbvh.h"
+#include "light_buffer.h"
 
 namespace atx {
 
@@ -24,7 +25,7 @@ atx_status SceneStore::upload(const atx_sphere* s, uint32_t n, const atx_materia
 {
     if ((n && !s) || (nm && !m) || (nl && !l)) return fail(ATX_ERR_INVALID_ARG, "set_scene: null array");
     if (n > 0 && nm == 0) return fail(ATX_ERR_INVALID_ARG, "set_scene: spheres need at least one material");
-    for (DeviceBuffer* b : {&this->sph, &sph_mat, &sph_rad, &mat, &lights, &bvh}) b->use_stream_order(order);
+    for (DeviceBuffer* b : {&this->sph, &sph_mat, &sph_rad, &mat, &lights, &bvh, &lbuf}) b->use_stream_order(order);
 
     std::vector<float4> sph(n);
     std::vector<int32_t> smat(n);
@@ -91,6 +92,15 @@ atx_status SceneStore::upload(const atx_sphere* s, uint32_t n, const atx_materia
         view.use_bvh = 1;
     } else {
         bvh.reset();
+    }
+    // light buffer for the shadow rays of the brute-force tables
+    if (!view.use_bvh && n >= 1 && n <= kLbMaxSpheres && nl >= 1 && nl <= kLbMaxLights) {
+        ATX_TRY(lbuf.ensure(lb_bytes(nl), budget, "light buffer"));
+        LightBufferView lv{};
+        ATX_CUDA(lb_build(view.sph, sph_rad.as<float>(), n, view.lights, nl, lbuf.get(), lbuf.bytes(), &lv, stream));
+        view.lb = lv;
+    } else {
+        lbuf.reset();
     }
     ATX_CUDA(cudaStreamSynchronize(stream));
     return ATX_OK;

@@ -190,6 +190,196 @@ __device__ __forceinline__ bool occluded_brute(const float4* __restrict__ sph, u
     return false;
 }
 
+// ------------------------------------------------------------- warp cones
+//
+// Rays of one warp that leave one apex in a narrow cone of directions: the
+// primary rays of 32 neighbouring pixels (apex: the camera), and the
+// first-bounce shadow rays of neighbouring hit points towards one light, seen
+// from the light.  The warp tests every sphere once against the cone of its
+// active lanes' directions and the lanes run the exact test only on the
+// spheres that pass, in index order; results equal the brute-force loop's.
+//
+// Exactness.  A sphere the float test accepts for a ray from o is passed by
+// the exact ray within r + 4 sqrt(eps) D of its centre, D = |o - c|, at a ray
+// parameter above -4.5 sqrt(eps) D (the bound the LBVH walk uses, bvh_traverse
+// .cuh).  The cone test inflates the radius by m = kBvhK (D + 1e-3) >=
+// 5 sqrt(eps) (D + 1e-3), plus an absolute e for shadow rays (their 1e-4
+// surface offset bends the segment from the light), and passes a sphere whose
+// inflated ball meets the cone, or whose centre lies within R + m of the apex
+// (an acceptance just behind the apex).  Every bound below errs towards
+// passing: cos of the half-angle from below, sines from above, a relative
+// 1e-5 slack on the final comparison.
+struct WarpCone {
+    float3 u;       // unit axis
+    float cos_lo;   // <= cos(half-angle)
+    float sin_hi;   // >= sin(half-angle)
+};
+
+// The cone of the unit directions w of the lanes with me set (at least one).
+// All 32 lanes call it; the butterfly sums and minimum leave the same bits on
+// every lane, so the result is warp-uniform.  False when the cone is too
+// wide to pay (cos(half-angle) below 0.5) or a direction is not finite.
+__device__ __forceinline__ bool warp_cone(bool me, float3 w, WarpCone& c)
+{
+    float sx = me ? w.x : 0.0f, sy = me ? w.y : 0.0f, sz = me ? w.z : 0.0f;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, off);
+        sy += __shfl_xor_sync(0xffffffffu, sy, off);
+        sz += __shfl_xor_sync(0xffffffffu, sz, off);
+    }
+    const float inv = rsqrtf(sx * sx + sy * sy + sz * sz);   // approximate: cos_lo is measured against this u
+    c.u = mk3(sx * inv, sy * inv, sz * inv);
+    float cmin = me ? dot3(w, c.u) : 2.0f;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) cmin = fminf(cmin, __shfl_xor_sync(0xffffffffu, cmin, off));
+    c.cos_lo = cmin - 1e-5f;
+    if (!(c.cos_lo > 0.5f)) return false;
+    c.sin_hi = sqrtf(fmaxf(0.0f, 1.0f - c.cos_lo * c.cos_lo)) + 1e-6f;
+    return true;
+}
+
+// Whether a sphere (centre at v from the apex, radius r) may be hit by a ray
+// of the cone.  extra: added to |v| for the origin-to-centre distance D of the
+// margin; e: absolute inflation.  Approximate reciprocal square roots (a few
+// ulp) are covered by the relative slacks.
+__device__ __forceinline__ bool cone_meets(const WarpCone& c, float3 v, float r, float extra, float e)
+{
+    const float d2 = dot3(v, v);
+    const float inv = rsqrtf(d2);
+    const float dist = d2 * inv;
+    const float m = kBvhK * (dist + extra + 1e-3f);
+    const float R = r * 1.00001f + m + e;
+    if (!(dist > R + m)) return true;   // also a centre at the apex (dist NaN)
+    const float sb = R * inv * 1.0001f;   // >= sin(beta), beta = asin(R / dist)
+    // cos(theta + beta) >= cos(theta) (1 - sin^2 beta) - sin(theta) sin(beta),
+    // since cos(beta) >= cos^2(beta) = 1 - sin^2(beta)
+    const float rhs = c.cos_lo * (1.0f - sb * sb) - c.sin_hi * sb;
+    return dot3(v, c.u) >= dist * (rhs - 1e-5f);
+}
+
+// Radius of a sphere from its r^2, rounded up by more than the error of the
+// approximate square root (r^2 = 0 gives NaN, which passes every cone test).
+__device__ __forceinline__ float cone_radius(float r2)
+{
+    return r2 * rsqrtf(r2) * 1.000001f;
+}
+
+// Nearest hit of the rays (o, d) of the lanes with me set, all leaving the
+// apex o (the same on every lane) inside cone c.  All 32 lanes call it.
+template <bool SMEM>
+__device__ __forceinline__ int32_t nearest_cone(const float4* __restrict__ sph, uint32_t n, float3 o, float3 d, bool me,
+                                                const WarpCone& c, float& tmin)
+{
+    const float a = dot3(d, d);
+    const uint32_t lane = threadIdx.x & 31u;
+    int32_t best = -1;
+    float tm = kFltMax;
+    for (uint32_t base = 0; base < n; base += 32u) {
+        bool pass = false;
+        if (base + lane < n) {
+            const float4 s = table_sphere<SMEM>(sph, base + lane);
+            pass = cone_meets(c, mk3(s.x - o.x, s.y - o.y, s.z - o.z), cone_radius(s.w), 0.0f, 0.0f);
+        }
+        uint32_t mask = __ballot_sync(0xffffffffu, pass);
+        while (mask) {   // lowest index first: ties keep it, as in the brute-force loop
+            const uint32_t i = base + (uint32_t)(__ffs(mask) - 1);
+            mask &= mask - 1u;
+            float t;
+            if (me && sphere_t(table_sphere<SMEM>(sph, i), o, d, a, t) && t > 0.0f && t < tm) {
+                tm = t;
+                best = (int32_t)i;
+            }
+        }
+    }
+    tmin = tm;
+    return best;
+}
+
+// Any hit for the shadow rays (o, d, dist2) of the lanes with me set, whose
+// segments end near the light at apex; c is the cone of the directions from
+// the apex to the origins and dmax the largest apex-to-origin distance.  All
+// 32 lanes call it.
+template <bool SMEM>
+__device__ __forceinline__ bool occluded_cone(const float4* __restrict__ sph, uint32_t n, float3 o, float3 d,
+                                              float dist2, bool me, float3 apex, const WarpCone& c, float dmax)
+{
+    const float a = dot3(d, d);
+    const uint32_t lane = threadIdx.x & 31u;
+    bool occ = false;
+    for (uint32_t base = 0; base < n; base += 32u) {
+        bool pass = false;
+        if (base + lane < n) {
+            const float4 s = table_sphere<SMEM>(sph, base + lane);
+            // D <= |c - apex| + dmax; the segment's bend (1e-4 offset, float
+            // error of the direction) stays within 2e-4 + kBvhK dmax
+            pass = cone_meets(c, mk3(s.x - apex.x, s.y - apex.y, s.z - apex.z), cone_radius(s.w), 2.0f * dmax, 2e-4f);
+        }
+        uint32_t mask = __ballot_sync(0xffffffffu, pass);
+        while (mask) {
+            const uint32_t i = base + (uint32_t)(__ffs(mask) - 1);
+            mask &= mask - 1u;
+            float t;
+            if (me && !occ && sphere_t(table_sphere<SMEM>(sph, i), o, d, a, t) && t > 0.0f && t * t < dist2)
+                occ = true;
+        }
+        if (__all_sync(0xffffffffu, occ || !me)) break;
+    }
+    return occ;
+}
+
+// ------------------------------------------------------------ light buffer
+
+// Cell of direction w around a light, as light_buffer.cu lays out the cube:
+// the face of the largest |component| (+x, -x, +y, -y, +z, -z), then the other
+// two components over it (in [-1, 1]) on a kLbRes grid.  -1 for a zero or
+// non-finite w.
+__device__ __forceinline__ int lb_cell(float3 w)
+{
+    const float ax = fabsf(w.x), ay = fabsf(w.y), az = fabsf(w.z);
+    uint32_t face;
+    float m, a, b;
+    if (ax >= ay && ax >= az) {
+        face = w.x >= 0.0f ? 0u : 1u;
+        m = ax, a = w.y, b = w.z;
+    } else if (ay >= az) {
+        face = w.y >= 0.0f ? 2u : 3u;
+        m = ay, a = w.x, b = w.z;
+    } else {
+        face = w.z >= 0.0f ? 4u : 5u;
+        m = az, a = w.x, b = w.y;
+    }
+    if (!(m > 0.0f && m < 3.0e38f) || !(fabsf(a) <= m && fabsf(b) <= m)) return -1;
+    const float h = 0.5f * (float)kLbRes / m;
+    const int i = min((int)((a + m) * h), (int)kLbRes - 1);
+    const int j = min((int)((b + m) * h), (int)kLbRes - 1);
+    return (int)((face * kLbRes + (uint32_t)i) * kLbRes + (uint32_t)j);
+}
+
+// Any hit for a shadow ray (o, d, dist2) towards light li: the spheres the
+// light buffer lists for the cell of o seen from the light, or the whole table
+// when that cell overflowed, o lies beyond the buffer's reach or the
+// direction is degenerate.
+template <bool SMEM>
+__device__ __forceinline__ bool occluded_lb(const SceneView& sc, const float4* __restrict__ sph, uint32_t li, float3 o,
+                                            float3 d, float dist2)
+{
+    const float4 l0 = __ldg(reinterpret_cast<const float4*>(sc.lights + li));
+    const float3 w = mk3(o.x - l0.x, o.y - l0.y, o.z - l0.z);
+    const float dc = __ldg(&sc.lb.dcap[li]);
+    const int cell = dot3(w, w) <= dc * dc ? lb_cell(w) : -1;
+    const uint32_t slot = li * kLbCells + (uint32_t)cell;
+    const uint32_t cnt = cell >= 0 ? (uint32_t)__ldg(&sc.lb.count[slot]) : (uint32_t)kLbAll;
+    if (cnt == kLbAll) return occluded_brute<SMEM>(sph, sc.n_sph, o, d, dist2);
+    const float a = dot3(d, d);
+    const uint16_t* lst = sc.lb.list + (size_t)slot * kLbMaxList;
+    for (uint32_t k = 0; k < cnt; ++k) {
+        float t;
+        if (sphere_t(table_sphere<SMEM>(sph, __ldg(&lst[k])), o, d, a, t) && t > 0.0f && t * t < dist2) return true;
+    }
+    return false;
+}
+
 template <int IS>
 __device__ __forceinline__ int32_t scene_nearest(const SceneView& sc, const float4* sph, float3 o, float3 d,
                                                  float& tmin)

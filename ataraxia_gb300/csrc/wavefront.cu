@@ -36,6 +36,10 @@ constexpr int kThreads = 256;
 constexpr int kExtendThreads = 256;
 constexpr int kExtendBlocksPerSm = 4;
 
+// k_shadow's blocks per SM: the shared-memory variant fits 40 registers
+// without spilling (6 blocks of 256 threads); the others take up to 64 (4).
+template <int IS>
+constexpr int kShadowBlocksPerSm = IS == kIsSmem ? 6 : 4;
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
@@ -67,10 +71,13 @@ __device__ __forceinline__ float4 light_dir(const SceneView& sc, uint32_t li, fl
 }
 
 // Primary nearest hit once per pixel of the wave (shared by its samples).
+// With the brute-force tables a warp's 32 neighbouring primary rays share the
+// camera as apex and a narrow cone of directions, so the warp culls the
+// sphere table against the cone first (nearest_cone).
 // With per-(pixel, light) shadow rays (wave_light_vis) it also clears the
 // pixel's visibility word and queues, as bounce 0's shadow rays, one ray per
 // distinct light its samples pick (record: origin and squared distance, L and
-// the wave pixel, the light index and the hit sphere).
+// the wave pixel, the light index and the hit sphere with the light).
 template <int IS>
 __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView cam, WaveState ws, WaveJob job)
 {
@@ -88,21 +95,24 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
     const bool vis = wave_light_vis(job, sc.n_lights);   // uniform
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {   // warp-uniform trip count
         const uint32_t j = base + threadIdx.x;
+        const bool me = j < n;
+        const uint32_t p = job.pixel0 + j;
         int32_t id = -1;
         float t = 0.0f;
         float3 d = o;
-        if (j < n) {
-            const uint32_t p = job.pixel0 + j;
-            if (cached) {
+        if (cached) {
+            if (me) {
                 const uint2 pr = prim[j];
                 id = (int32_t)pr.y;
                 t = __uint_as_float(pr.x);
                 if (vis && id >= 0) d = primary_dir(cam, p % cam.width, p / cam.width);
-            } else {
-                d = primary_dir(cam, p % cam.width, p / cam.width);
-                id = scene_nearest<IS>(sc, sph, o, d, t);
-                prim[j] = make_uint2(__float_as_uint(t), (uint32_t)id);
             }
+        } else {
+            if (me) d = primary_dir(cam, p % cam.width, p / cam.width);
+            WarpCone cone;
+            if (IS != kIsBvh && warp_cone(me, d, cone)) id = nearest_cone<SMEM>(sph, sc.n_sph, o, d, me, cone, t);
+            else if (me) id = scene_nearest<IS>(sc, sph, o, d, t);
+            if (me) prim[j] = make_uint2(__float_as_uint(t), (uint32_t)id);
         }
         // pixels whose primary ray hits get first-bounce paths; the others'
         // samples are closed-form (accumulated by k_accumulate)
@@ -112,13 +122,12 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
 
         uint32_t lights = 0u;   // distinct lights the pixel's samples pick (Renderer.cu:339)
         float3 pos = o, nrm = o;
-        if (j < n) ws.vis[j] = 0u;
         if (id >= 0) {
             ray_hit(__ldg(&sc.sph[id]), o, d, t, pos, nrm);
-            const uint32_t p = job.pixel0 + j;
             for (uint32_t s = 0; s < job.spp; ++s) lights |= 1u << (pcg_hash(p * (job.frame0 + s)) % sc.n_lights);
         }
         const float3 so = add3(pos, muls3(nrm, kOffset));
+        if (me) ws.vis[j] = 0u;
         while (__any_sync(kFull, lights != 0u)) {
             const bool has = lights != 0u;
             const uint32_t li = has ? (uint32_t)(__ffs(lights) - 1) : 0u;
@@ -130,7 +139,7 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
                 light_dir(sc, li, pos, L, dist2);
                 ws.sh_o[ss] = make_float4(so.x, so.y, so.z, dist2);
                 ws.sh_d[ss] = make_float4(L.x, L.y, L.z, __uint_as_float(j));
-                ws.sh_c[ss] = make_float4(__uint_as_float(li), 0.0f, 0.0f, __uint_as_float((uint32_t)id));
+                ws.sh_c[ss] = make_float4(__uint_as_float(li), 0.0f, 0.0f, __uint_as_float(shadow_tag((uint32_t)id, li)));
             }
         }
     }
@@ -240,8 +249,9 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
                         const float3 so = add3(pos, muls3(nrm, kOffset));
                         sho = make_float4(so.x, so.y, so.z, dist2);
                         shd = make_float4(L.x, L.y, L.z, __uint_as_float(pid));
-                        // w: the sphere the shadow ray leaves from, tested first by k_shadow
-                        shc = make_float4(c.x, c.y, c.z, __uint_as_float((uint32_t)hit));
+                        // w: the sphere the shadow ray leaves from (tested first by the
+                        // LBVH walk) and the light (for the light buffer)
+                        shc = make_float4(c.x, c.y, c.z, __uint_as_float(shadow_tag((uint32_t)hit, li)));
                         push_sh = true;
                     }
                 }
@@ -320,11 +330,6 @@ __device__ __forceinline__ void shadow_light(const WaveState& ws, uint32_t idx, 
     ws.col[pid] = col;
 }
 
-// k_shadow's blocks per SM: the shared-memory variant fits 40 registers
-// without spilling (6 blocks of 256 threads); the others take up to 64 (4).
-template <int IS>
-constexpr int kShadowBlocksPerSm = IS == kIsSmem ? 6 : 4;
-
 template <int IS, bool VIS>
 __global__ void __launch_bounds__(kThreads, kShadowBlocksPerSm<IS>) k_shadow(SceneView sc, WaveState ws, int bounce)
 {
@@ -337,14 +342,17 @@ __global__ void __launch_bounds__(kThreads, kShadowBlocksPerSm<IS>) k_shadow(Sce
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
 
-    if (IS == kIsBvh || sc.n_sph == 0u) {
+    if (IS == kIsBvh || sc.n_sph == 0u || sc.lb.n_lights != 0u) {
         for (uint32_t idx = first; idx < n; idx += stride) {
             const float4 so = ws.sh_o[idx];
             const float4 sd = ws.sh_d[idx];
             const float3 o = mk3(so.x, so.y, so.z), d = mk3(sd.x, sd.y, sd.z);
-            if (!own_occludes(sc, sph, SMEM, __float_as_uint(ws.sh_c[idx].w), o, d, so.w) &&
-                !scene_occluded<IS>(sc, sph, o, d, so.w))
-                shadow_light<VIS>(ws, idx, sd);
+            const uint32_t tag = __float_as_uint(ws.sh_c[idx].w);
+            bool occ;
+            if (IS == kIsBvh) occ = own_occludes(sc, sph, SMEM, tag & kShadowSphereMask, o, d, so.w) ||
+                                    scene_occluded<IS>(sc, sph, o, d, so.w);
+            else occ = sc.n_sph != 0u && occluded_lb<SMEM>(sc, sph, tag >> 26, o, d, so.w);
+            if (!occ) shadow_light<VIS>(ws, idx, sd);
         }
         return;
     }

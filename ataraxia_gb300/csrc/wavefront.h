@@ -49,6 +49,34 @@ struct BvhView {
     uint32_t root;
 };
 
+// Light buffer (Haines and Greenberg's light buffer, 1986) for the
+// brute-force sphere tables: for each point light a cube of directions around
+// it, 6 faces of kLbRes x kLbRes cells, and for each cell the spheres that can
+// block a shadow ray towards that light whose origin, seen from the light,
+// lies in the cell (built by light_buffer.cu).  A shadow ray then tests the
+// spheres of one cell instead of the whole table.
+constexpr uint32_t kLbRes = 16;
+constexpr uint32_t kLbCells = 6 * kLbRes * kLbRes;
+constexpr uint32_t kLbMaxList = 32;
+constexpr uint32_t kLbMaxLights = 64;
+constexpr uint32_t kLbMaxSpheres = 65535;   // indices are 16-bit
+constexpr uint8_t kLbAll = 0xff;            // the cell's list overflowed: test every sphere
+struct LightBufferView {
+    const uint8_t* count;    // [n_lights * kLbCells] spheres listed, or kLbAll
+    const uint16_t* list;    // [n_lights * kLbCells * kLbMaxList] sphere indices, ascending
+    const float* dcap;       // [n_lights] the lists hold for shadow-ray origins within dcap of the light
+    uint32_t n_lights;       // 0: no light buffer
+};
+
+// Shadow-ray records carry the sphere the ray leaves from and the light it
+// goes to in one word: sphere in the low 26 bits, light in the high 6 (only
+// read when the light buffer, at most 64 lights, is in use).
+constexpr uint32_t kShadowSphereMask = (1u << 26) - 1u;
+__host__ __device__ inline uint32_t shadow_tag(uint32_t sphere, uint32_t light)
+{
+    return (sphere & kShadowSphereMask) | (light << 26);
+}
+
 // Scene tables, all in device memory.
 struct SceneView {
     const float4* sph;        // (cx, cy, cz, radius*radius), n_sph entries
@@ -60,6 +88,7 @@ struct SceneView {
     uint32_t n_lights;
     uint32_t use_bvh;         // 1: traverse bvh instead of the brute-force loop
     BvhView bvh;
+    LightBufferView lb;       // shadow-ray cells of the brute-force tables (lb.n_lights 0: none)
 };
 
 // Camera as the ray generator needs it (Camera.cpp:161-195): column-major

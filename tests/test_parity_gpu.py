@@ -155,10 +155,11 @@ def test_sky_light_and_emission(po):
     assert bit_mismatches(acc, ref) == 0
 
 
-@pytest.mark.parametrize("n_lights,spp", [(32, 8), (33, 8), (5, 1), (31, 40)])
+@pytest.mark.parametrize("n_lights,spp", [(32, 8), (33, 8), (5, 1), (31, 40), (70, 3)])
 def test_first_bounce_light_visibility_per_pixel(po, n_lights, spp):
     # up to 32 lights a pixel's samples share one shadow ray per distinct light
-    # at the first bounce; above that every sample casts its own
+    # at the first bounce; above that every sample casts its own.  Up to 64
+    # lights shadow rays go through the light buffer, above that the whole table
     sc = scenes.config1().with_resolution(72, 40)
     rng = np.random.default_rng(n_lights)
     lights = np.zeros(n_lights, dtype=scenes.LIGHT_DTYPE)
@@ -170,6 +171,54 @@ def test_first_bounce_light_visibility_per_pixel(po, n_lights, spp):
     ref, _, _ = oracle_render(sc, spp)
     assert bit_mismatches(acc, ref) == 0
     assert np.array_equal(img, po.pack_rgba8(ref, spp))
+
+
+def _cone_scene(kind):
+    st = scenes.Stream(7, "cone-" + kind)
+    mats = scenes.draw_materials(st, 8)
+    if kind == "far_narrow":     # distant camera, 3 deg: most primary rays pass within float error of a sphere
+        n = 600
+        c = st.uniform(3 * n, -5, 5).reshape(n, 3)
+        r = st.uniform(n, 0.05, 0.4)
+        cam, look, fov, far = (0.0, 30.0, 400.0), (0.0, -30.0, -400.0), 3.0, 1000.0
+        lts = scenes.draw_lights(st, 4, 8.0)
+    elif kind == "inside":       # camera inside a large sphere, small spheres around it and behind it
+        n = 200
+        c = np.concatenate([np.zeros((1, 3)), st.uniform(3 * (n - 1), -30, 30).reshape(n - 1, 3)])
+        r = np.concatenate([[50.0], st.uniform(n - 1, 0.2, 2.0)])
+        cam, look, fov, far = (0.0, 0.0, 5.0), (0.3, -0.2, -1.0), 60.0, 100.0
+        lts = scenes.draw_lights(st, 6, 10.0)
+    else:                        # spheres touching the near plane; lights on and inside sphere surfaces
+        n = 64
+        c = np.concatenate([[[0.6, 0.0, 0.0]], st.uniform(3 * (n - 1), -3, 3).reshape(n - 1, 3)])
+        r = np.concatenate([[0.45], st.uniform(n - 1, 0.05, 0.6)])
+        cam, look, fov, far = (0.0, 0.0, 0.5), (0.0, 0.0, -1.0), 70.0, 100.0
+        lts = np.zeros(3, dtype=scenes.LIGHT_DTYPE)
+        lts["position"] = [c[1], c[2] + [0.0, r[2], 0.0], [0.0, 4.0, 2.0]]
+        lts["color"] = 1.0
+        lts["intensity"] = [30.0, 60.0, 90.0]
+    sph = np.zeros(n, dtype=scenes.SPHERE_DTYPE)
+    sph["center"] = c
+    sph["radius"] = r
+    sph["material"] = np.arange(n) % 8
+    return scenes.SyntheticScene("cone-" + kind, sph, mats, lts, cam, look, fov=fov, far=far, width=96, height=64,
+                                 max_bounces=4)
+
+
+@pytest.mark.parametrize("kind", ["far_narrow", "inside", "near"])
+def test_warp_cone_culling_edge_cases(po, kind):
+    # the warp-cone culling of primary rays and first-bounce shadow rays must
+    # never drop a sphere the float test accepts: grazing rays from far away,
+    # a camera inside a sphere, spheres at the near plane, lights on surfaces
+    sc = _cone_scene(kind)
+    acc, img = gpu_render(sc, 6)
+    ref, _, _ = oracle_render(sc, 6)
+    assert bit_mismatches(acc, ref) == 0
+    assert np.array_equal(img, po.pack_rgba8(ref, 6))
+    o = np.repeat(np.asarray(sc.camera_position, np.float32)[None], sc.pixels, 0)
+    d = np.asarray(po.ray_dirs(po.view_for(sc), po.EXACT), np.float32).reshape(-1, 3)
+    _, rids = po.trace(sc.spheres, o, d, po.EXACT)
+    assert (rids >= 0).mean() > 0.05    # the primary rays do meet spheres
 
 
 def test_empty_scene_no_lights_and_bad_material_ids(po):
