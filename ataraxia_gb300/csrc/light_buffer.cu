@@ -2,7 +2,7 @@
 // LightBufferView), after Haines and Greenberg's light buffer (1986): around
 // each point light a cube of direction cells, and per cell the spheres a
 // shadow ray towards the light can meet when its origin, seen from the light,
-// lies in that cell.  Built once per scene, in double precision.
+// lies in that cell.  Built once per scene.
 //
 // Exactness.  A shadow ray (origin o = p + 1e-4 N on a sphere, direction
 // L = normalize(light - p), occluded when some sphere has t > 0 and
@@ -33,85 +33,90 @@ uint64_t up(uint64_t x) { return (x + 255u) & ~uint64_t(255u); }
 // Unit direction of face f (0..5: +x, -x, +y, -y, +z, -z) at in-face
 // coordinates (u, v): the axes trace.cuh lb_cell divides by the face axis
 // (face x: y, z; face y: x, z; face z: x, y).
-__device__ void face_dir(uint32_t f, double u, double v, double out[3])
+__device__ float3 face_dir(uint32_t f, float u, float v)
 {
     const uint32_t ax = f >> 1;
+    float c[3];
     const uint32_t a = ax == 0 ? 1u : 0u, b = ax == 2 ? 1u : 2u;
-    out[ax] = (f & 1u) ? -1.0 : 1.0;
-    out[a] = u;
-    out[b] = v;
-    const double s = 1.0 / sqrt(out[0] * out[0] + out[1] * out[1] + out[2] * out[2]);
-    out[0] *= s;
-    out[1] *= s;
-    out[2] *= s;
+    c[ax] = (f & 1u) ? -1.0f : 1.0f;
+    c[a] = u;
+    c[b] = v;
+    const float s = 1.0f / sqrtf(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    return make_float3(c[0] * s, c[1] * s, c[2] * s);
 }
+
+__device__ float dotf3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
 // dcap[l] = max over spheres of |c - light| + r, plus 1: every shadow-ray
 // origin (a hit point lifted by 1e-4) lies within it.
 __global__ void k_lb_dcap(const float4* __restrict__ sph, const float* __restrict__ rad, uint32_t n,
                           const DevLight* __restrict__ lights, float* dcap)
 {
-    __shared__ double red[256];
+    __shared__ float red[256];
     const DevLight lt = lights[blockIdx.x];
-    double mx = 0.0;
+    float mx = 0.0f;
     for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
         const float4 s = sph[k];
-        const double x = (double)s.x - lt.pos[0], y = (double)s.y - lt.pos[1], z = (double)s.z - lt.pos[2];
-        mx = fmax(mx, sqrt(x * x + y * y + z * z) + (double)rad[k]);
+        const float3 v = make_float3(s.x - lt.pos[0], s.y - lt.pos[1], s.z - lt.pos[2]);
+        mx = fmaxf(mx, sqrtf(dotf3(v, v)) + rad[k]);
     }
     red[threadIdx.x] = mx;
     __syncthreads();
     for (uint32_t h = blockDim.x / 2; h > 0; h >>= 1) {
-        if (threadIdx.x < h) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + h]);
+        if (threadIdx.x < h) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + h]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) dcap[blockIdx.x] = (float)(red[0] * (1.0 + 1e-6) + 1.0);
+    if (threadIdx.x == 0) dcap[blockIdx.x] = red[0] * 1.0001f + 1.0f;
 }
 
-// One thread per (light, cell).
+// One warp per (light, cell); the lanes test 32 spheres at a time and append
+// the listed ones in index order.  Float arithmetic with every bound rounded
+// towards listing: the cell's half-angle widened by 2e-4 rad (1e-4 for the
+// lookup's rounding, the rest for this arithmetic), sin(beta) rounded up,
+// cos(beta) taken from it, a 2e-5 slack on the final comparison.
 __global__ void k_lb_build(const float4* __restrict__ sph, const float* __restrict__ rad, uint32_t n,
                            const DevLight* __restrict__ lights, uint32_t nl, const float* __restrict__ dcap,
                            uint8_t* count, uint16_t* list)
 {
-    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= nl * kLbCells) return;
+    const uint32_t id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (id >= nl * kLbCells) return;   // whole warps: blockDim is a multiple of 32
     const uint32_t l = id / kLbCells, cell = id % kLbCells;
     const uint32_t f = cell / (kLbRes * kLbRes), i = (cell / kLbRes) % kLbRes, j = cell % kLbRes;
-    const double u0 = 2.0 * i / kLbRes - 1.0, u1 = 2.0 * (i + 1) / kLbRes - 1.0;
-    const double v0 = 2.0 * j / kLbRes - 1.0, v1 = 2.0 * (j + 1) / kLbRes - 1.0;
-    double ctr[3];
-    face_dir(f, 0.5 * (u0 + u1), 0.5 * (v0 + v1), ctr);
+    const float u0 = 2.0f * i / kLbRes - 1.0f, u1 = 2.0f * (i + 1) / kLbRes - 1.0f;
+    const float v0 = 2.0f * j / kLbRes - 1.0f, v1 = 2.0f * (j + 1) / kLbRes - 1.0f;
+    const float3 ctr = face_dir(f, 0.5f * (u0 + u1), 0.5f * (v0 + v1));
     // bounding cone of the cell: its farthest points from the centre are corners
-    double half = 0.0;
-    for (int k = 0; k < 4; ++k) {
-        double c[3];
-        face_dir(f, (k & 1) ? u1 : u0, (k & 2) ? v1 : v0, c);
-        const double dp = ctr[0] * c[0] + ctr[1] * c[1] + ctr[2] * c[2];
-        half = fmax(half, acos(fmin(1.0, fmax(-1.0, dp))));
-    }
-    half += 1e-6;
+    float cmin = 1.0f;
+    for (int k = 0; k < 4; ++k) cmin = fminf(cmin, dotf3(ctr, face_dir(f, (k & 1) ? u1 : u0, (k & 2) ? v1 : v0)));
+    const float hw = acosf(fminf(1.0f, cmin)) + 2e-4f;
+    const float ch = cosf(hw), sh = sinf(hw);
     const DevLight lt = lights[l];
-    const double dc = dcap[l];
-    uint32_t cnt = 0;
-    bool all = false;
+    const float dc = dcap[l];
     uint16_t* out = list + (size_t)id * kLbMaxList;
-    for (uint32_t k = 0; k < n; ++k) {
-        const float4 s = sph[k];
-        const double vx = (double)s.x - lt.pos[0], vy = (double)s.y - lt.pos[1], vz = (double)s.z - lt.pos[2];
-        const double dist = sqrt(vx * vx + vy * vy + vz * vz);
-        const double m = kK * (dist + dc + 1e-3);
-        const double rp = (double)rad[k] * (1.0 + 1e-5) + m + 2e-4 + kK * dc;
-        bool listed = dist <= rp + m;
-        if (!listed) {
-            const double cosang = (ctr[0] * vx + ctr[1] * vy + ctr[2] * vz) / dist;
-            listed = acos(fmin(1.0, fmax(-1.0, cosang))) <= half + asin(fmin(1.0, rp / dist)) + 1e-4;
+    uint32_t cnt = 0;
+    for (uint32_t base = 0; base < n && cnt <= kLbMaxList; base += 32u) {
+        const uint32_t k = base + lane;
+        bool listed = false;
+        if (k < n) {
+            const float4 s = sph[k];
+            const float3 v = make_float3(s.x - lt.pos[0], s.y - lt.pos[1], s.z - lt.pos[2]);
+            const float dist = sqrtf(dotf3(v, v));
+            const float m = (float)kK * (dist + dc + 1e-3f);
+            const float rp = rad[k] * 1.00001f + m + 2e-4f + (float)kK * dc;
+            if (!(dist > (rp + m) * 1.0001f)) {
+                listed = true;   // the light may sit in (or next to) the sphere
+            } else {
+                const float sb = fminf(1.0f, rp / dist * 1.0001f);
+                const float cb = sqrtf(fmaxf(0.0f, 1.0f - sb * sb));
+                listed = dotf3(ctr, v) >= dist * (ch * cb - sh * sb - 2e-5f);   // cos(angle) >= cos(hw + beta)
+            }
         }
-        if (!listed) continue;
-        if (cnt < kLbMaxList) out[cnt] = (uint16_t)k;
-        else all = true;
-        ++cnt;
+        const uint32_t mask = __ballot_sync(0xffffffffu, listed);
+        const uint32_t pos = cnt + __popc(mask & ((1u << lane) - 1u));
+        if (listed && pos < kLbMaxList) out[pos] = (uint16_t)k;
+        cnt += __popc(mask);
     }
-    count[id] = all ? kLbAll : (uint8_t)cnt;
+    if (lane == 0) count[id] = cnt > kLbMaxList ? kLbAll : (uint8_t)cnt;
 }
 
 }  // namespace
@@ -135,7 +140,8 @@ cudaError_t lb_build(const float4* sph, const float* radius, uint32_t n, const D
     p += up(cells * kLbMaxList * sizeof(uint16_t));
     float* dcap = reinterpret_cast<float*>(p);
     k_lb_dcap<<<nl, 256, 0, stream>>>(sph, radius, n, lights, dcap);
-    k_lb_build<<<(unsigned)((cells + 127) / 128), 128, 0, stream>>>(sph, radius, n, lights, nl, dcap, count, list);
+    k_lb_build<<<(unsigned)((cells * 32 + 255) / 256), 256, 0, stream>>>(sph, radius, n, lights, nl, dcap, count,
+                                                                       list);
     out->count = count;
     out->list = list;
     out->dcap = dcap;

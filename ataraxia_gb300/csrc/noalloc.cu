@@ -171,6 +171,7 @@ extern "C" ATX_API atx_status atx_render_noalloc(const atx_sphere* spheres, uint
     sc.n_sph = n_spheres;
     sc.n_mat = n_materials;
     sc.n_lights = n_lights;
+    sc.light_mod = fastmod_multiplier(n_lights);
     sc.use_bvh = 0;
 
     CameraView cam{};

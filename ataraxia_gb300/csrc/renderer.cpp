@@ -80,6 +80,7 @@ atx_status SceneStore::upload(const atx_sphere* s, uint32_t n, const atx_materia
     view.n_sph = n;
     view.n_mat = nm;
     view.n_lights = nl;
+    view.light_mod = fastmod_multiplier(nl);
 
     const uint32_t thr = bvh_threshold ? bvh_threshold : kDefaultBvhThreshold;
     if (n >= thr && n > 1) {

@@ -57,6 +57,14 @@ __device__ __forceinline__ uint32_t warp_push(uint32_t* counter, bool pred)
     return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
 }
 
+// Renderer.cu:339: the light a shading point samples, PcgHash(seed) % lights
+// (the seed is not advanced), the remainder by multiplication (fastmod).
+__device__ __forceinline__ uint32_t light_pick(const SceneView& sc, uint32_t seed)
+{
+    const uint64_t low = sc.light_mod * (uint64_t)pcg_hash(seed);
+    return (uint32_t)__umul64hi(low, (uint64_t)sc.n_lights);
+}
+
 // Renderer.cu:339-348: light li's parameter row, the unit direction L from pos
 // to the light and the squared distance.  One function for the first bounce
 // and the per-(pixel, light) shadow rays, so both compute the same floats.
@@ -75,9 +83,10 @@ __device__ __forceinline__ float4 light_dir(const SceneView& sc, uint32_t li, fl
 // camera as apex and a narrow cone of directions, so the warp culls the
 // sphere table against the cone first (nearest_cone).
 // With per-(pixel, light) shadow rays (wave_light_vis) it also clears the
-// pixel's visibility word and queues, as bounce 0's shadow rays, one ray per
-// distinct light its samples pick (record: origin and squared distance, L and
-// the wave pixel, the light index and the hit sphere with the light).
+// pixel's visibility word, stores at the pixel's hit slot the hit point with
+// its sphere and the shadow-ray origin with the pixel, and queues in q[0], as
+// bounce 0's shadow rays, one entry (hit slot, light) per distinct light the
+// pixel's samples pick (q[0] is idle until the second bounce).
 template <int IS>
 __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView cam, WaveState ws, WaveJob job)
 {
@@ -124,23 +133,31 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
         float3 pos = o, nrm = o;
         if (id >= 0) {
             ray_hit(__ldg(&sc.sph[id]), o, d, t, pos, nrm);
-            for (uint32_t s = 0; s < job.spp; ++s) lights |= 1u << (pcg_hash(p * (job.frame0 + s)) % sc.n_lights);
+            for (uint32_t s = 0; s < job.spp; ++s) lights |= 1u << light_pick(sc, p * (job.frame0 + s));
         }
-        const float3 so = add3(pos, muls3(nrm, kOffset));
         if (me) ws.vis[j] = 0u;
-        while (__any_sync(kFull, lights != 0u)) {
-            const bool has = lights != 0u;
-            const uint32_t li = has ? (uint32_t)(__ffs(lights) - 1) : 0u;
+        if (id >= 0) {
+            const float3 so = add3(pos, muls3(nrm, kOffset));
+            ws.sh_o[slot] = make_float4(pos.x, pos.y, pos.z, __uint_as_float((uint32_t)id));
+            ws.sh_d[slot] = make_float4(so.x, so.y, so.z, __uint_as_float(j));
+        }
+        // one slot range per warp, lane after lane: an inclusive scan of the
+        // lanes' light counts and one atomicAdd
+        const uint32_t cnt = (uint32_t)__popc(lights);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t v = __shfl_up_sync(kFull, incl, off);
+            if ((int)lane_id() >= off) incl += v;
+        }
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        uint32_t at = 0u;
+        if (lane_id() == 31u && total) at = atomicAdd(&ws.counters[1], total);
+        at = __shfl_sync(kFull, at, 31) + incl - cnt;
+        while (lights) {
+            const uint32_t li = (uint32_t)(__ffs(lights) - 1);
             lights &= lights - 1u;
-            const uint32_t ss = warp_push(&ws.counters[1], has);
-            if (has) {
-                float3 L;
-                float dist2;
-                light_dir(sc, li, pos, L, dist2);
-                ws.sh_o[ss] = make_float4(so.x, so.y, so.z, dist2);
-                ws.sh_d[ss] = make_float4(L.x, L.y, L.z, __uint_as_float(j));
-                ws.sh_c[ss] = make_float4(__uint_as_float(li), 0.0f, 0.0f, __uint_as_float(shadow_tag((uint32_t)id, li)));
-            }
+            ws.q[0][at++] = shadow_tag(slot, li);
         }
     }
 }
@@ -236,7 +253,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
                 const float3 base = add3(muls3(f0, 1.0f - metallic), muls3(albedo, metallic));
 
                 if (sc.n_lights > 0u) {  // Renderer.cu:338-369
-                    const uint32_t li = pcg_hash(seed) % sc.n_lights;
+                    const uint32_t li = light_pick(sc, seed);
                     float3 L;
                     float dist2;
                     const float4 l1 = light_dir(sc, li, pos, L, dist2);
@@ -312,22 +329,60 @@ __device__ __forceinline__ bool own_occludes(const SceneView& sc, const float4* 
     return sphere_t(s, o, d, dot3(d, d), t) && t > 0.0f && t * t < dist2;
 }
 
-// Adds the light a shadow ray carries to its path (Renderer.cu:356-368), or,
-// for a per-(pixel, light) ray (VIS), marks the light visible from the pixel.
+// A shadow ray of one bounce's queue: origin, direction, squared distance to
+// the light, tag (the sphere it leaves from and the light) and target (the
+// path, or for VIS the wave pixel).  Per-sample rays are stored whole (sh_o:
+// origin, dist^2; sh_d: direction, path; sh_c: light contribution, tag).
+// First-bounce (pixel, light) entries (VIS) hold the hit slot and the light;
+// the slot's record gives the hit point and sphere, the origin and the pixel,
+// and the direction and distance are recomputed by light_dir exactly as the
+// shading computes them.
+struct ShadowRay {
+    float3 o, d;
+    float dist2;
+    uint32_t tag;
+    uint32_t target;
+};
+
 template <bool VIS>
-__device__ __forceinline__ void shadow_light(const WaveState& ws, uint32_t idx, float4 sd)
+__device__ __forceinline__ ShadowRay load_shadow(const SceneView& sc, const WaveState& ws, uint32_t idx)
+{
+    ShadowRay r;
+    if (VIS) {
+        const uint32_t e = ws.q[0][idx];
+        const uint32_t slot = e & kShadowSphereMask, li = e >> 26;
+        const float4 a = ws.sh_o[slot], b = ws.sh_d[slot];
+        light_dir(sc, li, mk3(a.x, a.y, a.z), r.d, r.dist2);
+        r.o = mk3(b.x, b.y, b.z);
+        r.tag = shadow_tag(__float_as_uint(a.w), li);
+        r.target = __float_as_uint(b.w);
+    } else {
+        const float4 so = ws.sh_o[idx], sd = ws.sh_d[idx];
+        r.o = mk3(so.x, so.y, so.z);
+        r.d = mk3(sd.x, sd.y, sd.z);
+        r.dist2 = so.w;
+        r.tag = __float_as_uint(ws.sh_c[idx].w);
+        r.target = __float_as_uint(sd.w);
+    }
+    return r;
+}
+
+// Adds the light an unoccluded shadow ray carries to its path (Renderer.cu:
+// 356-368), or, for a (pixel, light) ray (VIS), marks the light visible from
+// the pixel.
+template <bool VIS>
+__device__ __forceinline__ void shadow_light(const WaveState& ws, uint32_t idx, const ShadowRay& r)
 {
     if (VIS) {
-        atomicOr(&ws.vis[__float_as_uint(sd.w)], 1u << __float_as_uint(ws.sh_c[idx].x));
+        atomicOr(&ws.vis[r.target], 1u << (r.tag >> 26));
         return;
     }
     const float4 c = ws.sh_c[idx];
-    const uint32_t pid = __float_as_uint(sd.w);
-    float4 col = ws.col[pid];
+    float4 col = ws.col[r.target];
     col.x = col.x + c.x;
     col.y = col.y + c.y;
     col.z = col.z + c.z;
-    ws.col[pid] = col;
+    ws.col[r.target] = col;
 }
 
 template <int IS, bool VIS>
@@ -344,15 +399,12 @@ __global__ void __launch_bounds__(kThreads, kShadowBlocksPerSm<IS>) k_shadow(Sce
 
     if (IS == kIsBvh || sc.n_sph == 0u || sc.lb.n_lights != 0u) {
         for (uint32_t idx = first; idx < n; idx += stride) {
-            const float4 so = ws.sh_o[idx];
-            const float4 sd = ws.sh_d[idx];
-            const float3 o = mk3(so.x, so.y, so.z), d = mk3(sd.x, sd.y, sd.z);
-            const uint32_t tag = __float_as_uint(ws.sh_c[idx].w);
+            const ShadowRay r = load_shadow<VIS>(sc, ws, idx);
             bool occ;
-            if (IS == kIsBvh) occ = own_occludes(sc, sph, SMEM, tag & kShadowSphereMask, o, d, so.w) ||
-                                    scene_occluded<IS>(sc, sph, o, d, so.w);
-            else occ = sc.n_sph != 0u && occluded_lb<SMEM>(sc, sph, tag >> 26, o, d, so.w);
-            if (!occ) shadow_light<VIS>(ws, idx, sd);
+            if (IS == kIsBvh) occ = own_occludes(sc, sph, SMEM, r.tag & kShadowSphereMask, r.o, r.d, r.dist2) ||
+                                    scene_occluded<IS>(sc, sph, r.o, r.d, r.dist2);
+            else occ = sc.n_sph != 0u && occluded_lb<SMEM>(sc, sph, r.tag >> 26, r.o, r.d, r.dist2);
+            if (!occ) shadow_light<VIS>(ws, idx, r);
         }
         return;
     }
@@ -369,32 +421,23 @@ __global__ void __launch_bounds__(kThreads, kShadowBlocksPerSm<IS>) k_shadow(Sce
     const uint32_t nchunks = (sc.n_sph + 31u) / 32u;
     const uint32_t tail = sc.n_sph - (nchunks - 1u) * 32u;   // spheres in the last chunk
     uint32_t idx = 0u, left = 0u, chunk = 0u;
-    float3 o = mk3(0.f, 0.f, 0.f), d = o;
-    float a = 0.0f, dist2 = 0.0f;
-    float4 sd = make_float4(0.f, 0.f, 0.f, 0.f);
+    float a = 0.0f;
+    ShadowRay cur{}, nxt{};
     bool live = false;   // lane holds a ray
     uint32_t nidx = first;
-    float4 nso = sd, nsd = sd;
-    if (nidx < n) {
-        nso = ws.sh_o[nidx];
-        nsd = ws.sh_d[nidx];
-    }
+    if (nidx < n) nxt = load_shadow<VIS>(sc, ws, nidx);
     for (;;) {   // ends: every iteration retires a ray or takes a chunk off one
         if (!live && nidx < n) {
             idx = nidx;
-            sd = nsd;
-            o = mk3(nso.x, nso.y, nso.z);
-            d = mk3(nsd.x, nsd.y, nsd.z);
-            a = dot3(d, d);
-            dist2 = nso.w;
+            cur = nxt;
+            a = dot3(cur.d, cur.d);
             left = nchunks;
             live = true;
             nidx += stride;
-            if (nidx < n) {
-                nso = ws.sh_o[nidx];
-                nsd = ws.sh_d[nidx];
-            }
+            if (nidx < n) nxt = load_shadow<VIS>(sc, ws, nidx);
         }
+        const float3 o = cur.o, d = cur.d;
+        const float dist2 = cur.dist2;
         if (!__any_sync(kFull, live)) break;
         if (live) {
             const uint32_t base = chunk * 32u;
@@ -413,7 +456,7 @@ __global__ void __launch_bounds__(kThreads, kShadowBlocksPerSm<IS>) k_shadow(Sce
                 }
             }
             if (hit || --left == 0u) {
-                if (!hit) shadow_light<VIS>(ws, idx, sd);   // Renderer.cu:353-369: unoccluded
+                if (!hit) shadow_light<VIS>(ws, idx, cur);   // Renderer.cu:353-369: unoccluded
                 live = false;
             }
         }

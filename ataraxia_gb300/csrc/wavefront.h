@@ -89,7 +89,17 @@ struct SceneView {
     uint32_t use_bvh;         // 1: traverse bvh instead of the brute-force loop
     BvhView bvh;
     LightBufferView lb;       // shadow-ray cells of the brute-force tables (lb.n_lights 0: none)
+    uint64_t light_mod;       // fastmod_multiplier(n_lights): x % n_lights by multiplication
 };
+
+// x % d for d >= 1 by two multiplications (Lemire, Kaser and Kurz, "Faster
+// remainder by direct computation", 2019): with M = floor((2^64 - 1) / d) + 1,
+// x % d is the high 64 bits of (M * x mod 2^64) * d, for every 32-bit x
+// (d = 1 gives M = 0 and the right answer, 0).
+__host__ __device__ inline uint64_t fastmod_multiplier(uint32_t d)
+{
+    return d ? ~uint64_t(0) / d + 1u : 0u;
+}
 
 // Camera as the ray generator needs it (Camera.cpp:161-195): column-major
 // inverse projection and inverse view, the eye position and the viewport.
@@ -169,10 +179,10 @@ __host__ __device__ inline bool wave_shares_primary(const WaveJob& j)
 // cast the same shadow ray: k_primary queues one ray per distinct light the
 // pixel's samples pick, k_shadow records the visible ones in ws.vis, and the
 // first bounce adds the light of a sample whose light is visible.  Needs the
-// light set to fit one 32-bit word.
+// light set to fit one 32-bit word (and a wave's hit slots 26 bits).
 __host__ __device__ inline bool wave_light_vis(const WaveJob& j, uint32_t n_lights)
 {
-    return wave_shares_primary(j) && n_lights > 0u && n_lights <= 32u;
+    return wave_shares_primary(j) && n_lights > 0u && n_lights <= 32u && j.n_pixels <= (1u << 26);
 }
 
 // Kernel families timed by KernelTimer.
