@@ -119,6 +119,92 @@ __global__ void k_lb_build(const float4* __restrict__ sph, const float* __restri
     if (lane == 0) count[id] = cnt > kLbMaxList ? kLbAll : (uint8_t)cnt;
 }
 
+// ---------------------------------------------------------- direction buffer
+//
+// Exactness.  An extension ray leaves the sphere its path last hit: origin
+// o = p + 1e-4 N with p the float hit point, direction d.  The lookup uses the
+// lists of that sphere i only when |o - c_i| <= reach_i (checked per ray;
+// else the whole table), so o = c_i + e with |e| <= reach_i.  A sphere j the
+// float test accepts has a ray point X = o + t d, t >= -4.5 sqrt(eps) D_j,
+// within r_j + 4 sqrt(eps) D_j of c_j (D_j = |o - c_j| <= |c_j - c_i| +
+// reach_i).  Then c_i + t d = X - e lies within R' = r_j + m + reach_i of c_j,
+// m = kK (D_j + 1e-3): for t >= 0 the ball (c_j, R') meets the cone of
+// directions of d's cell from apex c_i, and for t < 0 its centre lies within
+// R' + m of c_i.  A cell lists every sphere passing one of those two tests
+// (cell cone widened by 2e-4 rad, bounds rounded towards listing), sphere i
+// itself included.
+
+// E = max over spheres of |c|_1 + r, a bound on the coordinates the hit-point
+// arithmetic sees (one block).
+__global__ void k_db_extent(const float4* __restrict__ sph, const float* __restrict__ rad, uint32_t n, float* ext)
+{
+    __shared__ float red[256];
+    float mx = 0.0f;
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+        const float4 s = sph[k];
+        mx = fmaxf(mx, fabsf(s.x) + fabsf(s.y) + fabsf(s.z) + rad[k]);
+    }
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (uint32_t h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + h]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *ext = red[0];
+}
+
+// reach_i: the sphere's radius, its 1e-4 surface offset and a float hit
+// point's typical error (a hit point farther off falls back to the whole table).
+__global__ void k_db_reach(const float* __restrict__ rad, uint32_t n, const float* __restrict__ ext, float* reach)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) reach[i] = rad[i] * 1.001f + 2e-4f + (float)kK * *ext;
+}
+
+// One warp per (sphere, cell), as k_lb_build.
+__global__ void k_db_build(const float4* __restrict__ sph, const float* __restrict__ rad, uint32_t n,
+                           const float* __restrict__ reach, uint8_t* count, uint16_t* list)
+{
+    const uint32_t id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (id >= n * kLbCells) return;   // whole warps: blockDim is a multiple of 32
+    const uint32_t i = id / kLbCells, cell = id % kLbCells;
+    const uint32_t f = cell / (kLbRes * kLbRes), ci = (cell / kLbRes) % kLbRes, cj = cell % kLbRes;
+    const float u0 = 2.0f * ci / kLbRes - 1.0f, u1 = 2.0f * (ci + 1) / kLbRes - 1.0f;
+    const float v0 = 2.0f * cj / kLbRes - 1.0f, v1 = 2.0f * (cj + 1) / kLbRes - 1.0f;
+    const float3 ctr = face_dir(f, 0.5f * (u0 + u1), 0.5f * (v0 + v1));
+    float cmin = 1.0f;
+    for (int k = 0; k < 4; ++k) cmin = fminf(cmin, dotf3(ctr, face_dir(f, (k & 1) ? u1 : u0, (k & 2) ? v1 : v0)));
+    const float hw = acosf(fminf(1.0f, cmin)) + 2e-4f;
+    const float ch = cosf(hw), sh = sinf(hw);
+    const float4 o = sph[i];
+    const float rho = reach[i];
+    uint16_t* out = list + (size_t)id * kLbMaxList;
+    uint32_t cnt = 0;
+    for (uint32_t base = 0; base < n && cnt <= kLbMaxList; base += 32u) {
+        const uint32_t k = base + lane;
+        bool listed = false;
+        if (k < n) {
+            const float4 s = sph[k];
+            const float3 v = make_float3(s.x - o.x, s.y - o.y, s.z - o.z);
+            const float dist = sqrtf(dotf3(v, v));
+            const float m = (float)kK * (dist + rho + 1e-3f);
+            const float rp = rad[k] * 1.00001f + m + rho;
+            if (!(dist > (rp + m) * 1.0001f)) {
+                listed = true;   // overlaps the origin's neighbourhood (sphere i itself too)
+            } else {
+                const float sb = fminf(1.0f, rp / dist * 1.0001f);
+                const float cb = sqrtf(fmaxf(0.0f, 1.0f - sb * sb));
+                listed = dotf3(ctr, v) >= dist * (ch * cb - sh * sb - 2e-5f);
+            }
+        }
+        const uint32_t mask = __ballot_sync(0xffffffffu, listed);
+        const uint32_t pos = cnt + __popc(mask & ((1u << lane) - 1u));
+        if (listed && pos < kLbMaxList) out[pos] = (uint16_t)k;
+        cnt += __popc(mask);
+    }
+    if (lane == 0) count[id] = cnt > kLbMaxList ? kLbAll : (uint8_t)cnt;
+}
+
 }  // namespace
 
 uint64_t lb_bytes(uint32_t nl)
@@ -146,6 +232,35 @@ cudaError_t lb_build(const float4* sph, const float* radius, uint32_t n, const D
     out->list = list;
     out->dcap = dcap;
     out->n_lights = nl;
+    return cudaGetLastError();
+}
+
+uint64_t db_bytes(uint32_t n)
+{
+    const uint64_t cells = (uint64_t)n * kLbCells;
+    return up(cells) + up(cells * kLbMaxList * sizeof(uint16_t)) + up(n * sizeof(float)) + up(sizeof(float)) + 256;
+}
+
+cudaError_t db_build(const float4* sph, const float* radius, uint32_t n, void* buf, uint64_t bytes,
+                     DirBufferView* out, cudaStream_t stream)
+{
+    if (n == 0 || n > kDbMaxSpheres || bytes < db_bytes(n)) return cudaErrorInvalidValue;
+    const uint64_t cells = (uint64_t)n * kLbCells;
+    unsigned char* p = static_cast<unsigned char*>(buf);
+    uint8_t* count = p;
+    p += up(cells);
+    uint16_t* list = reinterpret_cast<uint16_t*>(p);
+    p += up(cells * kLbMaxList * sizeof(uint16_t));
+    float* reach = reinterpret_cast<float*>(p);
+    p += up(n * sizeof(float));
+    float* ext = reinterpret_cast<float*>(p);
+    k_db_extent<<<1, 256, 0, stream>>>(sph, radius, n, ext);
+    k_db_reach<<<(n + 255) / 256, 256, 0, stream>>>(radius, n, ext, reach);
+    k_db_build<<<(unsigned)((cells * 32 + 255) / 256), 256, 0, stream>>>(sph, radius, n, reach, count, list);
+    out->count = count;
+    out->list = list;
+    out->reach = reach;
+    out->n = n;
     return cudaGetLastError();
 }
 

@@ -25,7 +25,8 @@ atx_status SceneStore::upload(const atx_sphere* s, uint32_t n, const atx_materia
 {
     if ((n && !s) || (nm && !m) || (nl && !l)) return fail(ATX_ERR_INVALID_ARG, "set_scene: null array");
     if (n > 0 && nm == 0) return fail(ATX_ERR_INVALID_ARG, "set_scene: spheres need at least one material");
-    for (DeviceBuffer* b : {&this->sph, &sph_mat, &sph_rad, &mat, &lights, &bvh, &lbuf}) b->use_stream_order(order);
+    for (DeviceBuffer* b : {&this->sph, &sph_mat, &sph_rad, &mat, &lights, &bvh, &lbuf, &dbuf})
+        b->use_stream_order(order);
 
     std::vector<float4> sph(n);
     std::vector<int32_t> smat(n);
@@ -102,6 +103,15 @@ atx_status SceneStore::upload(const atx_sphere* s, uint32_t n, const atx_materia
         view.lb = lv;
     } else {
         lbuf.reset();
+    }
+    // direction buffer for the extension rays of the brute-force tables
+    if (!view.use_bvh && n >= 1 && n <= kDbMaxSpheres) {
+        ATX_TRY(dbuf.ensure(db_bytes(n), budget, "direction buffer"));
+        DirBufferView dv{};
+        ATX_CUDA(db_build(view.sph, sph_rad.as<float>(), n, dbuf.get(), dbuf.bytes(), &dv, stream));
+        view.db = dv;
+    } else {
+        dbuf.reset();
     }
     ATX_CUDA(cudaStreamSynchronize(stream));
     return ATX_OK;

@@ -14,7 +14,7 @@ namespace atx {
 // Device-resident scene: sphere table (float4 centre + radius^2), clamped
 // material ids, radii (for BVH boxes), shading tables and the optional LBVH.
 struct SceneStore {
-    DeviceBuffer sph, sph_mat, sph_rad, mat, lights, bvh, lbuf;
+    DeviceBuffer sph, sph_mat, sph_rad, mat, lights, bvh, lbuf, dbuf;
     SceneView view{};
     uint32_t bvh_threshold = 0;
     uint32_t bvh_leaf = 0;
@@ -26,7 +26,7 @@ struct SceneStore {
     uint64_t device_bytes() const
     {
         return sph.bytes() + sph_mat.bytes() + sph_rad.bytes() + mat.bytes() + lights.bytes() + bvh.bytes() +
-               lbuf.bytes();
+               lbuf.bytes() + dbuf.bytes();
     }
 };
 

@@ -15,6 +15,7 @@
 #include <map>
 
 #include "lbvh.h"
+#include "light_buffer.h"
 
 namespace atx {
 
@@ -288,7 +289,12 @@ uint64_t Server::job_bytes(const atx_batch_scene& s, uint32_t bvh_threshold)
 {
     const uint64_t n = s.n_spheres;
     uint64_t b = up256(16 * n) + up256(4 * n) + up256(4 * n) + up256(48ull * s.n_materials) + up256(32ull * s.n_lights);
-    if (n >= (bvh_threshold ? bvh_threshold : kDefaultBvhThreshold) && n > 1) b += up256(lbvh_bytes((uint32_t)n));
+    const bool bvh = n >= (bvh_threshold ? bvh_threshold : kDefaultBvhThreshold) && n > 1;
+    if (bvh) b += up256(lbvh_bytes((uint32_t)n));
+    // light and direction buffers, as SceneStore::upload builds them
+    if (!bvh && n >= 1 && n <= kLbMaxSpheres && s.n_lights >= 1 && s.n_lights <= kLbMaxLights)
+        b += up256(lb_bytes(s.n_lights));
+    if (!bvh && n >= 1 && n <= kDbMaxSpheres) b += up256(db_bytes((uint32_t)n));
     const uint64_t px = (uint64_t)s.width * s.height;
     b += up256(16 * px) + up256(4 * px) + up256(8 * px);   // accumulator, image, primary hits
     return b;

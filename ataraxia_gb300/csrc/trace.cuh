@@ -380,12 +380,58 @@ __device__ __forceinline__ bool occluded_lb(const SceneView& sc, const float4* _
     return false;
 }
 
+// Nearest hit of an extension ray leaving sphere own: the spheres the
+// direction buffer lists for own and the cell of d, in index order (ties keep
+// the lowest index, as in the brute-force loop), or the whole table when own
+// is not covered, o lies beyond own's reach, the cell overflowed or d is
+// degenerate.
+template <bool SMEM>
+__device__ __forceinline__ int32_t nearest_db(const SceneView& sc, const float4* __restrict__ sph, uint32_t own,
+                                              float3 o, float3 d, float& tmin)
+{
+    uint32_t cnt = kLbAll, slot = 0u;
+    if (own < sc.db.n) {
+        const float4 c = __ldg(&sc.sph[own]);
+        const float3 e = mk3(o.x - c.x, o.y - c.y, o.z - c.z);
+        const float reach = __ldg(&sc.db.reach[own]);
+        const int cell = dot3(e, e) <= reach * reach ? lb_cell(d) : -1;
+        if (cell >= 0) {
+            slot = own * kLbCells + (uint32_t)cell;
+            cnt = __ldg(&sc.db.count[slot]);
+        }
+    }
+    if (cnt == kLbAll) return nearest_brute<SMEM>(sph, sc.n_sph, o, d, tmin);
+    const float a = dot3(d, d);
+    const uint16_t* lst = sc.db.list + (size_t)slot * kLbMaxList;
+    int32_t best = -1;
+    float tm = kFltMax;
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t i = __ldg(&lst[k]);
+        float t;
+        if (sphere_t(table_sphere<SMEM>(sph, i), o, d, a, t) && t > 0.0f && t < tm) {
+            tm = t;
+            best = (int32_t)i;
+        }
+    }
+    tmin = tm;
+    return best;
+}
+
 template <int IS>
 __device__ __forceinline__ int32_t scene_nearest(const SceneView& sc, const float4* sph, float3 o, float3 d,
                                                  float& tmin)
 {
     if (IS == kIsBvh) return bvh_nearest(sc, o, d, tmin);
     return nearest_brute<IS == kIsSmem>(sph, sc.n_sph, o, d, tmin);
+}
+
+// Nearest hit of a ray leaving sphere own (~0u: from elsewhere).
+template <int IS>
+__device__ __forceinline__ int32_t scene_nearest_from(const SceneView& sc, const float4* sph, uint32_t own, float3 o,
+                                                      float3 d, float& tmin)
+{
+    if (IS != kIsBvh && sc.db.n != 0u) return nearest_db<IS == kIsSmem>(sc, sph, own, o, d, tmin);
+    return scene_nearest<IS>(sc, sph, o, d, tmin);
 }
 
 template <int IS>

@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t idx = base + threadIdx.x;
         bool push_next = false, push_sh = false, lit = false;
-        uint32_t pid = 0u, seed = 0u, j = 0u;
+        uint32_t pid = 0u, seed = 0u, j = 0u, own = ~0u;   // own: the sphere the ray leaves
         float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o, lc = o;
         float4 sho = make_float4(0.f, 0.f, 0.f, 0.f), shd = sho, shc = sho;
 
@@ -213,6 +213,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
                 o = mk3(ro.x, ro.y, ro.z);
                 seed = __float_as_uint(ro.w);
                 d = mk3(rd.x, rd.y, rd.z);
+                own = __float_as_uint(rd.w);
                 thr = mk3(tt.x, tt.y, tt.z);
             }
             seed += (uint32_t)bounce;
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
                 tmin = __uint_as_float(pr.x);
                 hit = (int32_t)pr.y;
             } else {
-                hit = scene_nearest<IS>(sc, sph, o, d, tmin);
+                hit = scene_nearest_from<IS>(sc, sph, own, o, d, tmin);
             }
             bool touch = false;
             float3 add = mk3(0.f, 0.f, 0.f);
@@ -280,6 +281,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
                     if (!(pcg_float(seed) > p)) {
                         thr = divs3(thr, p);
                         d = (metallic > 0.0f) ? sample_ggx(nrm, rough, seed) : sample_cosine(nrm, seed);
+                        own = (uint32_t)hit;   // the next ray leaves this sphere
                         push_next = true;
                     }
                 }
@@ -307,7 +309,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
         if (push_next) {
             qout[sn] = pid;
             ws.ray_o[pid] = make_float4(o.x, o.y, o.z, __uint_as_float(seed));
-            ws.ray_d[pid] = make_float4(d.x, d.y, d.z, 0.0f);
+            ws.ray_d[pid] = make_float4(d.x, d.y, d.z, __uint_as_float(own));
             ws.thr[pid] = make_float4(thr.x, thr.y, thr.z, 0.0f);
         }
     }

@@ -68,6 +68,21 @@ struct LightBufferView {
     uint32_t n_lights;       // 0: no light buffer
 };
 
+// Direction buffer for the extension rays of the brute-force tables (ray
+// classification by origin sphere and direction, in the spirit of Arvo and
+// Kirk's ray classification, 1987): for each sphere a cube of direction cells
+// as the light buffer's, and for each cell the spheres a ray leaving that
+// sphere in a direction of the cell can hit (built by light_buffer.cu).
+// Every extension ray after the first bounce leaves the sphere its path last
+// hit, so its nearest hit tests the spheres of one cell.
+constexpr uint32_t kDbMaxSpheres = 1024;   // 100 KB of cells per sphere
+struct DirBufferView {
+    const uint8_t* count;    // [n * kLbCells] spheres listed, or kLbAll
+    const uint16_t* list;    // [n * kLbCells * kLbMaxList] sphere indices, ascending
+    const float* reach;      // [n] the lists hold for ray origins within reach of the sphere's centre
+    uint32_t n;              // spheres covered; 0: no direction buffer
+};
+
 // Shadow-ray records carry the sphere the ray leaves from and the light it
 // goes to in one word: sphere in the low 26 bits, light in the high 6 (only
 // read when the light buffer, at most 64 lights, is in use).
@@ -89,6 +104,7 @@ struct SceneView {
     uint32_t use_bvh;         // 1: traverse bvh instead of the brute-force loop
     BvhView bvh;
     LightBufferView lb;       // shadow-ray cells of the brute-force tables (lb.n_lights 0: none)
+    DirBufferView db;         // extension-ray cells of the brute-force tables (db.n 0: none)
     uint64_t light_mod;       // fastmod_multiplier(n_lights): x % n_lights by multiplication
 };
 

@@ -51,3 +51,16 @@ def frac_outside(a: np.ndarray, ref: np.ndarray, rel: float = 1e-3, floor: float
     """Fraction of pixels whose rgb differs from ref by more than rel (relative to max(|ref|, floor))."""
     d = np.abs(a[:, :3].astype(np.float64) - ref[:, :3]) / np.maximum(np.abs(ref[:, :3]), floor)
     return float((d.max(axis=1) > rel).mean())
+
+
+def job_bytes_bound(sc):
+    """Upper bound of a served job's device bytes: accumulator, image and primary hits, scene
+    tables, and the LBVH (512 spheres and up) or the light and direction buffers (below)."""
+    n, nl = len(sc.spheres), len(sc.lights)
+    px = sc.width * sc.height
+    tables = 24 * n + 48 * len(sc.materials) + 32 * nl + 8 * 256
+    bvh = 200 * n if n >= 512 else 0
+    cells = 6 * 16 * 16 * 65          # per light / per sphere: a count and 32 indices per direction cell
+    lb = cells * nl + 2048 if n < 512 and 1 <= nl <= 64 else 0
+    db = cells * n + 2048 if n < 512 else 0
+    return tables + bvh + lb + db + 28 * px + 512

@@ -177,9 +177,9 @@ def _cone_scene(kind):
     st = scenes.Stream(7, "cone-" + kind)
     mats = scenes.draw_materials(st, 8)
     if kind == "far_narrow":     # distant camera, 3 deg: most primary rays pass within float error of a sphere
-        n = 600
+        n = 500                  # below the LBVH threshold: brute-force tables with their buffers
         c = st.uniform(3 * n, -5, 5).reshape(n, 3)
-        r = st.uniform(n, 0.05, 0.4)
+        r = st.uniform(n, 0.05, 0.45)
         cam, look, fov, far = (0.0, 30.0, 400.0), (0.0, -30.0, -400.0), 3.0, 1000.0
         lts = scenes.draw_lights(st, 4, 8.0)
     elif kind == "inside":       # camera inside a large sphere, small spheres around it and behind it

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from ataraxia_gb300 import Camera, Renderer, Server, Settings, scenes
-from tests.helpers import bit_mismatches
+from tests.helpers import bit_mismatches, job_bytes_bound
 
 pytestmark = pytest.mark.gpu
 
@@ -56,7 +56,7 @@ def test_budget_bounds_device_memory_and_concurrent_submitters():
     jobs = mix(16, scale=4, seed=9)
     from ataraxia_gb300 import _native as N
 
-    per = max(N_bytes(sc) for sc, _ in jobs)
+    per = max(job_bytes_bound(sc) for sc, _ in jobs)
     budget = 3 * per
     with Server(hbm_budget_bytes=budget, pass_spp=4) as s:
         ids, lock = [], threading.Lock()
@@ -79,17 +79,6 @@ def test_budget_bounds_device_memory_and_concurrent_submitters():
         assert peak <= budget
         for j, target in ids:
             assert s.poll(j)["frames_done"] == target
-
-
-def N_bytes(sc):
-    """Upper bound of a job's device bytes (accumulator + image + tables + LBVH)."""
-    from ataraxia_gb300 import _native as N  # noqa: F401
-
-    n = len(sc.spheres)
-    px = sc.width * sc.height
-    tables = 24 * n + 48 * len(sc.materials) + 32 * len(sc.lights) + 8 * 256
-    bvh = 200 * n if n >= 512 else 0
-    return tables + bvh + 28 * px + 512
 
 
 def test_camera_change_while_queued_and_while_active():

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from ataraxia_gb300 import AtxError, Camera, Server, Settings, scenes
+from tests.helpers import job_bytes_bound
 
 
 def job_scene(w=32, h=16, n=20, seed=0):
@@ -36,7 +37,7 @@ def test_admission_respects_hbm_budget():
     from ataraxia_gb300 import _native as N
     import ctypes as C
 
-    per_job = 64 * 64 * 20 + 4096          # accumulator + image + tables, rounded up
+    per_job = job_bytes_bound(sc)
     budget = int(2.5 * per_job)
     peak = {"bytes": 0, "active": 0}
     with Server(host_executor=True, hbm_budget_bytes=budget, pass_spp=2) as s:
