@@ -186,10 +186,13 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
     // first bounce with per-(pixel, light) shadow rays: the light of a sample
     // is added here when k_shadow found it visible from the pixel's hit
     const bool vis = FIRST && SHARED && wave_light_vis(job, sc.n_lights);
+    // with a light buffer the shadow ray is tested here, right after the
+    // shading (a lookup and a few spheres), instead of through k_shadow
+    const bool inline_shadow = IS != kIsBvh && sc.lb.n_lights != 0u;
 
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t idx = base + threadIdx.x;
-        bool push_next = false, push_sh = false, lit = false;
+        bool push_next = false, push_sh = false, lit = false, traced_sh = false;
         uint32_t pid = 0u, seed = 0u, j = 0u, own = ~0u;   // own: the sphere the ray leaves
         float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o, lc = o;
         float4 sho = make_float4(0.f, 0.f, 0.f, 0.f), shd = sho, shc = sho;
@@ -263,6 +266,11 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
                     if (vis) {
                         lit = ((ws.vis[j] >> li) & 1u) != 0u;
                         lc = c;
+                    } else if (inline_shadow) {   // Renderer.cu:348-352
+                        const float3 so = add3(pos, muls3(nrm, kOffset));
+                        lit = sc.n_sph == 0u || !occluded_lb<SMEM>(sc, sph, li, so, L, dist2);
+                        lc = c;
+                        traced_sh = true;
                     } else {
                         const float3 so = add3(pos, muls3(nrm, kOffset));
                         sho = make_float4(so.x, so.y, so.z, dist2);
@@ -290,15 +298,24 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
                 float3 c = add3(mk3(0.f, 0.f, 0.f), add);
                 if (lit) c = add3(c, lc);   // as k_shadow adds it: after the emission
                 ws.col[pid] = make_float4(c.x, c.y, c.z, 0.0f);
-            } else if (touch) {
+            } else if (touch || lit) {
+                // emission of bounce b, then its light (the order k_shadow adds it in)
                 float4 c = ws.col[pid];
-                c.x = c.x + add.x;
-                c.y = c.y + add.y;
-                c.z = c.z + add.z;
+                if (touch) {
+                    c.x = c.x + add.x;
+                    c.y = c.y + add.y;
+                    c.z = c.z + add.z;
+                }
+                if (lit) {
+                    c.x = c.x + lc.x;
+                    c.y = c.y + lc.y;
+                    c.z = c.z + lc.z;
+                }
                 ws.col[pid] = c;
             }
         }
 
+        if (inline_shadow) warp_push(&ws.counters[2 * bounce + 1], traced_sh);   // count the traced rays
         const uint32_t ss = warp_push(&ws.counters[2 * bounce + 1], push_sh);
         if (push_sh) {
             ws.sh_o[ss] = sho;
@@ -654,7 +671,7 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
                     end(kFamExtend);
                     ++nl;
                 }
-                if (vis && b == 0) continue;
+                if ((vis && b == 0) || sc.lb.n_lights != 0u) continue;   // tested in k_extend
                 begin(kFamShadow);
                 k_shadow<IS, false><<<shape.blocks_shadow, shape.threads, sm, stream>>>(sc, ws, b);
                 end(kFamShadow);
