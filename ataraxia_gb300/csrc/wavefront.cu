@@ -1,24 +1,29 @@
 // Wavefront path tracer for sm_103a: the reference's per-pixel loop
 // (Renderer.cu:287-387) split into queue-driven stages.
 //
-//   k_extend<FIRST>  bounce b: (FIRST: generate the primary ray, Camera.cpp:
-//                    161-195) nearest hit over the sphere table staged in
-//                    shared memory, shading, light pick and the shadow ray,
-//                    Russian roulette and the next direction.  Survivors go to
-//                    the next extension queue, shadow rays to the shadow
-//                    queue, both through warp-aggregated atomics.
-//   k_shadow         any-hit over the shadow queue of bounce b; unoccluded
-//                    rays add their contribution to the path colour.
+//   k_primary        primary nearest hit once per pixel (Camera.cpp:161-195
+//                    for the ray), shared by the pixel's samples; queues the
+//                    first bounce's (pixel, light) shadow rays.
+//   k_first          bounce 0 over (hit pixel, sample): shading, light pick
+//                    and the shadow ray, Russian roulette and the next
+//                    direction.  Survivors go to the extension queue.
+//   k_bounce         bounce b >= 1: nearest hit, then the same shading, with
+//                    the block's hits gathered in shared memory first.
+//   k_shadow         any-hit over a shadow queue: the first bounce's (pixel,
+//                    light) rays, and per-sample shadow rays of scenes without
+//                    a light buffer (with one they are tested in k_first /
+//                    k_bounce right after the shading).
 //   k_accumulate     adds the wave's per-sample colours to the float4
 //                    accumulator in frame order (Renderer.cu:165) and packs
 //                    the RGBA8 image (Renderer.cu:166-168).
 //
-// Order of the colour sums is the reference's: emission of bounce b (extend b),
-// light of bounce b (shadow b), then bounce b+1.  Each path owns its colour
-// row, so no float atomics are needed and results do not depend on queue
-// order.  The random stream is consumed per path exactly as the reference
-// does: seed += b at the top of the bounce, PcgHash(seed) (no advance) for the
-// light, one PcgFloat for roulette and two for the new direction.
+// Queues are filled through warp-aggregated atomics.  Order of the colour
+// sums is the reference's: emission of bounce b, light of bounce b, then
+// bounce b+1.  Each path owns its colour row, so no float atomics are needed
+// and results do not depend on queue order.  The random stream is consumed
+// per path exactly as the reference does: seed += b at the top of the bounce,
+// PcgHash(seed) (no advance) for the light, one PcgFloat for roulette and two
+// for the new direction.
 #include <type_traits>
 
 #include "wavefront.h"
@@ -30,9 +35,9 @@ namespace {
 
 constexpr uint32_t kFull = 0xffffffffu;
 constexpr int kThreads = 256;
-// k_extend's block: its shading code sets the register count.  4 blocks of
-// 256 threads per SM (64 registers, no spills in the shared-memory variant)
-// beat 6 of 192 (56 registers, 44 bytes spilled) by 0.6% on the medium scene.
+// k_first's and k_bounce's block: the shading code sets the register count.
+// 4 blocks of 256 threads per SM (64 registers) beat 6 of 192 (56 registers)
+// and 3 of 256 (80 registers) on the medium scene.
 constexpr int kExtendThreads = 256;
 constexpr int kExtendBlocksPerSm = 4;
 
@@ -162,20 +167,193 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
     }
 }
 
-// SHARED (first bounce only): take the nearest hit from k_primary's per-pixel
-// record instead of tracing the primary ray again.
-template <bool FIRST, int IS, bool SHARED>
+// What shading a hit leaves behind (Renderer.cu:318-384 for one bounce).
+struct Shaded {
+    float3 add;        // emission (Renderer.cu:329-333), when touch
+    float3 lc;         // the light's contribution, when lit
+    bool touch, lit;
+    bool traced_sh;    // a shadow ray was tested here (light buffer)
+    bool push_sh;      // a shadow ray goes to k_shadow: sho, shd, shc
+    bool push_next;    // the path continues: o, d, thr, own, seed
+    float4 sho, shd, shc;
+};
+
+// Shading of the hit (sphere hit at tmin) of path pid's ray (o, d) with
+// throughput thr at bounce `bounce` (seed already advanced by it): emission,
+// the light pick and its BRDF term, the shadow ray (visibility bit j for vis,
+// tested here through the light buffer for INL, else a record for k_shadow),
+// roulette and the next direction, which replace o, d, thr, own and advance
+// seed.
+template <bool SMEM, bool INL>
+__device__ __forceinline__ void shade_hit(const SceneView& sc, const float4* sph, const WaveState& ws, uint32_t pid,
+                                          int32_t hit, float tmin, float3& o, float3& d, float3& thr, uint32_t& own,
+                                          uint32_t& seed, bool last, bool vis, uint32_t j, Shaded& r)
+{
+    const float4 s = table_sphere<SMEM>(sph, (uint32_t)hit);
+    float3 pos, nrm;
+    ray_hit(s, o, d, tmin, pos, nrm);
+    const int32_t mi = __ldg(&sc.sph_mat[hit]);
+    const float4* mrow = reinterpret_cast<const float4*>(sc.mat + mi);
+    const float4 m0 = __ldg(mrow), m1 = __ldg(mrow + 1), m2 = __ldg(mrow + 2);
+    const float3 albedo = mk3(m0.x, m0.y, m0.z);
+    const float rough = m0.w;
+    const float3 f0 = mk3(m1.x, m1.y, m1.z);
+    const float metallic = m1.w;
+
+    if (m2.w > 0.0f) {  // Renderer.cu:329-333
+        r.add = mul3(mk3(m2.x, m2.y, m2.z), thr);
+        r.touch = true;
+    }
+    // glm::mix(F0, albedo, metallic), Renderer.cu:335
+    const float3 base = add3(muls3(f0, 1.0f - metallic), muls3(albedo, metallic));
+
+    if (sc.n_lights > 0u) {  // Renderer.cu:338-369
+        const uint32_t li = light_pick(sc, seed);
+        float3 L;
+        float dist2;
+        const float4 l1 = light_dir(sc, li, pos, L, dist2);
+        const float3 f = cook_torrance(albedo, base, metallic, rough, nrm, neg3(d), L);
+        const float3 c = mul3(mul3(mk3(l1.x, l1.y, l1.z), f), thr);
+        if (vis) {
+            r.lit = ((ws.vis[j] >> li) & 1u) != 0u;
+            r.lc = c;
+        } else if (INL) {   // Renderer.cu:348-352
+            const float3 so = add3(pos, muls3(nrm, kOffset));
+            r.lit = sc.n_sph == 0u || !occluded_lb<SMEM>(sc, sph, li, so, L, dist2);
+            r.lc = c;
+            r.traced_sh = true;
+        } else {
+            const float3 so = add3(pos, muls3(nrm, kOffset));
+            r.sho = make_float4(so.x, so.y, so.z, dist2);
+            r.shd = make_float4(L.x, L.y, L.z, __uint_as_float(pid));
+            // w: the sphere the shadow ray leaves from (tested first by the
+            // LBVH walk) and the light (for the light buffer)
+            r.shc = make_float4(c.x, c.y, c.z, __uint_as_float(shadow_tag((uint32_t)hit, li)));
+            r.push_sh = true;
+        }
+    }
+
+    if (!last) {  // Renderer.cu:371-384
+        thr = mul3(thr, albedo);
+        o = add3(pos, muls3(nrm, kOffset));
+        const float p = gmax(0.1f, gmin(1.0f, length3(thr)));
+        if (!(pcg_float(seed) > p)) {
+            thr = divs3(thr, p);
+            d = (metallic > 0.0f) ? sample_ggx(nrm, rough, seed) : sample_cosine(nrm, seed);
+            own = (uint32_t)hit;   // the next ray leaves this sphere
+            r.push_next = true;
+        }
+    }
+}
+
+// Queue pushes after shading (all 32 lanes of the warp call it).
+template <bool INL>
+__device__ __forceinline__ void push_shaded(const WaveState& ws, uint32_t* qout, int bounce, uint32_t pid,
+                                            const Shaded& r, float3 o, float3 d, float3 thr, uint32_t own,
+                                            uint32_t seed)
+{
+    if (INL) {
+        warp_push(&ws.counters[2 * bounce + 1], r.traced_sh);   // count the traced rays
+    } else {
+        const uint32_t ss = warp_push(&ws.counters[2 * bounce + 1], r.push_sh);
+        if (r.push_sh) {
+            ws.sh_o[ss] = r.sho;
+            ws.sh_d[ss] = r.shd;
+            ws.sh_c[ss] = r.shc;
+        }
+    }
+    const uint32_t sn = warp_push(&ws.counters[2 * (bounce + 1)], r.push_next);
+    if (r.push_next) {
+        qout[sn] = pid;
+        ws.ray_o[pid] = make_float4(o.x, o.y, o.z, __uint_as_float(seed));
+        ws.ray_d[pid] = make_float4(d.x, d.y, d.z, __uint_as_float(own));
+        ws.thr[pid] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+    }
+}
+
+// The first bounce over (pixel, sample) paths.  SHARED: the nearest hit comes
+// from k_primary's per-pixel record instead of tracing the primary ray again,
+// and idx enumerates (hit pixel, sample).
+// INL: the scene has a light buffer and shadow rays are tested right after
+// the shading (a lookup and a few spheres) instead of through k_shadow.
+template <int IS, bool SHARED, bool INL>
 __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
-    k_extend(SceneView sc, CameraView cam, WaveState ws, WaveJob job, int bounce)
+    k_first(SceneView sc, CameraView cam, WaveState ws, WaveJob job)
 {
     constexpr bool SMEM = IS == kIsSmem;
     extern __shared__ float4 s_sph[];
-    const uint32_t n = !FIRST ? ws.counters[2 * bounce]
-                     : SHARED ? ws.counters[2 * ((uint32_t)job.max_bounces + 1u)] * job.spp
+    const uint32_t n = SHARED ? ws.counters[2 * ((uint32_t)job.max_bounces + 1u)] * job.spp
                               : job.n_pixels * job.spp;
     if (blockIdx.x * blockDim.x >= n) return;
     if (SMEM) stage_spheres(sc, s_sph);
     const float4* sph = SMEM ? s_sph : sc.sph;
+    const bool last = 1 >= job.max_bounces;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // per-(pixel, light) shadow rays: the light of a sample is added here when
+    // k_shadow found it visible from the pixel's hit
+    const bool vis = SHARED && wave_light_vis(job, sc.n_lights);
+
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t idx = base + threadIdx.x;
+        Shaded r{};
+        uint32_t pid = 0u, seed = 0u, own = ~0u;
+        float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o;
+        if (idx < n) {
+            const uint32_t j = SHARED ? ws.hitq[idx / job.spp] : idx / job.spp;   // path ids stay pixel-major
+            const uint32_t smp = idx % job.spp;
+            pid = j * job.spp + smp;
+            const uint32_t p = job.pixel0 + j;
+            o = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
+            d = primary_dir(cam, p % cam.width, p / cam.width);
+            thr = mk3(1.f, 1.f, 1.f);
+            seed = p * (job.frame0 + smp);   // bounce 0: seed += 0
+            float tmin;
+            int32_t hit;
+            if (SHARED) {
+                const uint2 pr = job.prim_cache ? job.prim_cache[job.pixel0 + j] : ws.prim[j];
+                tmin = __uint_as_float(pr.x);
+                hit = (int32_t)pr.y;
+            } else {
+                hit = scene_nearest<IS>(sc, sph, o, d, tmin);
+            }
+            if (hit < 0) {
+                if (job.sky) {  // Renderer.cu:311-316
+                    r.add = mul3(mk3(0.6f, 0.7f, 0.9f), thr);
+                    r.touch = true;
+                }
+            } else {
+                shade_hit<SMEM, INL>(sc, sph, ws, pid, hit, tmin, o, d, thr, own, seed, last, vis, j, r);
+            }
+            float3 c = add3(mk3(0.f, 0.f, 0.f), r.add);
+            if (r.lit) c = add3(c, r.lc);   // as k_shadow adds it: after the emission
+            ws.col[pid] = make_float4(c.x, c.y, c.z, 0.0f);
+        }
+        push_shaded<INL>(ws, ws.q[1], 0, pid, r, o, d, thr, own, seed);
+    }
+}
+
+// Bounce b >= 1 over the extension queue, in rounds of two phases per block.
+// Intersect: each thread takes rays from its grid-stride share of the queue;
+// a miss is finished at once (sky), a hit goes to the block's hit list in
+// shared memory (path, sphere, t).  Shade: once the list holds a block's
+// worth of hits, or the queue is done, every thread shades one.  Most rays
+// after the first bounce leave the scene, so shading (the larger part of the
+// work) then runs on full warps instead of on the few lanes that hit.
+template <int IS, bool INL>
+__global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
+    k_bounce(SceneView sc, WaveState ws, WaveJob job, int bounce)
+{
+    constexpr bool SMEM = IS == kIsSmem;
+    constexpr uint32_t kCap = 2u * kExtendThreads;
+    extern __shared__ float4 s_sph[];
+    __shared__ uint32_t h_pid[kCap], h_id[kCap];
+    __shared__ float h_t[kCap];
+    __shared__ uint32_t h_n;
+    const uint32_t n = ws.counters[2 * bounce];
+    if (blockIdx.x * blockDim.x >= n) return;
+    if (SMEM) stage_spheres(sc, s_sph);   // ends with a barrier
+    const float4* sph = SMEM ? s_sph : sc.sph;
+    if (threadIdx.x == 0) h_n = 0u;
 
     // select, not index: a runtime index into the parameter's array would
     // copy the whole WaveState to local memory
@@ -183,152 +361,81 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
     uint32_t* qout = (bounce & 1) ? ws.q[0] : ws.q[1];
     const bool last = bounce + 1 >= job.max_bounces;
     const uint32_t stride = gridDim.x * blockDim.x;
-    // first bounce with per-(pixel, light) shadow rays: the light of a sample
-    // is added here when k_shadow found it visible from the pixel's hit
-    const bool vis = FIRST && SHARED && wave_light_vis(job, sc.n_lights);
-    // with a light buffer the shadow ray is tested here, right after the
-    // shading (a lookup and a few spheres), instead of through k_shadow
-    const bool inline_shadow = IS != kIsBvh && sc.lb.n_lights != 0u;
+    uint32_t base = blockIdx.x * blockDim.x;
+    __syncthreads();
 
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        const uint32_t idx = base + threadIdx.x;
-        bool push_next = false, push_sh = false, lit = false, traced_sh = false;
-        uint32_t pid = 0u, seed = 0u, j = 0u, own = ~0u;   // own: the sphere the ray leaves
-        float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o, lc = o;
-        float4 sho = make_float4(0.f, 0.f, 0.f, 0.f), shd = sho, shc = sho;
-
-        if (idx < n) {
-            if (FIRST) {
-                // SHARED: idx enumerates (hit pixel, sample); path ids stay pixel-major
-                j = SHARED ? ws.hitq[idx / job.spp] : idx / job.spp;
-                const uint32_t s = idx % job.spp;
-                pid = j * job.spp + s;
-                const uint32_t p = job.pixel0 + j;
-                o = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
-                d = primary_dir(cam, p % cam.width, p / cam.width);
-                thr = mk3(1.f, 1.f, 1.f);
-                seed = p * (job.frame0 + s);
-            } else {
+    for (;;) {   // ends: every round takes rays off the queue or hits off the list
+        while (base < n && h_n < blockDim.x) {   // block-uniform: base, h_n after the barrier
+            const uint32_t idx = base + threadIdx.x;
+            bool found = false;
+            uint32_t pid = 0u;
+            int32_t hit = -1;
+            float tmin = 0.0f;
+            if (idx < n) {
                 pid = qin[idx];
                 const float4 ro = ws.ray_o[pid];
                 const float4 rd = ws.ray_d[pid];
-                const float4 tt = ws.thr[pid];
-                o = mk3(ro.x, ro.y, ro.z);
-                seed = __float_as_uint(ro.w);
-                d = mk3(rd.x, rd.y, rd.z);
-                own = __float_as_uint(rd.w);
-                thr = mk3(tt.x, tt.y, tt.z);
-            }
-            seed += (uint32_t)bounce;
-
-            float tmin;
-            int32_t hit;
-            if (SHARED) {
-                const uint2 pr = job.prim_cache ? job.prim_cache[job.pixel0 + pid / job.spp] : ws.prim[pid / job.spp];
-                tmin = __uint_as_float(pr.x);
-                hit = (int32_t)pr.y;
-            } else {
-                hit = scene_nearest_from<IS>(sc, sph, own, o, d, tmin);
-            }
-            bool touch = false;
-            float3 add = mk3(0.f, 0.f, 0.f);
-            if (hit < 0) {
-                if (job.sky) {  // Renderer.cu:311-316
-                    add = mul3(mk3(0.6f, 0.7f, 0.9f), thr);
-                    touch = true;
-                }
-            } else {
-                const float4 s = table_sphere<SMEM>(sph, (uint32_t)hit);
-                float3 pos, nrm;
-                ray_hit(s, o, d, tmin, pos, nrm);
-                const int32_t mi = __ldg(&sc.sph_mat[hit]);
-                const float4* mrow = reinterpret_cast<const float4*>(sc.mat + mi);
-                const float4 m0 = __ldg(mrow), m1 = __ldg(mrow + 1), m2 = __ldg(mrow + 2);
-                const float3 albedo = mk3(m0.x, m0.y, m0.z);
-                const float rough = m0.w;
-                const float3 f0 = mk3(m1.x, m1.y, m1.z);
-                const float metallic = m1.w;
-
-                if (m2.w > 0.0f) {  // Renderer.cu:329-333
-                    add = mul3(mk3(m2.x, m2.y, m2.z), thr);
-                    touch = true;
-                }
-                // glm::mix(F0, albedo, metallic), Renderer.cu:335
-                const float3 base = add3(muls3(f0, 1.0f - metallic), muls3(albedo, metallic));
-
-                if (sc.n_lights > 0u) {  // Renderer.cu:338-369
-                    const uint32_t li = light_pick(sc, seed);
-                    float3 L;
-                    float dist2;
-                    const float4 l1 = light_dir(sc, li, pos, L, dist2);
-                    const float3 f = cook_torrance(albedo, base, metallic, rough, nrm, neg3(d), L);
-                    const float3 c = mul3(mul3(mk3(l1.x, l1.y, l1.z), f), thr);
-                    if (vis) {
-                        lit = ((ws.vis[j] >> li) & 1u) != 0u;
-                        lc = c;
-                    } else if (inline_shadow) {   // Renderer.cu:348-352
-                        const float3 so = add3(pos, muls3(nrm, kOffset));
-                        lit = sc.n_sph == 0u || !occluded_lb<SMEM>(sc, sph, li, so, L, dist2);
-                        lc = c;
-                        traced_sh = true;
-                    } else {
-                        const float3 so = add3(pos, muls3(nrm, kOffset));
-                        sho = make_float4(so.x, so.y, so.z, dist2);
-                        shd = make_float4(L.x, L.y, L.z, __uint_as_float(pid));
-                        // w: the sphere the shadow ray leaves from (tested first by the
-                        // LBVH walk) and the light (for the light buffer)
-                        shc = make_float4(c.x, c.y, c.z, __uint_as_float(shadow_tag((uint32_t)hit, li)));
-                        push_sh = true;
-                    }
-                }
-
-                if (!last) {  // Renderer.cu:371-384
-                    thr = mul3(thr, albedo);
-                    o = add3(pos, muls3(nrm, kOffset));
-                    const float p = gmax(0.1f, gmin(1.0f, length3(thr)));
-                    if (!(pcg_float(seed) > p)) {
-                        thr = divs3(thr, p);
-                        d = (metallic > 0.0f) ? sample_ggx(nrm, rough, seed) : sample_cosine(nrm, seed);
-                        own = (uint32_t)hit;   // the next ray leaves this sphere
-                        push_next = true;
-                    }
-                }
-            }
-            if (FIRST) {
-                float3 c = add3(mk3(0.f, 0.f, 0.f), add);
-                if (lit) c = add3(c, lc);   // as k_shadow adds it: after the emission
-                ws.col[pid] = make_float4(c.x, c.y, c.z, 0.0f);
-            } else if (touch || lit) {
-                // emission of bounce b, then its light (the order k_shadow adds it in)
-                float4 c = ws.col[pid];
-                if (touch) {
+                hit = scene_nearest_from<IS>(sc, sph, __float_as_uint(rd.w), mk3(ro.x, ro.y, ro.z),
+                                             mk3(rd.x, rd.y, rd.z), tmin);
+                found = hit >= 0;
+                if (!found && job.sky) {   // Renderer.cu:311-316: the path ends in the sky
+                    const float4 tt = ws.thr[pid];
+                    const float3 add = mul3(mk3(0.6f, 0.7f, 0.9f), mk3(tt.x, tt.y, tt.z));
+                    float4 c = ws.col[pid];
                     c.x = c.x + add.x;
                     c.y = c.y + add.y;
                     c.z = c.z + add.z;
+                    ws.col[pid] = c;
                 }
-                if (lit) {
-                    c.x = c.x + lc.x;
-                    c.y = c.y + lc.y;
-                    c.z = c.z + lc.z;
+            }
+            const uint32_t k = warp_push(&h_n, found);
+            if (found) {
+                h_pid[k] = pid;
+                h_id[k] = (uint32_t)hit;
+                h_t[k] = tmin;
+            }
+            base += stride;
+            __syncthreads();
+        }
+        const uint32_t nh = h_n;
+        if (nh == 0u) break;   // and the queue is done
+        const uint32_t take = min(nh, blockDim.x);
+        Shaded r{};
+        uint32_t pid = 0u, seed = 0u, own = ~0u;
+        float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o;
+        if (threadIdx.x < take) {
+            const uint32_t k = nh - take + threadIdx.x;
+            pid = h_pid[k];
+            const int32_t hit = (int32_t)h_id[k];
+            const float tmin = h_t[k];
+            const float4 ro = ws.ray_o[pid];
+            const float4 rd = ws.ray_d[pid];
+            const float4 tt = ws.thr[pid];
+            o = mk3(ro.x, ro.y, ro.z);
+            seed = __float_as_uint(ro.w) + (uint32_t)bounce;
+            d = mk3(rd.x, rd.y, rd.z);
+            thr = mk3(tt.x, tt.y, tt.z);
+            shade_hit<SMEM, INL>(sc, sph, ws, pid, hit, tmin, o, d, thr, own, seed, last, false, 0u, r);
+            if (r.touch || r.lit) {
+                // emission of bounce b, then its light (the order k_shadow adds it in)
+                float4 c = ws.col[pid];
+                if (r.touch) {
+                    c.x = c.x + r.add.x;
+                    c.y = c.y + r.add.y;
+                    c.z = c.z + r.add.z;
+                }
+                if (r.lit) {
+                    c.x = c.x + r.lc.x;
+                    c.y = c.y + r.lc.y;
+                    c.z = c.z + r.lc.z;
                 }
                 ws.col[pid] = c;
             }
         }
-
-        if (inline_shadow) warp_push(&ws.counters[2 * bounce + 1], traced_sh);   // count the traced rays
-        const uint32_t ss = warp_push(&ws.counters[2 * bounce + 1], push_sh);
-        if (push_sh) {
-            ws.sh_o[ss] = sho;
-            ws.sh_d[ss] = shd;
-            ws.sh_c[ss] = shc;
-        }
-        const uint32_t sn = warp_push(&ws.counters[2 * (bounce + 1)], push_next);
-        if (push_next) {
-            qout[sn] = pid;
-            ws.ray_o[pid] = make_float4(o.x, o.y, o.z, __uint_as_float(seed));
-            ws.ray_d[pid] = make_float4(d.x, d.y, d.z, __uint_as_float(own));
-            ws.thr[pid] = make_float4(thr.x, thr.y, thr.z, 0.0f);
-        }
+        push_shaded<INL>(ws, qout, bounce, pid, r, o, d, thr, own, seed);
+        __syncthreads();   // every thread has read its entry
+        if (threadIdx.x == 0) h_n = nh - take;
+        __syncthreads();
     }
 }
 
@@ -588,15 +695,19 @@ cudaError_t occupancy(int threads, size_t bytes, int* ext, int* sh, int* pr)
     if (bytes > 48 * 1024) {
         const int b = (int)bytes;
         const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-        cudaError_t e = cudaFuncSetAttribute(k_extend<true, IS, false>, a, b);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_extend<false, IS, false>, a, b);
+        cudaError_t e = cudaFuncSetAttribute(k_first<IS, false, false>, a, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bounce<IS, false>, a, b);
+        if constexpr (IS != kIsBvh) {
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_first<IS, false, true>, a, b);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bounce<IS, true>, a, b);
+        }
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_primary<IS>, a, b);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shadow<IS, false>, a, b);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shadow<IS, true>, a, b);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace<IS>, a, b);
         if (e != cudaSuccess) return e;
     }
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ext, k_extend<false, IS, false>, kExtendThreads, bytes);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ext, k_bounce<IS, false>, kExtendThreads, bytes);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(sh, k_shadow<IS, false>, threads, bytes);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(pr, k_primary<IS>, threads, bytes);
     return e;
@@ -640,6 +751,8 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
         const int g0 = grid_for(paths, kExtendThreads, shape.blocks_extend);
         const bool share = wave_shares_primary(job);
         const bool vis = wave_light_vis(job, sc.n_lights);
+        // a light buffer exists only for the brute-force tables
+        const bool inl = shape.mode != kIsBvh && sc.lb.n_lights != 0u;
         with_mode(shape.mode, [&](auto m) {
             constexpr int IS = decltype(m)::value;
             if (share) {
@@ -656,22 +769,33 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
                 }
                 // no sphere table needed: the nearest hit comes from k_primary
                 begin(kFamExtend);
-                k_extend<true, kIsGlobal, true><<<g0, kExtendThreads, 0, stream>>>(sc, cam, ws, job, 0);
+                if (inl) k_first<kIsGlobal, true, true><<<g0, kExtendThreads, 0, stream>>>(sc, cam, ws, job);
+                else k_first<kIsGlobal, true, false><<<g0, kExtendThreads, 0, stream>>>(sc, cam, ws, job);
                 end(kFamExtend);
             } else {
                 begin(kFamExtend);
-                k_extend<true, IS, false><<<g0, kExtendThreads, sm, stream>>>(sc, cam, ws, job, 0);
+                if constexpr (IS != kIsBvh) {
+                    if (inl) k_first<IS, false, true><<<g0, kExtendThreads, sm, stream>>>(sc, cam, ws, job);
+                    else k_first<IS, false, false><<<g0, kExtendThreads, sm, stream>>>(sc, cam, ws, job);
+                } else {
+                    k_first<IS, false, false><<<g0, kExtendThreads, sm, stream>>>(sc, cam, ws, job);
+                }
                 end(kFamExtend);
             }
             ++nl;
             for (int b = 0; b < bounces; ++b) {
                 if (b > 0) {
                     begin(kFamExtend);
-                    k_extend<false, IS, false><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, cam, ws, job, b);
+                    if constexpr (IS != kIsBvh) {
+                        if (inl) k_bounce<IS, true><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
+                        else k_bounce<IS, false><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
+                    } else {
+                        k_bounce<IS, false><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
+                    }
                     end(kFamExtend);
                     ++nl;
                 }
-                if ((vis && b == 0) || sc.lb.n_lights != 0u) continue;   // tested in k_extend
+                if ((vis && b == 0) || inl) continue;   // tested in k_first / k_bounce
                 begin(kFamShadow);
                 k_shadow<IS, false><<<shape.blocks_shadow, shape.threads, sm, stream>>>(sc, ws, b);
                 end(kFamShadow);
