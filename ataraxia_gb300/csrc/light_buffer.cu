@@ -30,6 +30,10 @@ constexpr double kK = 1.2207031e-3;   // 5 sqrt(2^-24) per unit of distance, as 
 
 uint64_t up(uint64_t x) { return (x + 255u) & ~uint64_t(255u); }
 
+// Scratch for the cell cones (k_cell_cones) at the end of both buffers.
+constexpr uint64_t kConeBytes = ((kLbCells * sizeof(float4) + 255u) & ~uint64_t(255u)) +
+                                ((kLbCells * sizeof(float) + 255u) & ~uint64_t(255u));
+
 // Unit direction of face f (0..5: +x, -x, +y, -y, +z, -z) at in-face
 // coordinates (u, v): the axes trace.cuh lb_cell divides by the face axis
 // (face x: y, z; face y: x, z; face z: x, y).
@@ -46,6 +50,25 @@ __device__ float3 face_dir(uint32_t f, float u, float v)
 }
 
 __device__ float dotf3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// Bounding cone of every direction cell, widened by 2e-4 rad (1e-4 for the
+// lookup's rounding, the rest for the build's arithmetic): axis and the
+// cosine of the half-angle in cone[cell], its sine in cone_sin[cell].  The
+// farthest points of a cell from its centre are its corners.
+__global__ void k_cell_cones(float4* cone, float* cone_sin)
+{
+    const uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= kLbCells) return;
+    const uint32_t f = cell / (kLbRes * kLbRes), i = (cell / kLbRes) % kLbRes, j = cell % kLbRes;
+    const float u0 = 2.0f * i / kLbRes - 1.0f, u1 = 2.0f * (i + 1) / kLbRes - 1.0f;
+    const float v0 = 2.0f * j / kLbRes - 1.0f, v1 = 2.0f * (j + 1) / kLbRes - 1.0f;
+    const float3 ctr = face_dir(f, 0.5f * (u0 + u1), 0.5f * (v0 + v1));
+    float cmin = 1.0f;
+    for (int k = 0; k < 4; ++k) cmin = fminf(cmin, dotf3(ctr, face_dir(f, (k & 1) ? u1 : u0, (k & 2) ? v1 : v0)));
+    const float hw = acosf(fminf(1.0f, cmin)) + 2e-4f;
+    cone[cell] = make_float4(ctr.x, ctr.y, ctr.z, cosf(hw));
+    cone_sin[cell] = sinf(hw);
+}
 
 // dcap[l] = max over spheres of |c - light| + r, plus 1: every shadow-ray
 // origin (a hit point lifted by 1e-4) lies within it.
@@ -71,25 +94,19 @@ __global__ void k_lb_dcap(const float4* __restrict__ sph, const float* __restric
 
 // One warp per (light, cell); the lanes test 32 spheres at a time and append
 // the listed ones in index order.  Float arithmetic with every bound rounded
-// towards listing: the cell's half-angle widened by 2e-4 rad (1e-4 for the
-// lookup's rounding, the rest for this arithmetic), sin(beta) rounded up,
-// cos(beta) taken from it, a 2e-5 slack on the final comparison.
+// towards listing: the widened cell cone, sin(beta) rounded up, cos(beta)
+// taken from it, a 2e-5 slack on the final comparison.
 __global__ void k_lb_build(const float4* __restrict__ sph, const float* __restrict__ rad, uint32_t n,
                            const DevLight* __restrict__ lights, uint32_t nl, const float* __restrict__ dcap,
-                           uint8_t* count, uint16_t* list)
+                           const float4* __restrict__ cone, const float* __restrict__ cone_sin, uint8_t* count,
+                           uint16_t* list)
 {
     const uint32_t id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
     if (id >= nl * kLbCells) return;   // whole warps: blockDim is a multiple of 32
     const uint32_t l = id / kLbCells, cell = id % kLbCells;
-    const uint32_t f = cell / (kLbRes * kLbRes), i = (cell / kLbRes) % kLbRes, j = cell % kLbRes;
-    const float u0 = 2.0f * i / kLbRes - 1.0f, u1 = 2.0f * (i + 1) / kLbRes - 1.0f;
-    const float v0 = 2.0f * j / kLbRes - 1.0f, v1 = 2.0f * (j + 1) / kLbRes - 1.0f;
-    const float3 ctr = face_dir(f, 0.5f * (u0 + u1), 0.5f * (v0 + v1));
-    // bounding cone of the cell: its farthest points from the centre are corners
-    float cmin = 1.0f;
-    for (int k = 0; k < 4; ++k) cmin = fminf(cmin, dotf3(ctr, face_dir(f, (k & 1) ? u1 : u0, (k & 2) ? v1 : v0)));
-    const float hw = acosf(fminf(1.0f, cmin)) + 2e-4f;
-    const float ch = cosf(hw), sh = sinf(hw);
+    const float4 cc = cone[cell];
+    const float3 ctr = make_float3(cc.x, cc.y, cc.z);
+    const float ch = cc.w, sh = cone_sin[cell];
     const DevLight lt = lights[l];
     const float dc = dcap[l];
     uint16_t* out = list + (size_t)id * kLbMaxList;
@@ -161,48 +178,82 @@ __global__ void k_db_reach(const float* __restrict__ rad, uint32_t n, const floa
     if (i < n) reach[i] = rad[i] * 1.001f + 2e-4f + (float)kK * *ext;
 }
 
-// One warp per (sphere, cell), as k_lb_build.
-__global__ void k_db_build(const float4* __restrict__ sph, const float* __restrict__ rad, uint32_t n,
-                           const float* __restrict__ reach, uint8_t* count, uint16_t* list)
+// Whether sphere (s, r) may be hit by a ray leaving within rho of o whose
+// direction lies in the cone (axis ctr, half-angle with cosine ch and sine
+// sh): see the exactness note above.  Bounds rounded towards listing.
+__device__ bool db_listed(float3 ctr, float ch, float sh, float4 o, float rho, float4 s, float r)
 {
-    const uint32_t id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
-    if (id >= n * kLbCells) return;   // whole warps: blockDim is a multiple of 32
-    const uint32_t i = id / kLbCells, cell = id % kLbCells;
-    const uint32_t f = cell / (kLbRes * kLbRes), ci = (cell / kLbRes) % kLbRes, cj = cell % kLbRes;
-    const float u0 = 2.0f * ci / kLbRes - 1.0f, u1 = 2.0f * (ci + 1) / kLbRes - 1.0f;
-    const float v0 = 2.0f * cj / kLbRes - 1.0f, v1 = 2.0f * (cj + 1) / kLbRes - 1.0f;
-    const float3 ctr = face_dir(f, 0.5f * (u0 + u1), 0.5f * (v0 + v1));
-    float cmin = 1.0f;
-    for (int k = 0; k < 4; ++k) cmin = fminf(cmin, dotf3(ctr, face_dir(f, (k & 1) ? u1 : u0, (k & 2) ? v1 : v0)));
-    const float hw = acosf(fminf(1.0f, cmin)) + 2e-4f;
-    const float ch = cosf(hw), sh = sinf(hw);
+    const float3 v = make_float3(s.x - o.x, s.y - o.y, s.z - o.z);
+    const float dist = sqrtf(dotf3(v, v));
+    const float m = (float)kK * (dist + rho + 1e-3f);
+    const float rp = r * 1.00001f + m + rho;
+    if (!(dist > (rp + m) * 1.0001f)) return true;   // overlaps the origin's neighbourhood (sphere i itself too)
+    const float sb = fminf(1.0f, rp / dist * 1.0001f);
+    const float cb = sqrtf(fmaxf(0.0f, 1.0f - sb * sb));
+    return dotf3(ctr, v) >= dist * (ch * cb - sh * sb - 2e-5f);   // cos(angle) >= cos(half-angle + beta)
+}
+
+// One block of 256 threads per (sphere i, cube face): first the spheres whose
+// caps meet the face's bounding cone (its corners lie acos(1/sqrt 3) from the
+// face axis), kept in index order; then one warp per cell at a time tests only
+// those and appends the listed ones in index order.
+__global__ void __launch_bounds__(256) k_db_build(const float4* __restrict__ sph, const float* __restrict__ rad,
+                                                  uint32_t n, const float* __restrict__ reach,
+                                                  const float4* __restrict__ cone, const float* __restrict__ cone_sin,
+                                                  uint8_t* count, uint16_t* list)
+{
+    __shared__ uint16_t cand[kDbMaxSpheres];
+    __shared__ uint32_t warp_n[8];
+    const uint32_t i = blockIdx.x / 6u, f = blockIdx.x % 6u;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const float4 o = sph[i];
     const float rho = reach[i];
-    uint16_t* out = list + (size_t)id * kLbMaxList;
-    uint32_t cnt = 0;
-    for (uint32_t base = 0; base < n && cnt <= kLbMaxList; base += 32u) {
-        const uint32_t k = base + lane;
-        bool listed = false;
-        if (k < n) {
-            const float4 s = sph[k];
-            const float3 v = make_float3(s.x - o.x, s.y - o.y, s.z - o.z);
-            const float dist = sqrtf(dotf3(v, v));
-            const float m = (float)kK * (dist + rho + 1e-3f);
-            const float rp = rad[k] * 1.00001f + m + rho;
-            if (!(dist > (rp + m) * 1.0001f)) {
-                listed = true;   // overlaps the origin's neighbourhood (sphere i itself too)
-            } else {
-                const float sb = fminf(1.0f, rp / dist * 1.0001f);
-                const float cb = sqrtf(fmaxf(0.0f, 1.0f - sb * sb));
-                listed = dotf3(ctr, v) >= dist * (ch * cb - sh * sb - 2e-5f);
-            }
-        }
+
+    // pass 1: candidates of the face, block-wide ordered compaction
+    const float3 axis = face_dir(f, 0.0f, 0.0f);
+    const float hf = 0.95531662f + 3e-4f;   // acos(1/sqrt(3)), widened
+    const float chf = cosf(hf), shf = sinf(hf);
+    uint32_t nc = 0;
+    for (uint32_t base = 0; base < n; base += blockDim.x) {
+        const uint32_t k = base + threadIdx.x;
+        const bool listed = k < n && db_listed(axis, chf, shf, o, rho, sph[k], rad[k]);
         const uint32_t mask = __ballot_sync(0xffffffffu, listed);
-        const uint32_t pos = cnt + __popc(mask & ((1u << lane) - 1u));
-        if (listed && pos < kLbMaxList) out[pos] = (uint16_t)k;
-        cnt += __popc(mask);
+        if (lane == 0) warp_n[warp] = (uint32_t)__popc(mask);
+        __syncthreads();
+        uint32_t off = nc, tot = 0;
+        for (uint32_t w = 0; w < 8u; ++w) {
+            if (w < warp) off += warp_n[w];
+            tot += warp_n[w];
+        }
+        if (listed) cand[off + __popc(mask & ((1u << lane) - 1u))] = (uint16_t)k;
+        nc += tot;
+        __syncthreads();
     }
-    if (lane == 0) count[id] = cnt > kLbMaxList ? kLbAll : (uint8_t)cnt;
+
+    // pass 2: one warp per cell
+    for (uint32_t c = warp; c < kLbRes * kLbRes; c += 8u) {
+        const uint32_t cell = f * kLbRes * kLbRes + c;
+        const float4 cc = cone[cell];
+        const float3 ctr = make_float3(cc.x, cc.y, cc.z);
+        const float ch = cc.w, sh = cone_sin[cell];
+        const uint32_t id = i * kLbCells + cell;
+        uint16_t* out = list + (size_t)id * kLbMaxList;
+        uint32_t cnt = 0;
+        for (uint32_t base = 0; base < nc && cnt <= kLbMaxList; base += 32u) {
+            const uint32_t q = base + lane;
+            uint32_t k = 0;
+            bool listed = false;
+            if (q < nc) {
+                k = cand[q];
+                listed = db_listed(ctr, ch, sh, o, rho, sph[k], rad[k]);
+            }
+            const uint32_t mask = __ballot_sync(0xffffffffu, listed);
+            const uint32_t pos = cnt + __popc(mask & ((1u << lane) - 1u));
+            if (listed && pos < kLbMaxList) out[pos] = (uint16_t)k;
+            cnt += __popc(mask);
+        }
+        if (lane == 0) count[id] = cnt > kLbMaxList ? kLbAll : (uint8_t)cnt;
+    }
 }
 
 }  // namespace
@@ -210,7 +261,7 @@ __global__ void k_db_build(const float4* __restrict__ sph, const float* __restri
 uint64_t lb_bytes(uint32_t nl)
 {
     const uint64_t cells = (uint64_t)nl * kLbCells;
-    return up(cells) + up(cells * kLbMaxList * sizeof(uint16_t)) + up(nl * sizeof(float)) + 256;
+    return up(cells) + up(cells * kLbMaxList * sizeof(uint16_t)) + up(nl * sizeof(float)) + kConeBytes + 256;
 }
 
 cudaError_t lb_build(const float4* sph, const float* radius, uint32_t n, const DevLight* lights, uint32_t nl,
@@ -225,9 +276,13 @@ cudaError_t lb_build(const float4* sph, const float* radius, uint32_t n, const D
     uint16_t* list = reinterpret_cast<uint16_t*>(p);
     p += up(cells * kLbMaxList * sizeof(uint16_t));
     float* dcap = reinterpret_cast<float*>(p);
+    p += up(nl * sizeof(float));
+    float4* cone = reinterpret_cast<float4*>(p);
+    float* cone_sin = reinterpret_cast<float*>(p + up(kLbCells * sizeof(float4)));
+    k_cell_cones<<<(kLbCells + 255) / 256, 256, 0, stream>>>(cone, cone_sin);
     k_lb_dcap<<<nl, 256, 0, stream>>>(sph, radius, n, lights, dcap);
-    k_lb_build<<<(unsigned)((cells * 32 + 255) / 256), 256, 0, stream>>>(sph, radius, n, lights, nl, dcap, count,
-                                                                       list);
+    k_lb_build<<<(unsigned)((cells * 32 + 255) / 256), 256, 0, stream>>>(sph, radius, n, lights, nl, dcap, cone,
+                                                                       cone_sin, count, list);
     out->count = count;
     out->list = list;
     out->dcap = dcap;
@@ -238,7 +293,8 @@ cudaError_t lb_build(const float4* sph, const float* radius, uint32_t n, const D
 uint64_t db_bytes(uint32_t n)
 {
     const uint64_t cells = (uint64_t)n * kLbCells;
-    return up(cells) + up(cells * kLbMaxList * sizeof(uint16_t)) + up(n * sizeof(float)) + up(sizeof(float)) + 256;
+    return up(cells) + up(cells * kLbMaxList * sizeof(uint16_t)) + up(n * sizeof(float)) + up(sizeof(float)) +
+           kConeBytes + 256;
 }
 
 cudaError_t db_build(const float4* sph, const float* radius, uint32_t n, void* buf, uint64_t bytes,
@@ -254,9 +310,13 @@ cudaError_t db_build(const float4* sph, const float* radius, uint32_t n, void* b
     float* reach = reinterpret_cast<float*>(p);
     p += up(n * sizeof(float));
     float* ext = reinterpret_cast<float*>(p);
+    p += up(sizeof(float));
+    float4* cone = reinterpret_cast<float4*>(p);
+    float* cone_sin = reinterpret_cast<float*>(p + up(kLbCells * sizeof(float4)));
+    k_cell_cones<<<(kLbCells + 255) / 256, 256, 0, stream>>>(cone, cone_sin);
     k_db_extent<<<1, 256, 0, stream>>>(sph, radius, n, ext);
     k_db_reach<<<(n + 255) / 256, 256, 0, stream>>>(radius, n, ext, reach);
-    k_db_build<<<(unsigned)((cells * 32 + 255) / 256), 256, 0, stream>>>(sph, radius, n, reach, count, list);
+    k_db_build<<<n * 6u, 256, 0, stream>>>(sph, radius, n, reach, cone, cone_sin, count, list);
     out->count = count;
     out->list = list;
     out->reach = reach;

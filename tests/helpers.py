@@ -61,6 +61,7 @@ def job_bytes_bound(sc):
     tables = 24 * n + 48 * len(sc.materials) + 32 * nl + 8 * 256
     bvh = 200 * n if n >= 512 else 0
     cells = 6 * 16 * 16 * 65          # per light / per sphere: a count and 32 indices per direction cell
-    lb = cells * nl + 2048 if n < 512 and 1 <= nl <= 64 else 0
-    db = cells * n + 2048 if n < 512 else 0
+    cones = 6 * 16 * 16 * 20 + 4096   # build scratch: the cells' bounding cones
+    lb = cells * nl + cones if n < 512 and 1 <= nl <= 64 else 0
+    db = cells * n + cones if n < 512 else 0
     return tables + bvh + lb + db + 28 * px + 512
