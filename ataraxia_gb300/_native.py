@@ -69,7 +69,8 @@ class Config(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("frames", C.c_uint64), ("paths", C.c_uint64), ("extension_rays", C.c_uint64),
                 ("shadow_rays", C.c_uint64), ("kernel_launches", C.c_uint64), ("device_bytes", C.c_uint64),
-                ("last_render_ms", C.c_double), ("bvh_in_use", C.c_uint32), ("reserved", C.c_uint32)]
+                ("last_render_ms", C.c_double), ("bvh_in_use", C.c_uint32), ("reserved", C.c_uint32),
+                ("shaded_first", C.c_uint64)]
 
 
 class KernelTimes(C.Structure):

@@ -80,8 +80,8 @@ atx_status Batch::init()
     order_ = StreamOrder{pool_, up_stream_, stream_};
     ATX_CUDA(cudaEventCreate(&ev0_));
     ATX_CUDA(cudaEventCreate(&ev1_));
-    ATX_TRY(totals_.ensure(2 * sizeof(unsigned long long), &scratch_, "ray totals"));
-    ATX_CUDA(cudaMemsetAsync(totals_.get(), 0, 2 * sizeof(unsigned long long), stream_));
+    ATX_TRY(totals_.ensure(3 * sizeof(unsigned long long), &scratch_, "ray totals"));
+    ATX_CUDA(cudaMemsetAsync(totals_.get(), 0, 3 * sizeof(unsigned long long), stream_));
     tuning_.lanes = kDefaultLanes;
     tuning_.lane_wave_paths = cfg_.wave_paths ? cfg_.wave_paths : kDefaultLaneWavePaths;
     tuning_.threads = cfg_.threads;

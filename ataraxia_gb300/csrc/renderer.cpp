@@ -318,8 +318,8 @@ atx_status Renderer::init()
     ATX_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
     ATX_CUDA(cudaEventCreate(&ev_start_));
     ATX_CUDA(cudaEventCreate(&ev_stop_));
-    ATX_TRY(totals_.ensure(2 * sizeof(unsigned long long), &budget_, "ray totals"));
-    ATX_CUDA(cudaMemsetAsync(totals_.get(), 0, 2 * sizeof(unsigned long long), stream_));
+    ATX_TRY(totals_.ensure(3 * sizeof(unsigned long long), &budget_, "ray totals"));
+    ATX_CUDA(cudaMemsetAsync(totals_.get(), 0, 3 * sizeof(unsigned long long), stream_));
     scene_.bvh_threshold = cfg_.bvh_threshold;
     scene_.bvh_leaf = cfg_.bvh_leaf_size;
     // empty scene until set_scene
@@ -508,7 +508,7 @@ atx_status Renderer::stats(atx_stats* out)
 {
     ATX_TRY(activate());
     ATX_CUDA(cudaStreamSynchronize(stream_));
-    unsigned long long dev[2] = {0, 0};
+    unsigned long long dev[3] = {0, 0, 0};
     ATX_CUDA(cudaMemcpy(dev, totals_.get(), sizeof(dev), cudaMemcpyDeviceToHost));
     if (timed_) {
         float ms = 0.0f;
@@ -518,6 +518,7 @@ atx_status Renderer::stats(atx_stats* out)
     *out = st_;
     out->extension_rays = totals_host_[0] + dev[0];
     out->shadow_rays = dev[1];
+    out->shaded_first = dev[2];
     out->device_bytes = budget_.used();
     out->bvh_in_use = scene_.view.use_bvh;
     return ATX_OK;

@@ -297,6 +297,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
         const uint32_t idx = base + threadIdx.x;
         Shaded r{};
         uint32_t pid = 0u, seed = 0u, own = ~0u;
+        bool shaded = false;
         float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o;
         if (idx < n) {
             const uint32_t j = SHARED ? ws.hitq[idx / job.spp] : idx / job.spp;   // path ids stay pixel-major
@@ -323,11 +324,14 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
                 }
             } else {
                 shade_hit<SMEM, INL>(sc, sph, ws, pid, hit, tmin, o, d, thr, own, seed, last, vis, j, r);
+                shaded = true;
             }
             float3 c = add3(mk3(0.f, 0.f, 0.f), r.add);
             if (r.lit) c = add3(c, r.lc);   // as k_shadow adds it: after the emission
             ws.col[pid] = make_float4(c.x, c.y, c.z, 0.0f);
         }
+        // count the shaded paths (SHARED: every path of the launch is one)
+        if (!SHARED) warp_push(&ws.counters[2 * ((uint32_t)job.max_bounces + 1u) + 1u], shaded);
         push_shaded<INL>(ws, ws.q[1], 0, pid, r, o, d, thr, own, seed);
     }
 }
@@ -602,6 +606,11 @@ __global__ void __launch_bounds__(kThreads) k_accumulate(WaveState ws, WaveJob j
         }
         atomicAdd(&ws.totals[0], ext);
         atomicAdd(&ws.totals[1], sh);
+        if (job.max_bounces > 0) {
+            const uint32_t* hc = &ws.counters[2 * ((uint32_t)job.max_bounces + 1u)];   // hit pixels, shaded paths
+            atomicAdd(&ws.totals[2], wave_shares_primary(job) ? (unsigned long long)hc[0] * job.spp
+                                                              : (unsigned long long)hc[1]);
+        }
     }
     // a sample whose shared primary ray missed has colour 0 + sky * 1 (Renderer.cu:311-316)
     const bool shared = wave_shares_primary(job);

@@ -147,7 +147,8 @@ struct WaveState {
     float4* sh_d;
     float4* sh_c;
     uint32_t* counters;
-    unsigned long long* totals;   // [0] extension rays after bounce 0, [1] shadow rays (running sums)
+    unsigned long long* totals;   // running sums: [0] extension rays after bounce 0, [1] shadow rays,
+                                  // [2] paths shaded at the first bounce
     uint2* prim;                  // per pixel of the wave: primary hit (t bits, sphere id), shared by its samples
     uint32_t* hitq;               // wave pixels whose primary ray hits (only those get first-bounce paths)
     uint32_t* vis;                // per pixel of the wave: bit l set when light l is visible from the primary hit
@@ -160,7 +161,9 @@ struct WaveState {
 constexpr uint64_t kWaveBytesPerPath = 7 * 16 + 4 * 4 + 8;
 constexpr uint64_t kWaveArrays = 12;
 
-// Counter slots after the per-bounce pairs: [2*(max_bounces+1)] = hit pixels.
+// Counter slots after the per-bounce pairs: [2*(max_bounces+1)] = hit pixels,
+// [2*(max_bounces+1)+1] = paths shaded at the first bounce (counted only when
+// the wave does not share primary hits; else it is hit pixels x spp).
 inline size_t wave_counter_words(int max_bounces) { return 2 * ((size_t)(max_bounces > 0 ? max_bounces : 0) + 1) + 2; }
 
 // One wave: pixels [pixel0, pixel0 + n_pixels) x samples [0, spp) with the

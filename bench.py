@@ -31,8 +31,18 @@ ROOT = Path(__file__).resolve().parent
 if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
-FLOP_PER_TEST = 20       # FP32 FLOP per ray-sphere test, FMA counted as 2
-FLOP_PER_SHADE = 120     # FP32 FLOP per shaded hit (BRDF + sampler + roulette)
+# Algorithmic HBM bytes of the wavefront path state (minimal records):
+BYTES_PER_EXTENSION = 104   # ray record (origin, direction, throughput, seed: 44 B) written and read, hit record 2 x 8
+BYTES_PER_SHADOW = 80       # shadow-ray record (origin, direction, contribution, path: 40 B) written and read
+BYTES_PER_PIXEL = 52        # primary hit record written and read (2 x 8), accumulator read and written (2 x 16), RGBA8 (4)
+
+
+def hbm_peak_gbs():
+    """Measured copy bandwidth of the GB300s (MEASURED_PEAKS.json, driver-written), else the fallback."""
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
 METRIC = "Mpaths/s per GB300"
 UNIT = "Mpaths/s"
 
@@ -248,7 +258,7 @@ def run_ours(args, dist: Dist):
            "ms_per_step": round(e2e_s * 1e3 / args.steps, 3)}
     _ = host_img
 
-    # ---- roofline of the dominant kernel (extension: nearest hit + shading) from per-kernel events
+    # ---- roofline: one render launch against HBM, from per-kernel events (one lane, kernels serialised)
     rp = make(N.FLAG_PROFILE_KERNELS)
     for _ in range(max(1, args.warmup)):
         rp.render_frames(sc.spp)
@@ -261,35 +271,44 @@ def run_ours(args, dist: Dist):
     kt = rp.kernel_times()
     p1 = rp.stats()
     rp.close()
-    ext_rays = p1["extension_rays"] - p0["extension_rays"]
+    # the primary ray of a pixel is traced once per launch (its samples share it)
+    ext_after0 = (p1["extension_rays"] - p0["extension_rays"]) - sc.pixels * prof_steps
     sh_rays = p1["shadow_rays"] - p0["shadow_rays"]
-    n_sph = len(sc.spheres)
-    ext_flops = ext_rays * n_sph * FLOP_PER_TEST + sh_rays * FLOP_PER_SHADE
+    shaded0 = p1["shaded_first"] - p0["shaded_first"]
+    alg_bytes = (BYTES_PER_EXTENSION * ext_after0 + BYTES_PER_SHADOW * sh_rays
+                 + BYTES_PER_PIXEL * sc.pixels * prof_steps) / prof_steps
     total_kernel_ms = kt["extend_ms"] + kt["shadow_ms"] + kt["accumulate_ms"] + kt["other_ms"]
-    peak = atx.measure_fp32_peak(dev)
-    achieved = ext_flops / (kt["extend_ms"] * 1e-3) / 1e12
+    launch_ms = total_kernel_ms / prof_steps
+    peak = hbm_peak_gbs()
+    achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     roofline = {
-        "kernel": "k_extend (nearest hit over shared-memory sphere table + shading)",
-        "bound": "fp32", "achieved": round(achieved, 2), "peak": round(peak, 2), "unit": "TFLOP/s",
+        "kernel": "one atx_render of the workload: k_primary, k_shadow (first-bounce pixel-light rays), "
+                  "k_first, k_bounce x7, k_accumulate per lane",
+        "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
         "frac": round(achieved / peak, 4) if peak else None,
-        "peak_source": "measured FFMA throughput (atx_measure_fp32_peak, this process); MEASURED_PEAKS.json "
-                       "has no FP32 figure",
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth, burst)",
         "traffic": None,
-        "launch": "one atx_render of the workload: all its k_primary and k_extend kernels",
-        "flop_per_launch": round(ext_flops / prof_steps),
-        "avg_launch_ms": round(kt["extend_ms"] / prof_steps, 4),
-        "kernel_launches_per_launch": round(kt["extend_launches"] / prof_steps, 1),
-        "share_of_kernel_time": round(kt["extend_ms"] / total_kernel_ms, 4) if total_kernel_ms else None,
+        "algorithmic_bytes_per_launch": round(alg_bytes),
+        "algorithmic_bytes": f"{BYTES_PER_EXTENSION} B per extension ray after the first bounce (ray record "
+                             f"2x44, hit record 2x8), {BYTES_PER_SHADOW} B per shadow ray (record 2x40), "
+                             f"{BYTES_PER_PIXEL} B per pixel (primary hit 2x8, accumulator 2x16, RGBA8 4)",
+        "units_per_launch": {"extension_rays_after_first_bounce": round(ext_after0 / prof_steps),
+                             "shadow_rays": round(sh_rays / prof_steps),
+                             "first_bounce_shaded_paths": round(shaded0 / prof_steps),
+                             "pixels": sc.pixels},
+        "avg_launch_ms": round(launch_ms, 4),
+        "kernel_launches_per_launch": round((kt["extend_launches"] + kt["shadow_launches"] +
+                                             kt["accumulate_launches"] + kt["other_launches"]) / prof_steps, 1),
         "kernel_ms_per_step": {k: round(kt[k] / prof_steps, 3) for k in
                                ("extend_ms", "shadow_ms", "accumulate_ms", "other_ms")},
     }
-    # DRAM bytes of the same kernels per atx_render, from an ncu capture summarised in profiles/
-    traffic_file = ROOT / "profiles" / "extension_traffic_medium_scene.txt"
+    # DRAM bytes of the same launch's kernels, from an ncu capture summarised in profiles/
+    traffic_file = ROOT / "profiles" / "render_traffic_medium_scene.txt"
     if traffic_file.exists():
         for line in traffic_file.read_text().splitlines():
             if line.startswith("dram_bytes_per_launch:"):
                 roofline["traffic"] = int(line.split(":", 1)[1])
-                roofline["traffic_source"] = "profiles/extension_traffic_medium_scene.txt (ncu)"
+                roofline["traffic_source"] = "profiles/render_traffic_medium_scene.txt (ncu)"
 
     ref_kernel = None
     if dist.world == 1 and not args.no_ref_kernel:
@@ -302,7 +321,7 @@ def run_ours(args, dist: Dist):
         "config": {"workload": "medium scene: 256 spheres, 64 materials, 8 lights, 1920x1080, 8 bounces, "
                                "16 spp per launch (one step = one launch)",
                    "paths_per_step": paths_step, "parallelism": f"replicas x{dist.world}",
-                   "l2": "working set > L2: 4 Mi-path wave state (480 MB) streamed per wave"},
+                   "l2": "working set > L2: four lanes of up to 8 Mi-path wave state (1.1 GB each) per launch"},
         "mrays_per_s": round(mrays, 1),
         "gpu_launches": int(launches),
         "clocks": clk,

@@ -119,6 +119,7 @@ typedef struct atx_stats {
     double last_render_ms;     /* device time of the last atx_render (CUDA events) */
     uint32_t bvh_in_use;       /* 1 if the current scene uses the LBVH */
     uint32_t reserved;
+    uint64_t shaded_first;     /* pixel-samples whose primary ray hits (the paths shaded at the first bounce) */
 } atx_stats;
 
 typedef struct atx_renderer atx_renderer;

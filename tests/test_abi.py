@@ -40,7 +40,7 @@ def test_struct_layouts_match_reference_sizes():
     assert LIGHT_DTYPE.itemsize == 28         # Scene.h:17-26
     assert C.sizeof(N.Settings) == 8          # Scene.h:49-56 (bool, bool, int)
     assert N.Settings.max_bounces.offset == 4
-    assert C.sizeof(N.Config) == 32 and C.sizeof(N.Stats) == 64
+    assert C.sizeof(N.Config) == 32 and C.sizeof(N.Stats) == 72
 
 
 def test_version_and_status_strings(native):
