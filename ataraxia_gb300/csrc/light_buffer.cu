@@ -98,8 +98,7 @@ __global__ void k_lb_dcap(const float4* __restrict__ sph, const float* __restric
 // taken from it, a 2e-5 slack on the final comparison.
 __global__ void k_lb_build(const float4* __restrict__ sph, const float* __restrict__ rad, uint32_t n,
                            const DevLight* __restrict__ lights, uint32_t nl, const float* __restrict__ dcap,
-                           const float4* __restrict__ cone, const float* __restrict__ cone_sin, uint8_t* count,
-                           uint16_t* list)
+                           const float4* __restrict__ cone, const float* __restrict__ cone_sin, uint16_t* line)
 {
     const uint32_t id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
     if (id >= nl * kLbCells) return;   // whole warps: blockDim is a multiple of 32
@@ -109,7 +108,7 @@ __global__ void k_lb_build(const float4* __restrict__ sph, const float* __restri
     const float ch = cc.w, sh = cone_sin[cell];
     const DevLight lt = lights[l];
     const float dc = dcap[l];
-    uint16_t* out = list + (size_t)id * kLbMaxList;
+    uint16_t* out = line + (size_t)id * kLbLine + 1;
     uint32_t cnt = 0;
     for (uint32_t base = 0; base < n && cnt <= kLbMaxList; base += 32u) {
         const uint32_t k = base + lane;
@@ -133,7 +132,7 @@ __global__ void k_lb_build(const float4* __restrict__ sph, const float* __restri
         if (listed && pos < kLbMaxList) out[pos] = (uint16_t)k;
         cnt += __popc(mask);
     }
-    if (lane == 0) count[id] = cnt > kLbMaxList ? kLbAll : (uint8_t)cnt;
+    if (lane == 0) out[-1] = (uint16_t)(cnt > kLbMaxList ? kLbAll : cnt);
 }
 
 // ---------------------------------------------------------- direction buffer
@@ -200,7 +199,7 @@ __device__ bool db_listed(float3 ctr, float ch, float sh, float4 o, float rho, f
 __global__ void __launch_bounds__(256) k_db_build(const float4* __restrict__ sph, const float* __restrict__ rad,
                                                   uint32_t n, const float* __restrict__ reach,
                                                   const float4* __restrict__ cone, const float* __restrict__ cone_sin,
-                                                  uint8_t* count, uint16_t* list)
+                                                  uint16_t* line)
 {
     __shared__ uint16_t cand[kDbMaxSpheres];
     __shared__ uint32_t warp_n[8];
@@ -237,7 +236,7 @@ __global__ void __launch_bounds__(256) k_db_build(const float4* __restrict__ sph
         const float3 ctr = make_float3(cc.x, cc.y, cc.z);
         const float ch = cc.w, sh = cone_sin[cell];
         const uint32_t id = i * kLbCells + cell;
-        uint16_t* out = list + (size_t)id * kLbMaxList;
+        uint16_t* out = line + (size_t)id * kLbLine + 1;
         uint32_t cnt = 0;
         for (uint32_t base = 0; base < nc && cnt <= kLbMaxList; base += 32u) {
             const uint32_t q = base + lane;
@@ -252,7 +251,7 @@ __global__ void __launch_bounds__(256) k_db_build(const float4* __restrict__ sph
             if (listed && pos < kLbMaxList) out[pos] = (uint16_t)k;
             cnt += __popc(mask);
         }
-        if (lane == 0) count[id] = cnt > kLbMaxList ? kLbAll : (uint8_t)cnt;
+        if (lane == 0) out[-1] = (uint16_t)(cnt > kLbMaxList ? kLbAll : cnt);
     }
 }
 
@@ -261,7 +260,7 @@ __global__ void __launch_bounds__(256) k_db_build(const float4* __restrict__ sph
 uint64_t lb_bytes(uint32_t nl)
 {
     const uint64_t cells = (uint64_t)nl * kLbCells;
-    return up(cells) + up(cells * kLbMaxList * sizeof(uint16_t)) + up(nl * sizeof(float)) + kConeBytes + 256;
+    return up(cells * kLbLine * sizeof(uint16_t)) + up(nl * sizeof(float)) + kConeBytes + 256;
 }
 
 cudaError_t lb_build(const float4* sph, const float* radius, uint32_t n, const DevLight* lights, uint32_t nl,
@@ -271,10 +270,8 @@ cudaError_t lb_build(const float4* sph, const float* radius, uint32_t n, const D
         return cudaErrorInvalidValue;
     const uint64_t cells = (uint64_t)nl * kLbCells;
     unsigned char* p = static_cast<unsigned char*>(buf);
-    uint8_t* count = p;
-    p += up(cells);
-    uint16_t* list = reinterpret_cast<uint16_t*>(p);
-    p += up(cells * kLbMaxList * sizeof(uint16_t));
+    uint16_t* line = reinterpret_cast<uint16_t*>(p);
+    p += up(cells * kLbLine * sizeof(uint16_t));
     float* dcap = reinterpret_cast<float*>(p);
     p += up(nl * sizeof(float));
     float4* cone = reinterpret_cast<float4*>(p);
@@ -282,9 +279,8 @@ cudaError_t lb_build(const float4* sph, const float* radius, uint32_t n, const D
     k_cell_cones<<<(kLbCells + 255) / 256, 256, 0, stream>>>(cone, cone_sin);
     k_lb_dcap<<<nl, 256, 0, stream>>>(sph, radius, n, lights, dcap);
     k_lb_build<<<(unsigned)((cells * 32 + 255) / 256), 256, 0, stream>>>(sph, radius, n, lights, nl, dcap, cone,
-                                                                       cone_sin, count, list);
-    out->count = count;
-    out->list = list;
+                                                                       cone_sin, line);
+    out->line = line;
     out->dcap = dcap;
     out->n_lights = nl;
     return cudaGetLastError();
@@ -293,8 +289,7 @@ cudaError_t lb_build(const float4* sph, const float* radius, uint32_t n, const D
 uint64_t db_bytes(uint32_t n)
 {
     const uint64_t cells = (uint64_t)n * kLbCells;
-    return up(cells) + up(cells * kLbMaxList * sizeof(uint16_t)) + up(n * sizeof(float)) + up(sizeof(float)) +
-           kConeBytes + 256;
+    return up(cells * kLbLine * sizeof(uint16_t)) + up(n * sizeof(float)) + up(sizeof(float)) + kConeBytes + 256;
 }
 
 cudaError_t db_build(const float4* sph, const float* radius, uint32_t n, void* buf, uint64_t bytes,
@@ -303,10 +298,8 @@ cudaError_t db_build(const float4* sph, const float* radius, uint32_t n, void* b
     if (n == 0 || n > kDbMaxSpheres || bytes < db_bytes(n)) return cudaErrorInvalidValue;
     const uint64_t cells = (uint64_t)n * kLbCells;
     unsigned char* p = static_cast<unsigned char*>(buf);
-    uint8_t* count = p;
-    p += up(cells);
-    uint16_t* list = reinterpret_cast<uint16_t*>(p);
-    p += up(cells * kLbMaxList * sizeof(uint16_t));
+    uint16_t* line = reinterpret_cast<uint16_t*>(p);
+    p += up(cells * kLbLine * sizeof(uint16_t));
     float* reach = reinterpret_cast<float*>(p);
     p += up(n * sizeof(float));
     float* ext = reinterpret_cast<float*>(p);
@@ -316,9 +309,8 @@ cudaError_t db_build(const float4* sph, const float* radius, uint32_t n, void* b
     k_cell_cones<<<(kLbCells + 255) / 256, 256, 0, stream>>>(cone, cone_sin);
     k_db_extent<<<1, 256, 0, stream>>>(sph, radius, n, ext);
     k_db_reach<<<(n + 255) / 256, 256, 0, stream>>>(radius, n, ext, reach);
-    k_db_build<<<n * 6u, 256, 0, stream>>>(sph, radius, n, reach, cone, cone_sin, count, list);
-    out->count = count;
-    out->list = list;
+    k_db_build<<<n * 6u, 256, 0, stream>>>(sph, radius, n, reach, cone, cone_sin, line);
+    out->line = line;
     out->reach = reach;
     out->n = n;
     return cudaGetLastError();

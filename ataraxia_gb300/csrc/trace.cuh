@@ -356,6 +356,27 @@ __device__ __forceinline__ int lb_cell(float3 w)
     return (int)((face * kLbRes + (uint32_t)i) * kLbRes + (uint32_t)j);
 }
 
+// The spheres of a cell line (words 1..count after the count in word 0):
+// calls f(i) for each in ascending order until f returns true, and returns
+// whether one did.  The count and the first seven indices come in one 16-byte
+// load (h, already loaded); the rest, for longer lists, word by word.
+template <class F>
+__device__ __forceinline__ bool walk_line(const uint16_t* line, uint4 h, uint32_t cnt, F&& f)
+{
+    // words 1..7 of h as a 112-bit window, consumed 16 bits at a time
+    uint64_t lo = (((uint64_t)h.y << 32) | h.x) >> 16 | ((uint64_t)h.z << 48);
+    uint64_t hi = (((uint64_t)h.w << 32) | h.z) >> 16;
+    const uint32_t first = cnt < 7u ? cnt : 7u;
+    for (uint32_t k = 0; k < first; ++k) {
+        if (f((uint32_t)(lo & 0xffffu))) return true;
+        lo = (lo >> 16) | (hi << 48);
+        hi >>= 16;
+    }
+    for (uint32_t k = 7; k < cnt; ++k)
+        if (f((uint32_t)__ldg(&line[1 + k]))) return true;
+    return false;
+}
+
 // Any hit for a shadow ray (o, d, dist2) towards light li: the spheres the
 // light buffer lists for the cell of o seen from the light, or the whole table
 // when that cell overflowed, o lies beyond the buffer's reach or the
@@ -368,53 +389,57 @@ __device__ __forceinline__ bool occluded_lb(const SceneView& sc, const float4* _
     const float3 w = mk3(o.x - l0.x, o.y - l0.y, o.z - l0.z);
     const float dc = __ldg(&sc.lb.dcap[li]);
     const int cell = dot3(w, w) <= dc * dc ? lb_cell(w) : -1;
-    const uint32_t slot = li * kLbCells + (uint32_t)cell;
-    const uint32_t cnt = cell >= 0 ? (uint32_t)__ldg(&sc.lb.count[slot]) : (uint32_t)kLbAll;
+    if (cell < 0) return occluded_brute<SMEM>(sph, sc.n_sph, o, d, dist2);
+    const uint16_t* line = sc.lb.line + (size_t)(li * kLbCells + (uint32_t)cell) * kLbLine;
+    const uint4 h = __ldg(reinterpret_cast<const uint4*>(line));
+    const uint32_t cnt = h.x & 0xffffu;
     if (cnt == kLbAll) return occluded_brute<SMEM>(sph, sc.n_sph, o, d, dist2);
     const float a = dot3(d, d);
-    const uint16_t* lst = sc.lb.list + (size_t)slot * kLbMaxList;
-    for (uint32_t k = 0; k < cnt; ++k) {
+    return walk_line(line, h, cnt, [&](uint32_t i) {
         float t;
-        if (sphere_t(table_sphere<SMEM>(sph, __ldg(&lst[k])), o, d, a, t) && t > 0.0f && t * t < dist2) return true;
-    }
-    return false;
+        return sphere_t(table_sphere<SMEM>(sph, i), o, d, a, t) && t > 0.0f && t * t < dist2;
+    });
 }
 
 // Nearest hit of an extension ray leaving sphere own: the spheres the
 // direction buffer lists for own and the cell of d, in index order (ties keep
 // the lowest index, as in the brute-force loop), or the whole table when own
-// is not covered, o lies beyond own's reach, the cell overflowed or d is
+// is not covered (~0u: also when the ray's origin lay beyond own's reach,
+// which the shading that made the ray checks), the cell overflowed or d is
 // degenerate.
 template <bool SMEM>
 __device__ __forceinline__ int32_t nearest_db(const SceneView& sc, const float4* __restrict__ sph, uint32_t own,
                                               float3 o, float3 d, float& tmin)
 {
-    uint32_t cnt = kLbAll, slot = 0u;
-    if (own < sc.db.n) {
-        const float4 c = __ldg(&sc.sph[own]);
-        const float3 e = mk3(o.x - c.x, o.y - c.y, o.z - c.z);
-        const float reach = __ldg(&sc.db.reach[own]);
-        const int cell = dot3(e, e) <= reach * reach ? lb_cell(d) : -1;
-        if (cell >= 0) {
-            slot = own * kLbCells + (uint32_t)cell;
-            cnt = __ldg(&sc.db.count[slot]);
-        }
-    }
+    const int cell = own < sc.db.n ? lb_cell(d) : -1;
+    if (cell < 0) return nearest_brute<SMEM>(sph, sc.n_sph, o, d, tmin);
+    const uint16_t* line = sc.db.line + (size_t)(own * kLbCells + (uint32_t)cell) * kLbLine;
+    const uint4 h = __ldg(reinterpret_cast<const uint4*>(line));
+    const uint32_t cnt = h.x & 0xffffu;
     if (cnt == kLbAll) return nearest_brute<SMEM>(sph, sc.n_sph, o, d, tmin);
     const float a = dot3(d, d);
-    const uint16_t* lst = sc.db.list + (size_t)slot * kLbMaxList;
     int32_t best = -1;
     float tm = kFltMax;
-    for (uint32_t k = 0; k < cnt; ++k) {
-        const uint32_t i = __ldg(&lst[k]);
+    walk_line(line, h, cnt, [&](uint32_t i) {
         float t;
         if (sphere_t(table_sphere<SMEM>(sph, i), o, d, a, t) && t > 0.0f && t < tm) {
             tm = t;
             best = (int32_t)i;
         }
-    }
+        return false;
+    });
     tmin = tm;
     return best;
+}
+
+// Whether the direction buffer's lists of sphere own hold for a ray leaving
+// from o (within reach of own's centre c).
+__device__ __forceinline__ bool db_reaches(const SceneView& sc, uint32_t own, float4 c, float3 o)
+{
+    if (own >= sc.db.n) return false;
+    const float3 e = mk3(o.x - c.x, o.y - c.y, o.z - c.z);
+    const float reach = __ldg(&sc.db.reach[own]);
+    return dot3(e, e) <= reach * reach;
 }
 
 template <int IS>

@@ -240,7 +240,8 @@ __device__ __forceinline__ void shade_hit(const SceneView& sc, const float4* sph
         if (!(pcg_float(seed) > p)) {
             thr = divs3(thr, p);
             d = (metallic > 0.0f) ? sample_ggx(nrm, rough, seed) : sample_cosine(nrm, seed);
-            own = (uint32_t)hit;   // the next ray leaves this sphere
+            // the next ray leaves this sphere (~0u: beyond the direction buffer's reach)
+            own = db_reaches(sc, (uint32_t)hit, s, o) ? (uint32_t)hit : ~0u;
             r.push_next = true;
         }
     }

@@ -55,15 +55,19 @@ struct BvhView {
 // block a shadow ray towards that light whose origin, seen from the light,
 // lies in the cell (built by light_buffer.cu).  A shadow ray then tests the
 // spheres of one cell instead of the whole table.
+// Each cell is one 64-byte line of 16-bit words: word 0 the number of spheres
+// listed (or kLbAll when they did not fit), words 1.. their indices in
+// ascending order, so the count and the first seven indices arrive in one
+// 16-byte load.
 constexpr uint32_t kLbRes = 16;
 constexpr uint32_t kLbCells = 6 * kLbRes * kLbRes;
-constexpr uint32_t kLbMaxList = 32;
+constexpr uint32_t kLbLine = 32;                 // 16-bit words per cell
+constexpr uint32_t kLbMaxList = kLbLine - 1;     // spheres a cell can list
 constexpr uint32_t kLbMaxLights = 64;
-constexpr uint32_t kLbMaxSpheres = 65535;   // indices are 16-bit
-constexpr uint8_t kLbAll = 0xff;            // the cell's list overflowed: test every sphere
+constexpr uint32_t kLbMaxSpheres = 65534;        // indices are 16-bit, 0xffff is kLbAll
+constexpr uint32_t kLbAll = 0xffff;              // the cell's list overflowed: test every sphere
 struct LightBufferView {
-    const uint8_t* count;    // [n_lights * kLbCells] spheres listed, or kLbAll
-    const uint16_t* list;    // [n_lights * kLbCells * kLbMaxList] sphere indices, ascending
+    const uint16_t* line;    // [n_lights * kLbCells * kLbLine] cell lines
     const float* dcap;       // [n_lights] the lists hold for shadow-ray origins within dcap of the light
     uint32_t n_lights;       // 0: no light buffer
 };
@@ -77,8 +81,7 @@ struct LightBufferView {
 // hit, so its nearest hit tests the spheres of one cell.
 constexpr uint32_t kDbMaxSpheres = 1024;   // 100 KB of cells per sphere
 struct DirBufferView {
-    const uint8_t* count;    // [n * kLbCells] spheres listed, or kLbAll
-    const uint16_t* list;    // [n * kLbCells * kLbMaxList] sphere indices, ascending
+    const uint16_t* line;    // [n * kLbCells * kLbLine] cell lines, as the light buffer's
     const float* reach;      // [n] the lists hold for ray origins within reach of the sphere's centre
     uint32_t n;              // spheres covered; 0: no direction buffer
 };
