@@ -20,12 +20,12 @@
 namespace atx {
 
 namespace {
-constexpr uint32_t kDefaultActive = 64;
-constexpr uint32_t kDefaultPassSpp = 16;
+constexpr uint32_t kDefaultActive = 16;
+constexpr uint32_t kDefaultPassSpp = 64;
 constexpr uint64_t kDefaultPassPaths = 1ull << 30;
 constexpr uint32_t kDefaultBvhThreshold = 512;   // fastest of 256-1024 on the 64-scene mix
 constexpr size_t kPassesInFlight = 2;                 // the one running and the next
-constexpr uint64_t kMinSlicePaths = 4ull << 20;       // a job's slice fills at least a few-Mi-path wave
+constexpr uint64_t kMinSlicePaths = 16ull << 20;      // a job's slice fills at least a 16 Mi-path wave
 constexpr uint64_t kPinnedCacheBytes = 4ull << 30;    // result buffers kept for reuse
 
 uint64_t up256(uint64_t x) { return (x + 255u) & ~uint64_t(255u); }

@@ -709,7 +709,7 @@ def main(argv=None) -> int:
     ap.add_argument("--rates", default="50,200,800", help="serve mode: arrival rates (jobs/s)")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="serve mode: run length per rate")
     ap.add_argument("--hbm-budget-gb", type=float, default=120.0, help="serve mode: admission budget")
-    ap.add_argument("--max-active", type=int, default=64, help="serve mode: jobs rendered together")
+    ap.add_argument("--max-active", type=int, default=0, help="serve mode: jobs rendered together (0 = library default)")
     ap.add_argument("--pass-spp", type=int, default=0, help="serve mode: frames per job per pass (0 = library default)")
     ap.add_argument("--max-pending", type=int, default=4096, help="serve mode: queue bound (then BUSY)")
     ap.add_argument("--pool", type=int, default=512, help="serve mode: scenes in the job pool")

@@ -311,8 +311,8 @@ typedef struct atx_server atx_server;
 
 typedef struct atx_server_config {
     atx_config base;            /* device, hbm_budget_bytes (0 = unlimited), bvh settings, flags */
-    uint32_t max_active_jobs;   /* jobs rendered together (0 = 64) */
-    uint32_t pass_spp;          /* frames per job per pass (0 = 16, raised for small images to 4 Mi paths per slice) */
+    uint32_t max_active_jobs;   /* jobs rendered together (0 = 16) */
+    uint32_t pass_spp;          /* frames per job per pass (0 = 64, raised for small images to 16 Mi paths per slice) */
     uint64_t max_pass_paths;    /* bound on pixel-samples per pass, scaling slices down (0 = 2^30) */
     uint32_t max_pending;       /* queued jobs before submit returns ATX_ERR_BUSY (0 = unbounded) */
     uint32_t host_fail_pass;    /* with ATX_FLAG_HOST_EXECUTOR: pass number at which the simulated device
