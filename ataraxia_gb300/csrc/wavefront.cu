@@ -40,6 +40,9 @@ constexpr int kThreads = 256;
 // and 3 of 256 (80 registers) on the medium scene.
 constexpr int kExtendThreads = 256;
 constexpr int kExtendBlocksPerSm = 4;
+// With a light buffer, bounces from this one on run in one persistent k_paths
+// launch instead of a k_bounce launch each.
+constexpr int kPathsFrom = 2;
 
 // k_shadow's blocks per SM: the shared-memory variant fits 40 registers
 // without spilling (6 blocks of 256 threads); the others take up to 64 (4).
@@ -60,6 +63,15 @@ __device__ __forceinline__ uint32_t warp_push(uint32_t* counter, bool pred)
     if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
     base = __shfl_sync(kFull, base, leader);
     return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+// Adds every lane's n to *counter with one atomicAdd per warp.  Must be
+// reached by all 32 lanes of the warp.
+__device__ __forceinline__ void warp_push_n(uint32_t* counter, uint32_t n)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) n += __shfl_xor_sync(kFull, n, off);
+    if (lane_id() == 0u && n) atomicAdd(counter, n);
 }
 
 // Renderer.cu:339: the light a shading point samples, PcgHash(seed) % lights
@@ -444,6 +456,157 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
     }
 }
 
+// The sparse late bounces (b >= b0) of scenes with a light buffer in one
+// persistent launch: a block keeps a pool of rays to trace (path id and
+// bounce) in shared memory, refilled with chunks of bounce b0's queue (one
+// atomic claim per chunk), and carries each path through all its remaining
+// bounces: a round traces up to a block of pool rays, gathers the hits and
+// shades them on full warps (as k_bounce), and puts the continuing rays back
+// into the pool.  Late bounces hold few rays, so separate launches would be
+// mostly launch latency and tails.  A path's bounces run in order in one
+// block, so its colour sums are in the reference's order.
+template <int IS>
+__global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
+    k_paths(SceneView sc, WaveState ws, WaveJob job, int b0)
+{
+    constexpr bool SMEM = IS == kIsSmem;
+    constexpr uint32_t kPool = 2u * kExtendThreads;
+    extern __shared__ float4 s_sph[];
+    __shared__ uint32_t p_pid[kPool];
+    __shared__ uint16_t p_bounce[kPool];   // bounces are at most 4096
+    __shared__ uint32_t h_pid[kExtendThreads], h_id[kExtendThreads];
+    __shared__ float h_t[kExtendThreads];
+    __shared__ uint16_t h_bounce[kExtendThreads];
+    __shared__ uint32_t p_n, h_n, chunk;
+    __shared__ bool dry;                      // bounce b0's queue is used up
+    const uint32_t n0 = ws.counters[2 * b0];  // bounce b0's queue
+    if (n0 == 0u) return;
+    if (SMEM) stage_spheres(sc, s_sph);   // ends with a barrier
+    const float4* sph = SMEM ? s_sph : sc.sph;
+    const uint32_t* q0 = (b0 & 1) ? ws.q[1] : ws.q[0];
+    uint32_t* claim = &ws.counters[2 * ((uint32_t)job.max_bounces + 1u) + 2u];
+    uint32_t rays = 0u, traced = 0u;   // this thread's rays after bounce b0, shadow rays
+    if (threadIdx.x == 0) {
+        p_n = 0u;
+        dry = false;
+    }
+    __syncthreads();
+
+    for (;;) {   // ends: every round takes rays off the pool, which only the queue refills
+        if (!dry && p_n < blockDim.x) {   // block-uniform: refill from bounce b0's queue
+            if (threadIdx.x == 0) {
+                chunk = atomicAdd(claim, blockDim.x);
+                dry = chunk >= n0;
+            }
+            __syncthreads();
+            const uint32_t c0 = chunk;
+            if (c0 < n0) {
+                const uint32_t take = min(blockDim.x, n0 - c0), at = p_n;
+                if (threadIdx.x < take) {
+                    p_pid[at + threadIdx.x] = q0[c0 + threadIdx.x];
+                    p_bounce[at + threadIdx.x] = (uint16_t)b0;
+                }
+                __syncthreads();
+                if (threadIdx.x == 0) p_n = at + take;
+            }
+            __syncthreads();
+        }
+        const uint32_t np = p_n;
+        if (np == 0u) break;
+
+        // trace up to a block of pool rays (from the top of the pool)
+        const uint32_t take = min(np, blockDim.x);
+        if (threadIdx.x == 0) h_n = 0u;
+        __syncthreads();
+        {
+            bool found = false;
+            uint32_t pid = 0u, b = 0u;
+            int32_t hit = -1;
+            float tmin = 0.0f;
+            if (threadIdx.x < take) {
+                pid = p_pid[np - 1u - threadIdx.x];
+                b = p_bounce[np - 1u - threadIdx.x];
+                const float4 ro = ws.ray_o[pid];
+                const float4 rd = ws.ray_d[pid];
+                hit = scene_nearest_from<IS>(sc, sph, __float_as_uint(rd.w), mk3(ro.x, ro.y, ro.z),
+                                             mk3(rd.x, rd.y, rd.z), tmin);
+                found = hit >= 0;
+                if (b > (uint32_t)b0) ++rays;
+                if (!found && job.sky) {   // Renderer.cu:311-316: the path ends in the sky
+                    const float4 tt = ws.thr[pid];
+                    const float3 add = mul3(mk3(0.6f, 0.7f, 0.9f), mk3(tt.x, tt.y, tt.z));
+                    float4 c = ws.col[pid];
+                    c.x = c.x + add.x;
+                    c.y = c.y + add.y;
+                    c.z = c.z + add.z;
+                    ws.col[pid] = c;
+                }
+            }
+            const uint32_t k = warp_push(&h_n, found);
+            if (found) {
+                h_pid[k] = pid;
+                h_id[k] = (uint32_t)hit;
+                h_t[k] = tmin;
+                h_bounce[k] = (uint16_t)b;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) p_n = np - take;
+        __syncthreads();
+
+        // shade the hits on full warps; continuing paths go back to the pool
+        const uint32_t nh = h_n;
+        Shaded r{};
+        uint32_t pid = 0u, seed = 0u, own = ~0u, b = 0u;
+        float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o;
+        if (threadIdx.x < nh) {
+            pid = h_pid[threadIdx.x];
+            b = h_bounce[threadIdx.x];
+            const float4 ro = ws.ray_o[pid];
+            const float4 rd = ws.ray_d[pid];
+            const float4 tt = ws.thr[pid];
+            o = mk3(ro.x, ro.y, ro.z);
+            seed = __float_as_uint(ro.w) + b;
+            d = mk3(rd.x, rd.y, rd.z);
+            thr = mk3(tt.x, tt.y, tt.z);
+            const bool last = (int)b + 1 >= job.max_bounces;
+            shade_hit<SMEM, true>(sc, sph, ws, pid, (int32_t)h_id[threadIdx.x], h_t[threadIdx.x], o, d, thr, own, seed,
+                                  last, false, 0u, r);
+            if (r.touch || r.lit) {
+                // emission of bounce b, then its light
+                float4 c = ws.col[pid];
+                if (r.touch) {
+                    c.x = c.x + r.add.x;
+                    c.y = c.y + r.add.y;
+                    c.z = c.z + r.add.z;
+                }
+                if (r.lit) {
+                    c.x = c.x + r.lc.x;
+                    c.y = c.y + r.lc.y;
+                    c.z = c.z + r.lc.z;
+                }
+                ws.col[pid] = c;
+            }
+            traced += r.traced_sh ? 1u : 0u;
+            if (r.push_next) {
+                ws.ray_o[pid] = make_float4(o.x, o.y, o.z, __uint_as_float(seed));
+                ws.ray_d[pid] = make_float4(d.x, d.y, d.z, __uint_as_float(own));
+                ws.thr[pid] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+            }
+        }
+        const uint32_t k = warp_push(&p_n, r.push_next);
+        if (r.push_next) {
+            p_pid[k] = pid;
+            p_bounce[k] = (uint16_t)(b + 1u);
+        }
+        __syncthreads();
+    }
+    // statistics: rays after bounce b0 into bounce b0+1's queue slot, shadow
+    // rays into bounce b0's (only their sums over bounces are read)
+    if (b0 + 1 < job.max_bounces) warp_push_n(&ws.counters[2 * (b0 + 1)], rays);
+    warp_push_n(&ws.counters[2 * b0 + 1], traced);
+}
+
 // Whether the sphere a shadow ray leaves from (own, an index into the table)
 // occludes it, with the brute-force test.  Testing it first changes nothing
 // but the time: "occluded" means some sphere has t > 0 and t*t < dist2, in any
@@ -710,6 +873,7 @@ cudaError_t occupancy(int threads, size_t bytes, int* ext, int* sh, int* pr)
         if constexpr (IS != kIsBvh) {
             if (e == cudaSuccess) e = cudaFuncSetAttribute(k_first<IS, false, true>, a, b);
             if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bounce<IS, true>, a, b);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_paths<IS>, a, b);
         }
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_primary<IS>, a, b);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shadow<IS, false>, a, b);
@@ -794,6 +958,15 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
             }
             ++nl;
             for (int b = 0; b < bounces; ++b) {
+                if constexpr (IS != kIsBvh) {
+                    if (inl && b >= kPathsFrom) {   // the late bounces in one persistent launch
+                        begin(kFamExtend);
+                        k_paths<IS><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
+                        end(kFamExtend);
+                        ++nl;
+                        break;
+                    }
+                }
                 if (b > 0) {
                     begin(kFamExtend);
                     if constexpr (IS != kIsBvh) {
