@@ -9,6 +9,8 @@
 //                    direction.  Survivors go to the extension queue.
 //   k_bounce         bounce b >= 1: nearest hit, then the same shading, with
 //                    the block's hits gathered in shared memory first.
+//   k_paths          with a light buffer, bounces >= 2 in one persistent
+//                    launch: each block carries a pool of paths to the end.
 //   k_shadow         any-hit over a shadow queue: the first bounce's (pixel,
 //                    light) rays, and per-sample shadow rays of scenes without
 //                    a light buffer (with one they are tested in k_first /
