@@ -413,11 +413,15 @@ atx_status Renderer::render(uint32_t spp)
     // One wave per lane when it fits: fewer, fuller kernels (the state is
     // allocated for this launch's paths, rounded up to 1 Mi, and kept).  All
     // lanes unless the caller fixed the wave size, kernels are being timed
-    // one by one, or the launch is too small to fill them.
+    // one by one, or the launch is too small to fill them.  Scenes with light
+    // and direction buffers run their late bounces in one persistent launch
+    // and overlap best on two lanes (medium scene: 2 lanes +4% over 4); LBVH
+    // scenes use all four (large scene: 4 lanes +11% over 2).
     const uint64_t px = (uint64_t)width_ * height_;
     const bool profile = (cfg_.flags & ATX_FLAG_PROFILE_KERNELS) != 0;
-    const uint32_t lanes =
-        (cfg_.wave_paths || profile || px < (uint64_t)kLanes || px * spp < (4ull << 20) * kLanes) ? 1u : kLanes;
+    const uint32_t max_lanes = (!scene_.view.use_bvh && scene_.view.lb.n_lights) ? kBufferedLanes : kLanes;
+    const uint32_t lanes = (cfg_.wave_paths || profile || px < (uint64_t)max_lanes ||
+                            px * spp < (4ull << 20) * max_lanes) ? 1u : max_lanes;
     const uint64_t lane_px = (px + lanes - 1) / lanes;
     uint32_t capacity = cfg_.wave_paths;
     if (!capacity) {

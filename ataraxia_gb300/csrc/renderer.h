@@ -132,6 +132,7 @@ private:
     // bounces overlap the others' work instead of leaving SMs idle.  Lane 0
     // is the renderer's stream.
     static constexpr int kLanes = 4;
+    static constexpr int kBufferedLanes = 2;   // lanes for scenes with light and direction buffers
     WaveStore wave_[kLanes];
     cudaStream_t lane_stream_[kLanes] = {};
     cudaEvent_t fork_ = nullptr, join_[kLanes] = {};
