@@ -341,7 +341,7 @@ def run_ours(args, dist: Dist):
         "config": {"workload": "medium scene: 256 spheres, 64 materials, 8 lights, 1920x1080, 8 bounces, "
                                "16 spp per launch (one step = one launch)",
                    "paths_per_step": paths_step, "parallelism": f"replicas x{dist.world}",
-                   "l2": "working set > L2: four lanes of up to 8 Mi-path wave state (1.1 GB each) per launch"},
+                   "l2": "working set > L2: two lanes of 16.6 Mi-path wave state (2.3 GB each) per launch"},
         "mrays_per_s": round(mrays, 1),
         "gpu_launches": int(launches),
         "clocks": clk,
