@@ -229,7 +229,7 @@ atx_status Batch::autotune(uint32_t passes, atx_batch_tuning* chosen)
         if (p && p->frame != 1) return fail(ATX_ERR_INVALID_ARG, "batch_autotune: scenes must be at frame 1");
     if (!passes) passes = 2;
     // lanes x path state per lane (Mi paths); at 136 B per path the largest is ~37 GB
-    const uint32_t cand[][2] = {{4, 32}, {8, 16}, {8, 32}, {16, 8}, {16, 16}};
+    const uint32_t cand[][2] = {{2, 64}, {4, 32}, {4, 16}, {8, 16}, {8, 32}, {16, 8}, {16, 16}};
     double best = 1e300;
     atx_batch_tuning pick = tuning_;
     auto reset_frames = [&]() {

@@ -288,7 +288,7 @@ ATX_API atx_status atx_batch_get_stats(atx_batch* b, atx_batch_stats* stats);
 ATX_API atx_status atx_batch_set_tuning(atx_batch* b, const atx_batch_tuning* tuning);
 ATX_API atx_status atx_batch_get_tuning(atx_batch* b, atx_batch_tuning* tuning);
 /* Times passes of the batch's current scenes (at their set spp) under lane
- * counts 4-16 and lane path state 8-32 Mi paths (at most ~37 GB of path
+ * counts 2-16 and lane path state 8-64 Mi paths (at most ~37 GB of path
  * state) and keeps the fastest; `passes` timed passes per setting (0 = 2).
  * Every scene must be at frame 1 (nothing rendered yet) and is reset to frame
  * 1 afterwards, so the tuning passes leave no trace in the images. */
