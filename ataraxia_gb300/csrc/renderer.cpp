@@ -381,6 +381,24 @@ atx_status Renderer::set_camera_matrices(const float inv_view[16], const float i
     return ATX_OK;
 }
 
+atx_status Renderer::refresh_dirs()
+{
+    // the table depends on the matrices and the viewport, not on the eye
+    camv_.dirs = nullptr;
+    const bool same = dirs_valid_ && dirs_cam_.width == camv_.width && dirs_cam_.height == camv_.height &&
+                      std::memcmp(dirs_cam_.inv_proj, camv_.inv_proj, sizeof(camv_.inv_proj)) == 0 &&
+                      std::memcmp(dirs_cam_.inv_view, camv_.inv_view, sizeof(camv_.inv_view)) == 0;
+    if (!same) {
+        const uint64_t px = (uint64_t)camv_.width * camv_.height;
+        ATX_TRY(dirs_.ensure(px * sizeof(float4), &budget_, "primary directions"));
+        ATX_CUDA(enqueue_dir_table(camv_, dirs_.as<float4>(), stream_));
+        dirs_cam_ = camv_;
+        dirs_valid_ = true;
+    }
+    camv_.dirs = dirs_.as<float4>();
+    return ATX_OK;
+}
+
 atx_status Renderer::refresh_camera()
 {
     camv_.width = width_;
@@ -434,6 +452,7 @@ atx_status Renderer::render(uint32_t spp)
         ATX_TRY(wave_[l].ensure(capacity, bounces > 0 ? (uint32_t)bounces : 0u, &budget_));
         wave_[l].view.totals = totals_.as<unsigned long long>();
     }
+    ATX_TRY(refresh_dirs());
 
     if (!settings_.accumulation) frame_ = 1;
     const uint32_t f0 = frame_;

@@ -108,6 +108,7 @@ public:
 private:
     atx_status activate() const;
     atx_status refresh_camera();
+    atx_status refresh_dirs();   // the primary-direction table for camv_
     atx_status ensure_shape();
 
     atx_config cfg_;
@@ -137,6 +138,11 @@ private:
     cudaStream_t lane_stream_[kLanes] = {};
     cudaEvent_t fork_ = nullptr, join_[kLanes] = {};
     DeviceBuffer accum_, image_, totals_;
+    // Primary directions for the camera they were computed for (dirs_cam_):
+    // rebuilt when the camera's matrices or the viewport change.
+    DeviceBuffer dirs_;
+    CameraView dirs_cam_{};
+    bool dirs_valid_ = false;
     LaunchShape shape_{};
     bool shape_valid_ = false;
 

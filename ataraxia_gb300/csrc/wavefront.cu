@@ -76,6 +76,17 @@ __device__ __forceinline__ void warp_push_n(uint32_t* counter, uint32_t n)
     if (lane_id() == 0u && n) atomicAdd(counter, n);
 }
 
+// The primary direction of wave pixel p: from the camera's per-pixel table
+// when it has one (the same function filled it), else computed.
+__device__ __forceinline__ float3 primary_ray(const CameraView& cam, uint32_t p)
+{
+    if (cam.dirs) {
+        const float4 v = __ldg(&cam.dirs[p]);
+        return mk3(v.x, v.y, v.z);
+    }
+    return primary_dir(cam, p % cam.width, p / cam.width);
+}
+
 // Renderer.cu:339: the light a shading point samples, PcgHash(seed) % lights
 // (the seed is not advanced), the remainder by multiplication (fastmod).
 __device__ __forceinline__ uint32_t light_pick(const SceneView& sc, uint32_t seed)
@@ -133,10 +144,10 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
                 const uint2 pr = prim[j];
                 id = (int32_t)pr.y;
                 t = __uint_as_float(pr.x);
-                if (vis && id >= 0) d = primary_dir(cam, p % cam.width, p / cam.width);
+                if (vis && id >= 0) d = primary_ray(cam, p);
             }
         } else {
-            if (me) d = primary_dir(cam, p % cam.width, p / cam.width);
+            if (me) d = primary_ray(cam, p);
             WarpCone cone;
             if (IS != kIsBvh && warp_cone(me, d, cone)) id = nearest_cone<SMEM>(sph, sc.n_sph, o, d, me, cone, t);
             else if (me) id = scene_nearest<IS>(sc, sph, o, d, t);
@@ -320,7 +331,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
             pid = j * job.spp + smp;
             const uint32_t p = job.pixel0 + j;
             o = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
-            d = primary_dir(cam, p % cam.width, p / cam.width);
+            d = primary_ray(cam, p);
             thr = mk3(1.f, 1.f, 1.f);
             seed = p * (job.frame0 + smp);   // bounce 0: seed += 0
             float tmin;
@@ -827,6 +838,17 @@ __global__ void __launch_bounds__(kThreads) k_trace(SceneView sc, const float* _
     }
 }
 
+// The camera's per-pixel direction table (CameraView::dirs).
+__global__ void k_dir_table(CameraView cam, float4* out)
+{
+    const uint64_t n = (uint64_t)cam.width * cam.height;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float3 d = primary_dir(cam, (uint32_t)(i % cam.width), (uint32_t)(i / cam.width));
+        out[i] = make_float4(d.x, d.y, d.z, 0.0f);
+    }
+}
+
 __global__ void k_primary_dirs(CameraView cam, float* out)
 {
     const uint64_t n = (uint64_t)cam.width * cam.height;
@@ -1017,6 +1039,14 @@ cudaError_t enqueue_trace_nearest(const SceneView& sc, const float* origins, con
         if (e == cudaSuccess) k_trace<IS><<<g, kThreads, bytes, stream>>>(sc, origins, dirs, n, t_out, id_out);
     });
     if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_dir_table(const CameraView& cam, float4* out, cudaStream_t stream)
+{
+    const uint64_t n = (uint64_t)cam.width * cam.height;
+    if (n == 0) return cudaSuccess;
+    k_dir_table<<<grid_for(n, kThreads, 4096), kThreads, 0, stream>>>(cam, out);
     return cudaGetLastError();
 }
 

@@ -128,6 +128,10 @@ struct CameraView {
     float pos[3];
     uint32_t width;
     uint32_t height;
+    // Optional per-pixel primary directions for this camera and viewport
+    // (xyz, w unused), as the reference keeps them between camera changes
+    // (Camera.cpp:161-195); nullptr: computed where needed.
+    const float4* dirs;
 };
 
 // Per-wave path state, structure of arrays of float4 rows.
@@ -251,5 +255,8 @@ cudaError_t enqueue_trace_nearest(const SceneView& sc, const float* origins, con
 
 // Writes W*H*3 primary directions (debug / parity hook).
 cudaError_t enqueue_primary_dirs(const CameraView& cam, float* out, cudaStream_t stream);
+
+// Fills the camera's per-pixel direction table (W*H float4, see CameraView::dirs).
+cudaError_t enqueue_dir_table(const CameraView& cam, float4* out, cudaStream_t stream);
 
 }  // namespace atx
