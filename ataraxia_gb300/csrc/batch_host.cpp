@@ -12,7 +12,7 @@ namespace {
 constexpr uint32_t kDefaultLanes = 8;
 constexpr uint32_t kMaxLanes = 64;
 constexpr uint32_t kDefaultLaneWavePaths = 16u << 20;  // 16 Mi paths (about 2.2 GB of path state) per lane
-constexpr uint32_t kDefaultBvhThreshold = 512;   // fastest of 256-1024 on the 64-scene mix
+constexpr uint32_t kDefaultBvhThreshold = 1025;  // LBVH above the direction buffer's 1,024 spheres (64-scene mix: +23% over 512)
 
 // Relative device time of one pass of a scene: paths x (1 + B/2) rays, each
 // N brute-force tests or an LBVH walk, plus a fixed cost per dependent launch
@@ -111,6 +111,7 @@ atx_status Batch::add_scene(const atx_batch_scene& d, uint32_t* id)
     s->accum.use_stream_order(&order_);
     s->image.use_stream_order(&order_);
     s->prim.use_stream_order(&order_);
+    s->dirs.use_stream_order(&order_);
     // on the upload stream: a pass running on the batch stream is not waited for
     ATX_TRY(s->scene.upload(d.spheres, d.n_spheres, d.materials, d.n_materials, d.lights, d.n_lights, &budget_,
                             up_stream_));
@@ -118,8 +119,7 @@ atx_status Batch::add_scene(const atx_batch_scene& d, uint32_t* id)
     ATX_TRY(s->accum.ensure(px * sizeof(float4), &budget_, "batch accumulator"));
     ATX_TRY(s->image.ensure(px * sizeof(uint32_t), &budget_, "batch image"));
     ATX_TRY(s->prim.ensure(px * sizeof(uint2), &budget_, "batch primary hits"));
-    ATX_CUDA(cudaEventRecord(uploaded_, up_stream_));
-    ATX_CUDA(plan_launch(s->scene.view, cfg_.device, (int)tuning_.threads, &s->shape));
+    ATX_TRY(s->dirs.ensure(px * sizeof(float4), &budget_, "batch primary directions"));
     s->w = d.width;
     s->h = d.height;
     s->settings = d.settings;
@@ -128,6 +128,11 @@ atx_status Batch::add_scene(const atx_batch_scene& d, uint32_t* id)
     std::memcpy(s->cam.pos, d.camera.position, sizeof(s->cam.pos));
     s->cam.width = d.width;
     s->cam.height = d.height;
+    s->cam.dirs = nullptr;
+    ATX_CUDA(enqueue_dir_table(s->cam, s->dirs.as<float4>(), up_stream_));
+    s->cam.dirs = s->dirs.as<float4>();
+    ATX_CUDA(cudaEventRecord(uploaded_, up_stream_));
+    ATX_CUDA(plan_launch(s->scene.view, cfg_.device, (int)tuning_.threads, &s->shape));
     uint32_t i = 0;   // reuse a free id
     while (i < slots_.size() && slots_[i]) ++i;
     if (i == slots_.size()) slots_.emplace_back();
@@ -195,6 +200,9 @@ atx_status Batch::set_camera(uint32_t id, const atx_camera& c)
     s->desc = c;
     camera_matrices(c, s->w, s->h, nullptr, s->cam.inv_view, nullptr, s->cam.inv_proj);
     std::memcpy(s->cam.pos, c.position, sizeof(s->cam.pos));
+    // passes already queued may still read the old direction table: from now
+    // on the scene's directions are computed where needed
+    s->cam.dirs = nullptr;
     s->frame = 1;   // a moved camera restarts the accumulation (main.cpp:24-29)
     s->prim_valid = false;
     return ATX_OK;

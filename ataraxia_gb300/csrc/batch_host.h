@@ -66,6 +66,7 @@ private:
         SceneStore scene;
         DeviceBuffer accum, image;
         DeviceBuffer prim;          // per-pixel primary hits, traced once per camera (8 B/pixel)
+        DeviceBuffer dirs;          // per-pixel primary directions of the camera it was added with (16 B/pixel)
         bool prim_valid = false;
         atx_camera desc{};
         CameraView cam{};

@@ -99,7 +99,7 @@ typedef struct atx_config {
     int32_t device;            /* CUDA device ordinal */
     uint32_t wave_paths;       /* paths in flight per wave; 0 = autotuned default */
     uint32_t threads;          /* threads per block; 0 = default */
-    uint32_t bvh_threshold;    /* sphere count at which the LBVH replaces the brute-force loop; 0 = autotuned */
+    uint32_t bvh_threshold;    /* sphere count at which the LBVH replaces the brute-force tables; 0 = 1025 */
     uint32_t bvh_leaf_size;    /* spheres per BVH leaf; 0 = autotuned */
     uint32_t flags;            /* ATX_FLAG_* */
     uint64_t hbm_budget_bytes; /* device bytes this renderer may hold; 0 = unlimited */

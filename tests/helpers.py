@@ -54,14 +54,14 @@ def frac_outside(a: np.ndarray, ref: np.ndarray, rel: float = 1e-3, floor: float
 
 
 def job_bytes_bound(sc):
-    """Upper bound of a served job's device bytes: accumulator, image and primary hits, scene
-    tables, and the LBVH (512 spheres and up) or the light and direction buffers (below)."""
+    """Upper bound of a served job's device bytes: accumulator, image, primary hits and primary
+    directions, scene tables, and the LBVH (1,025 spheres and up) or the light and direction buffers."""
     n, nl = len(sc.spheres), len(sc.lights)
     px = sc.width * sc.height
     tables = 24 * n + 48 * len(sc.materials) + 32 * nl + 8 * 256
-    bvh = 200 * n if n >= 512 else 0
+    bvh = 200 * n if n >= 1025 else 0
     cells = 6 * 16 * 16 * 65          # per light / per sphere: a count and 32 indices per direction cell
     cones = 6 * 16 * 16 * 20 + 4096   # build scratch: the cells' bounding cones
-    lb = cells * nl + cones if n < 512 and 1 <= nl <= 64 else 0
-    db = cells * n + cones if n < 512 else 0
-    return tables + bvh + lb + db + 28 * px + 512
+    lb = cells * nl + cones if n < 1025 and 1 <= nl <= 64 else 0
+    db = cells * n + cones if n < 1025 else 0
+    return tables + bvh + lb + db + 44 * px + 1024
