@@ -7,14 +7,17 @@
 //   k_first          bounce 0 over (hit pixel, sample): shading, light pick
 //                    and the shadow ray, Russian roulette and the next
 //                    direction.  Survivors go to the extension queue.
-//   k_bounce         bounce b >= 1: nearest hit, then the same shading, with
-//                    the block's hits gathered in shared memory first.
-//   k_paths          with a light buffer, bounces >= 2 in one persistent
-//                    launch: each block carries a pool of paths to the end.
+//   k_bounce         bounce b >= 1 (LBVH scenes): nearest hit, then the same
+//                    shading, with the block's hits gathered in shared memory
+//                    first.
+//   With a light buffer and a direction buffer (scenes up to 1,024 spheres)
+//   shadow rays are tested right after the shading and a continuation ray is
+//   traced where it is made, so only rays that hit are queued:
+//   k_shade          bounce 1: shades its queue of hits on full warps.
+//   k_paths          bounces >= 2 in one persistent launch: each block
+//                    carries a pool of paths to the end.
 //   k_shadow         any-hit over a shadow queue: the first bounce's (pixel,
-//                    light) rays, and per-sample shadow rays of scenes without
-//                    a light buffer (with one they are tested in k_first /
-//                    k_bounce right after the shading).
+//                    light) rays, and per-sample shadow rays of LBVH scenes.
 //   k_accumulate     adds the wave's per-sample colours to the float4
 //                    accumulator in frame order (Renderer.cu:165) and packs
 //                    the RGBA8 image (Renderer.cu:166-168).
@@ -297,6 +300,31 @@ __device__ __forceinline__ void push_shaded(const WaveState& ws, uint32_t* qout,
     }
 }
 
+// With a light buffer (INL) a continuation ray is traced where shading makes
+// it, and only a ray that hits is queued: its record carries the hit (ray_o:
+// origin, seed; ray_d: direction, t; thr: throughput, sphere).  A ray that
+// misses ends its path there, and the sky term of the next bounce
+// (Renderer.cu:311-316, sky_term) goes into the colour after this bounce's
+// terms, as the reference's loop adds it.
+__device__ __forceinline__ float3 sky_term(float3 c, float3 thr)
+{
+    return add3(c, mul3(mk3(0.6f, 0.7f, 0.9f), thr));
+}
+
+// Queues a traced continuation ray that hits (all 32 lanes of the warp call it).
+__device__ __forceinline__ void push_hit(const WaveState& ws, uint32_t* qout, uint32_t* counter, bool push,
+                                         uint32_t pid, float3 o, uint32_t seed, float3 d, float t, float3 thr,
+                                         int32_t hit)
+{
+    const uint32_t sn = warp_push(counter, push);
+    if (push) {
+        qout[sn] = pid;
+        ws.ray_o[pid] = make_float4(o.x, o.y, o.z, __uint_as_float(seed));
+        ws.ray_d[pid] = make_float4(d.x, d.y, d.z, t);
+        ws.thr[pid] = make_float4(thr.x, thr.y, thr.z, __uint_as_float((uint32_t)hit));
+    }
+}
+
 // The first bounce over (pixel, sample) paths.  SHARED: the nearest hit comes
 // from k_primary's per-pixel record instead of tracing the primary ray again,
 // and idx enumerates (hit pixel, sample).
@@ -318,6 +346,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
     // per-(pixel, light) shadow rays: the light of a sample is added here when
     // k_shadow found it visible from the pixel's hit
     const bool vis = SHARED && wave_light_vis(job, sc.n_lights);
+    uint32_t missed = 0u;   // INL: continuation rays traced here that missed
 
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t idx = base + threadIdx.x;
@@ -325,6 +354,8 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
         uint32_t pid = 0u, seed = 0u, own = ~0u;
         bool shaded = false;
         float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o;
+        int32_t nhit = -1;   // INL: the next ray's hit
+        float nt = 0.0f;
         if (idx < n) {
             const uint32_t j = SHARED ? ws.hitq[idx / job.spp] : idx / job.spp;   // path ids stay pixel-major
             const uint32_t smp = idx % job.spp;
@@ -354,12 +385,26 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
             }
             float3 c = add3(mk3(0.f, 0.f, 0.f), r.add);
             if (r.lit) c = add3(c, r.lc);   // as k_shadow adds it: after the emission
+            if (INL && r.push_next) {
+                nhit = scene_nearest_from<IS>(sc, sph, own, o, d, nt);
+                r.push_next = nhit >= 0;
+                if (!r.push_next) {
+                    ++missed;
+                    if (job.sky) c = sky_term(c, thr);
+                }
+            }
             ws.col[pid] = make_float4(c.x, c.y, c.z, 0.0f);
         }
         // count the shaded paths (SHARED: every path of the launch is one)
         if (!SHARED) warp_push(&ws.counters[2 * ((uint32_t)job.max_bounces + 1u) + 1u], shaded);
-        push_shaded<INL>(ws, ws.q[1], 0, pid, r, o, d, thr, own, seed);
+        if (INL) {
+            warp_push(&ws.counters[1], r.traced_sh);   // count the shadow rays tested here
+            push_hit(ws, ws.q[1], &ws.counters[2], r.push_next, pid, o, seed, d, nt, thr, nhit);
+        } else {
+            push_shaded<INL>(ws, ws.q[1], 0, pid, r, o, d, thr, own, seed);
+        }
     }
+    if (INL) warp_push_n(&ws.counters[2 * ((uint32_t)job.max_bounces + 1u) + 3u], missed);
 }
 
 // Bounce b >= 1 over the extension queue, in rounds of two phases per block.
@@ -369,7 +414,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
 // worth of hits, or the queue is done, every thread shades one.  Most rays
 // after the first bounce leave the scene, so shading (the larger part of the
 // work) then runs on full warps instead of on the few lanes that hit.
-template <int IS, bool INL>
+template <int IS>
 __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
     k_bounce(SceneView sc, WaveState ws, WaveJob job, int bounce)
 {
@@ -445,7 +490,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
             seed = __float_as_uint(ro.w) + (uint32_t)bounce;
             d = mk3(rd.x, rd.y, rd.z);
             thr = mk3(tt.x, tt.y, tt.z);
-            shade_hit<SMEM, INL>(sc, sph, ws, pid, hit, tmin, o, d, thr, own, seed, last, false, 0u, r);
+            shade_hit<SMEM, false>(sc, sph, ws, pid, hit, tmin, o, d, thr, own, seed, last, false, 0u, r);
             if (r.touch || r.lit) {
                 // emission of bounce b, then its light (the order k_shadow adds it in)
                 float4 c = ws.col[pid];
@@ -462,22 +507,91 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
                 ws.col[pid] = c;
             }
         }
-        push_shaded<INL>(ws, qout, bounce, pid, r, o, d, thr, own, seed);
+        push_shaded<false>(ws, qout, bounce, pid, r, o, d, thr, own, seed);
         __syncthreads();   // every thread has read its entry
         if (threadIdx.x == 0) h_n = nh - take;
         __syncthreads();
     }
 }
 
+// Adds the terms of one shaded bounce to a path's colour in the reference's
+// order: emission, then the light (then, by the caller, the sky when the
+// continuation missed).
+__device__ __forceinline__ float3 bounce_terms(float3 c, const Shaded& r)
+{
+    if (r.touch) c = add3(c, r.add);
+    if (r.lit) c = add3(c, r.lc);
+    return c;
+}
+
+// Bounce b >= 1 of scenes with a light buffer: every queued ray hits (it was
+// traced where it was made), so each thread shades one, on full warps, then
+// traces its continuation and queues it if it hits.
+template <int IS>
+__global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
+    k_shade(SceneView sc, WaveState ws, WaveJob job, int bounce)
+{
+    constexpr bool SMEM = IS == kIsSmem;
+    extern __shared__ float4 s_sph[];
+    const uint32_t n = ws.counters[2 * bounce];
+    if (blockIdx.x * blockDim.x >= n) return;
+    if (SMEM) stage_spheres(sc, s_sph);
+    const float4* sph = SMEM ? s_sph : sc.sph;
+    // select, not index: a runtime index into the parameter's array would
+    // copy the whole WaveState to local memory
+    const uint32_t* qin = (bounce & 1) ? ws.q[1] : ws.q[0];
+    uint32_t* qout = (bounce & 1) ? ws.q[0] : ws.q[1];
+    const bool last = bounce + 1 >= job.max_bounces;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t missed = 0u;   // continuation rays traced here that missed
+
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t idx = base + threadIdx.x;
+        Shaded r{};
+        uint32_t pid = 0u, seed = 0u, own = ~0u;
+        float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o;
+        int32_t nhit = -1;
+        float nt = 0.0f;
+        if (idx < n) {
+            pid = qin[idx];
+            const float4 ro = ws.ray_o[pid];
+            const float4 rd = ws.ray_d[pid];
+            const float4 tt = ws.thr[pid];
+            o = mk3(ro.x, ro.y, ro.z);
+            seed = __float_as_uint(ro.w) + (uint32_t)bounce;
+            d = mk3(rd.x, rd.y, rd.z);
+            thr = mk3(tt.x, tt.y, tt.z);
+            shade_hit<SMEM, true>(sc, sph, ws, pid, (int32_t)__float_as_uint(tt.w), rd.w, o, d, thr, own, seed, last,
+                                  false, 0u, r);
+            bool sky = false;
+            if (r.push_next) {
+                nhit = scene_nearest_from<IS>(sc, sph, own, o, d, nt);
+                r.push_next = nhit >= 0;
+                missed += r.push_next ? 0u : 1u;
+                sky = !r.push_next && job.sky;
+            }
+            if (r.touch || r.lit || sky) {
+                const float4 c0 = ws.col[pid];
+                float3 c = bounce_terms(mk3(c0.x, c0.y, c0.z), r);
+                if (sky) c = sky_term(c, thr);
+                ws.col[pid] = make_float4(c.x, c.y, c.z, c0.w);
+            }
+        }
+        warp_push(&ws.counters[2 * bounce + 1], r.traced_sh);   // count the shadow rays tested here
+        push_hit(ws, qout, &ws.counters[2 * (bounce + 1)], r.push_next, pid, o, seed, d, nt, thr, nhit);
+    }
+    warp_push_n(&ws.counters[2 * ((uint32_t)job.max_bounces + 1u) + 3u], missed);
+}
+
 // The sparse late bounces (b >= b0) of scenes with a light buffer in one
-// persistent launch: a block keeps a pool of rays to trace (path id and
-// bounce) in shared memory, refilled with chunks of bounce b0's queue (one
-// atomic claim per chunk), and carries each path through all its remaining
-// bounces: a round traces up to a block of pool rays, gathers the hits and
-// shades them on full warps (as k_bounce), and puts the continuing rays back
-// into the pool.  Late bounces hold few rays, so separate launches would be
-// mostly launch latency and tails.  A path's bounces run in order in one
-// block, so its colour sums are in the reference's order.
+// persistent launch: a block keeps a pool of paths (path id and bounce) whose
+// next ray hits, in shared memory, refilled with chunks of bounce b0's queue
+// (one atomic claim per chunk), and carries each path through all its
+// remaining bounces: a round shades up to a block of pool paths on full
+// warps, traces their continuations and puts those that hit back into the
+// pool.  Late bounces hold few rays, so separate launches would be mostly
+// launch latency and tails.  A path's bounces run in order in one block, so
+// its colour sums are in the reference's order.
 template <int IS>
 __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
     k_paths(SceneView sc, WaveState ws, WaveJob job, int b0)
@@ -487,10 +601,7 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
     extern __shared__ float4 s_sph[];
     __shared__ uint32_t p_pid[kPool];
     __shared__ uint16_t p_bounce[kPool];   // bounces are at most 4096
-    __shared__ uint32_t h_pid[kExtendThreads], h_id[kExtendThreads];
-    __shared__ float h_t[kExtendThreads];
-    __shared__ uint16_t h_bounce[kExtendThreads];
-    __shared__ uint32_t p_n, h_n, chunk;
+    __shared__ uint32_t p_n, chunk;
     __shared__ bool dry;                      // bounce b0's queue is used up
     const uint32_t n0 = ws.counters[2 * b0];  // bounce b0's queue
     if (n0 == 0u) return;
@@ -498,14 +609,14 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
     const float4* sph = SMEM ? s_sph : sc.sph;
     const uint32_t* q0 = (b0 & 1) ? ws.q[1] : ws.q[0];
     uint32_t* claim = &ws.counters[2 * ((uint32_t)job.max_bounces + 1u) + 2u];
-    uint32_t rays = 0u, traced = 0u;   // this thread's rays after bounce b0, shadow rays
+    uint32_t rays = 0u, traced = 0u;   // this thread's continuation rays, shadow rays
     if (threadIdx.x == 0) {
         p_n = 0u;
         dry = false;
     }
     __syncthreads();
 
-    for (;;) {   // ends: every round takes rays off the pool, which only the queue refills
+    for (;;) {   // ends: every round takes paths off the pool, which only the queue refills
         if (!dry && p_n < blockDim.x) {   // block-uniform: refill from bounce b0's queue
             if (threadIdx.x == 0) {
                 chunk = atomicAdd(claim, blockDim.x);
@@ -527,54 +638,23 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
         const uint32_t np = p_n;
         if (np == 0u) break;
 
-        // trace up to a block of pool rays (from the top of the pool)
+        // shade up to a block of pool paths (from the top of the pool)
         const uint32_t take = min(np, blockDim.x);
-        if (threadIdx.x == 0) h_n = 0u;
-        __syncthreads();
-        {
-            bool found = false;
-            uint32_t pid = 0u, b = 0u;
-            int32_t hit = -1;
-            float tmin = 0.0f;
-            if (threadIdx.x < take) {
-                pid = p_pid[np - 1u - threadIdx.x];
-                b = p_bounce[np - 1u - threadIdx.x];
-                const float4 ro = ws.ray_o[pid];
-                const float4 rd = ws.ray_d[pid];
-                hit = scene_nearest_from<IS>(sc, sph, __float_as_uint(rd.w), mk3(ro.x, ro.y, ro.z),
-                                             mk3(rd.x, rd.y, rd.z), tmin);
-                found = hit >= 0;
-                if (b > (uint32_t)b0) ++rays;
-                if (!found && job.sky) {   // Renderer.cu:311-316: the path ends in the sky
-                    const float4 tt = ws.thr[pid];
-                    const float3 add = mul3(mk3(0.6f, 0.7f, 0.9f), mk3(tt.x, tt.y, tt.z));
-                    float4 c = ws.col[pid];
-                    c.x = c.x + add.x;
-                    c.y = c.y + add.y;
-                    c.z = c.z + add.z;
-                    ws.col[pid] = c;
-                }
-            }
-            const uint32_t k = warp_push(&h_n, found);
-            if (found) {
-                h_pid[k] = pid;
-                h_id[k] = (uint32_t)hit;
-                h_t[k] = tmin;
-                h_bounce[k] = (uint16_t)b;
-            }
+        uint32_t pid = 0u, b = 0u;
+        if (threadIdx.x < take) {
+            pid = p_pid[np - 1u - threadIdx.x];
+            b = p_bounce[np - 1u - threadIdx.x];
         }
         __syncthreads();
         if (threadIdx.x == 0) p_n = np - take;
         __syncthreads();
 
-        // shade the hits on full warps; continuing paths go back to the pool
-        const uint32_t nh = h_n;
         Shaded r{};
-        uint32_t pid = 0u, seed = 0u, own = ~0u, b = 0u;
+        uint32_t seed = 0u, own = ~0u;
         float3 o = mk3(0.f, 0.f, 0.f), d = o, thr = o;
-        if (threadIdx.x < nh) {
-            pid = h_pid[threadIdx.x];
-            b = h_bounce[threadIdx.x];
+        int32_t nhit = -1;
+        float nt = 0.0f;
+        if (threadIdx.x < take) {
             const float4 ro = ws.ray_o[pid];
             const float4 rd = ws.ray_d[pid];
             const float4 tt = ws.thr[pid];
@@ -583,28 +663,26 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
             d = mk3(rd.x, rd.y, rd.z);
             thr = mk3(tt.x, tt.y, tt.z);
             const bool last = (int)b + 1 >= job.max_bounces;
-            shade_hit<SMEM, true>(sc, sph, ws, pid, (int32_t)h_id[threadIdx.x], h_t[threadIdx.x], o, d, thr, own, seed,
-                                  last, false, 0u, r);
-            if (r.touch || r.lit) {
-                // emission of bounce b, then its light
-                float4 c = ws.col[pid];
-                if (r.touch) {
-                    c.x = c.x + r.add.x;
-                    c.y = c.y + r.add.y;
-                    c.z = c.z + r.add.z;
-                }
-                if (r.lit) {
-                    c.x = c.x + r.lc.x;
-                    c.y = c.y + r.lc.y;
-                    c.z = c.z + r.lc.z;
-                }
-                ws.col[pid] = c;
-            }
+            shade_hit<SMEM, true>(sc, sph, ws, pid, (int32_t)__float_as_uint(tt.w), rd.w, o, d, thr, own, seed, last,
+                                  false, 0u, r);
             traced += r.traced_sh ? 1u : 0u;
+            bool sky = false;
+            if (r.push_next) {
+                ++rays;
+                nhit = scene_nearest_from<IS>(sc, sph, own, o, d, nt);
+                r.push_next = nhit >= 0;
+                sky = !r.push_next && job.sky;
+            }
+            if (r.touch || r.lit || sky) {
+                const float4 c0 = ws.col[pid];
+                float3 c = bounce_terms(mk3(c0.x, c0.y, c0.z), r);
+                if (sky) c = sky_term(c, thr);
+                ws.col[pid] = make_float4(c.x, c.y, c.z, c0.w);
+            }
             if (r.push_next) {
                 ws.ray_o[pid] = make_float4(o.x, o.y, o.z, __uint_as_float(seed));
-                ws.ray_d[pid] = make_float4(d.x, d.y, d.z, __uint_as_float(own));
-                ws.thr[pid] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+                ws.ray_d[pid] = make_float4(d.x, d.y, d.z, nt);
+                ws.thr[pid] = make_float4(thr.x, thr.y, thr.z, __uint_as_float((uint32_t)nhit));
             }
         }
         const uint32_t k = warp_push(&p_n, r.push_next);
@@ -614,9 +692,9 @@ __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
         }
         __syncthreads();
     }
-    // statistics: rays after bounce b0 into bounce b0+1's queue slot, shadow
-    // rays into bounce b0's (only their sums over bounces are read)
-    if (b0 + 1 < job.max_bounces) warp_push_n(&ws.counters[2 * (b0 + 1)], rays);
+    // statistics: every continuation ray traced here, shadow rays into bounce
+    // b0's slot (only sums over bounces are read)
+    warp_push_n(&ws.counters[2 * ((uint32_t)job.max_bounces + 1u) + 3u], rays);
     warp_push_n(&ws.counters[2 * b0 + 1], traced);
 }
 
@@ -781,6 +859,7 @@ __global__ void __launch_bounds__(kThreads) k_accumulate(WaveState ws, WaveJob j
             if (b > 0) ext += ws.counters[2 * b];
             sh += ws.counters[2 * b + 1];
         }
+        if (job.max_bounces > 0) ext += ws.counters[2 * ((uint32_t)job.max_bounces + 1u) + 3u];
         atomicAdd(&ws.totals[0], ext);
         atomicAdd(&ws.totals[1], sh);
         if (job.max_bounces > 0) {
@@ -893,10 +972,10 @@ cudaError_t occupancy(int threads, size_t bytes, int* ext, int* sh, int* pr)
         const int b = (int)bytes;
         const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
         cudaError_t e = cudaFuncSetAttribute(k_first<IS, false, false>, a, b);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bounce<IS, false>, a, b);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bounce<IS>, a, b);
         if constexpr (IS != kIsBvh) {
             if (e == cudaSuccess) e = cudaFuncSetAttribute(k_first<IS, false, true>, a, b);
-            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bounce<IS, true>, a, b);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shade<IS>, a, b);
             if (e == cudaSuccess) e = cudaFuncSetAttribute(k_paths<IS>, a, b);
         }
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_primary<IS>, a, b);
@@ -905,7 +984,7 @@ cudaError_t occupancy(int threads, size_t bytes, int* ext, int* sh, int* pr)
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace<IS>, a, b);
         if (e != cudaSuccess) return e;
     }
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ext, k_bounce<IS, false>, kExtendThreads, bytes);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ext, k_bounce<IS>, kExtendThreads, bytes);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(sh, k_shadow<IS, false>, threads, bytes);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(pr, k_primary<IS>, threads, bytes);
     return e;
@@ -994,15 +1073,15 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
                 if (b > 0) {
                     begin(kFamExtend);
                     if constexpr (IS != kIsBvh) {
-                        if (inl) k_bounce<IS, true><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
-                        else k_bounce<IS, false><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
+                        if (inl) k_shade<IS><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
+                        else k_bounce<IS><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
                     } else {
-                        k_bounce<IS, false><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
+                        k_bounce<IS><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
                     }
                     end(kFamExtend);
                     ++nl;
                 }
-                if ((vis && b == 0) || inl) continue;   // tested in k_first / k_bounce
+                if ((vis && b == 0) || inl) continue;   // tested in k_first / k_shade / k_paths
                 begin(kFamShadow);
                 k_shadow<IS, false><<<shape.blocks_shadow, shape.threads, sm, stream>>>(sc, ws, b);
                 end(kFamShadow);

@@ -171,8 +171,11 @@ constexpr uint64_t kWaveArrays = 12;
 // Counter slots after the per-bounce pairs: [2*(max_bounces+1)] = hit pixels,
 // [2*(max_bounces+1)+1] = paths shaded at the first bounce (counted only when
 // the wave does not share primary hits; else it is hit pixels x spp),
-// [2*(max_bounces+1)+2] = rays of k_paths' starting queue claimed so far.
-inline size_t wave_counter_words(int max_bounces) { return 2 * ((size_t)(max_bounces > 0 ? max_bounces : 0) + 1) + 3; }
+// [2*(max_bounces+1)+2] = rays of k_paths' starting queue claimed so far,
+// [2*(max_bounces+1)+3] = extension rays traced that no queue counts (with a
+// light buffer a ray is traced where it is made and only hits are queued:
+// the misses, and every ray k_paths traces).
+inline size_t wave_counter_words(int max_bounces) { return 2 * ((size_t)(max_bounces > 0 ? max_bounces : 0) + 1) + 4; }
 
 // One wave: pixels [pixel0, pixel0 + n_pixels) x samples [0, spp) with the
 // sample s of pixel p at path id (p - pixel0) * spp + s, traced as the
