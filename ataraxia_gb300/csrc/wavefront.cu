@@ -526,7 +526,10 @@ __device__ __forceinline__ float3 bounce_terms(float3 c, const Shaded& r)
 
 // Bounce b >= 1 of scenes with a light buffer: every queued ray hits (it was
 // traced where it was made), so each thread shades one, on full warps, then
-// traces its continuation and queues it if it hits.
+// traces its continuation and queues it if it hits.  Launched over the
+// global sphere table (IS = kIsGlobal): the few spheres a list walk touches
+// come faster from L1 than from the shared-memory pair layout, and no block
+// stages the table.
 template <int IS>
 __global__ void __launch_bounds__(kExtendThreads, kExtendBlocksPerSm)
     k_shade(SceneView sc, WaveState ws, WaveJob job, int bounce)
@@ -975,8 +978,6 @@ cudaError_t occupancy(int threads, size_t bytes, int* ext, int* sh, int* pr)
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bounce<IS>, a, b);
         if constexpr (IS != kIsBvh) {
             if (e == cudaSuccess) e = cudaFuncSetAttribute(k_first<IS, false, true>, a, b);
-            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shade<IS>, a, b);
-            if (e == cudaSuccess) e = cudaFuncSetAttribute(k_paths<IS>, a, b);
         }
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_primary<IS>, a, b);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shadow<IS, false>, a, b);
@@ -1064,7 +1065,7 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
                 if constexpr (IS != kIsBvh) {
                     if (inl && b >= kPathsFrom) {   // the late bounces in one persistent launch
                         begin(kFamExtend);
-                        k_paths<IS><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
+                        k_paths<kIsGlobal><<<shape.blocks_extend, kExtendThreads, 0, stream>>>(sc, ws, job, b);
                         end(kFamExtend);
                         ++nl;
                         break;
@@ -1073,7 +1074,7 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
                 if (b > 0) {
                     begin(kFamExtend);
                     if constexpr (IS != kIsBvh) {
-                        if (inl) k_shade<IS><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
+                        if (inl) k_shade<kIsGlobal><<<shape.blocks_extend, kExtendThreads, 0, stream>>>(sc, ws, job, b);
                         else k_bounce<IS><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
                     } else {
                         k_bounce<IS><<<shape.blocks_extend, kExtendThreads, sm, stream>>>(sc, ws, job, b);
