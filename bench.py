@@ -303,7 +303,7 @@ def run_ours(args, dist: Dist):
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     roofline = {
         "kernel": "one atx_render of the workload: k_primary, k_shadow (first-bounce pixel-light rays), "
-                  "k_first, k_bounce x7, k_accumulate per lane",
+                  "k_first, k_shade (bounce 1), k_paths (bounces 2-7), k_accumulate per lane",
         "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
         "frac": round(achieved / peak, 4) if peak else None,
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth, burst)",
