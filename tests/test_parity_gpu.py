@@ -221,6 +221,32 @@ def test_warp_cone_culling_edge_cases(po, kind):
     assert (rids >= 0).mean() > 0.05    # the primary rays do meet spheres
 
 
+@pytest.mark.parametrize("n", [1024, 1025])
+def test_direction_buffer_limit_and_packed_spheres(po, n):
+    # touching and overlapping spheres (continuation rays leave one sphere and
+    # graze its neighbours), lights in the gaps, at the direction buffer's
+    # 1,024-sphere limit and one sphere above it (the LBVH)
+    st = scenes.Stream(11, "packed")
+    g = int(np.ceil(n ** (1.0 / 3.0)))
+    ijk = np.stack(np.meshgrid(np.arange(g), np.arange(g), np.arange(g), indexing="ij"), -1).reshape(-1, 3)[:n]
+    c = (ijk - (g - 1) / 2.0).astype(np.float64)
+    r = np.where(np.arange(n) % 3 == 0, 0.5, 0.5 + 0.02 * st.uniform(n, 0.0, 1.0))
+    sph = np.zeros(n, dtype=scenes.SPHERE_DTYPE)
+    sph["center"] = c
+    sph["radius"] = r
+    sph["material"] = np.arange(n) % 8
+    lts = np.zeros(4, dtype=scenes.LIGHT_DTYPE)
+    lts["position"] = [[0.5, 0.5, 0.5], [-1.5, 0.5, 2.5], [0.0, 0.3 * g, 1.5 * g], [0.0, 2.0 * g, 0.0]]
+    lts["color"] = 1.0
+    lts["intensity"] = [20.0, 40.0, 800.0, 500.0]
+    sc = scenes.SyntheticScene("packed", sph, scenes.draw_materials(st, 8), lts, (0.0, 0.6 * g, 2.0 * g),
+                               (0.0, -0.6 * g, -2.0 * g), fov=50.0, far=1000.0, width=48, height=32, max_bounces=6)
+    acc, img = gpu_render(sc, 4)
+    ref, _, _ = oracle_render(sc, 4)
+    assert bit_mismatches(acc, ref) == 0
+    assert np.array_equal(img, po.pack_rgba8(ref, 4))
+
+
 def test_empty_scene_no_lights_and_bad_material_ids(po):
     sc = scenes.config0().with_resolution(40, 20)
     empty = scenes.SyntheticScene(**{**sc.__dict__, "spheres": sc.spheres[:0]})
