@@ -24,27 +24,46 @@
 namespace atx {
 
 constexpr float kBvhK = 1.2207031e-3f;
-constexpr int kBvhStack = 64;
 
-// Node box test against the box inflated by M.  Returns the entry distance
-// (may be negative when the origin is inside) or +inf when culled.
-__device__ __forceinline__ float bvh_box_enter(float4 ctr, float4 half, float3 o, float3 inv_d, float limit)
+// Box tests of two slots of a 4-wide node (lbvh.cu k_pack_quads: rows r0..r2
+// hold the two boxes interleaved) against the boxes inflated by M.
+// Each packed f32x2 instruction rounds its two halves as the scalar
+// instruction would, so the results are those of one scalar test per child.
+// Sets t0/t1 to the entry distance (may be negative when the origin is
+// inside) or +inf when culled.  no = -o; x - y is computed as x + (-y), or as
+// fma(y, -1, x): both round the exact difference once.
+__device__ __forceinline__ void bvh_boxes_enter(float4 r0, float4 r1, float4 r2, float3 no, float3 inv_d,
+                                                float limit, float& t0, float& t1)
 {
-    const float dx = ctr.x - o.x, dy = ctr.y - o.y, dz = ctr.z - o.z;
-    const float dmax = (fabsf(dx) + fabsf(dy) + fabsf(dz)) + (half.x + half.y + half.z);
-    const float m = kBvhK * (dmax + 1e-3f);
-    const float hx = half.x + m, hy = half.y + m, hz = half.z + m;
+    const float2 dx = __fadd2_rn(make_float2(r0.x, r0.y), make_float2(no.x, no.x));
+    const float2 dy = __fadd2_rn(make_float2(r0.z, r0.w), make_float2(no.y, no.y));
+    const float2 dz = __fadd2_rn(make_float2(r1.x, r1.y), make_float2(no.z, no.z));
+    const float2 hx = make_float2(r1.z, r1.w), hy = make_float2(r2.x, r2.y), hz = make_float2(r2.z, r2.w);
+    const float2 ad = __fadd2_rn(__fadd2_rn(make_float2(fabsf(dx.x), fabsf(dx.y)), make_float2(fabsf(dy.x), fabsf(dy.y))),
+                                 make_float2(fabsf(dz.x), fabsf(dz.y)));
+    const float2 dmax = __fadd2_rn(ad, __fadd2_rn(__fadd2_rn(hx, hy), hz));
+    const float2 m = __fmul2_rn(make_float2(kBvhK, kBvhK), __fadd2_rn(dmax, make_float2(1e-3f, 1e-3f)));
+    const float2 ex = __fadd2_rn(hx, m), ey = __fadd2_rn(hy, m), ez = __fadd2_rn(hz, m);
+    const float2 neg = make_float2(-1.0f, -1.0f);
     // slab distances; inv_d may be +-inf for zero components, where the
     // products give +-inf or NaN; fminf/fmaxf drop NaN operands.
-    const float tx0 = (dx - hx) * inv_d.x, tx1 = (dx + hx) * inv_d.x;
-    const float ty0 = (dy - hy) * inv_d.y, ty1 = (dy + hy) * inv_d.y;
-    const float tz0 = (dz - hz) * inv_d.z, tz1 = (dz + hz) * inv_d.z;
-    const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
-    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+    const float2 ix = make_float2(inv_d.x, inv_d.x), iy = make_float2(inv_d.y, inv_d.y),
+                 iz = make_float2(inv_d.z, inv_d.z);
+    const float2 tx0 = __fmul2_rn(__ffma2_rn(ex, neg, dx), ix), tx1 = __fmul2_rn(__fadd2_rn(dx, ex), ix);
+    const float2 ty0 = __fmul2_rn(__ffma2_rn(ey, neg, dy), iy), ty1 = __fmul2_rn(__fadd2_rn(dy, ey), iy);
+    const float2 tz0 = __fmul2_rn(__ffma2_rn(ez, neg, dz), iz), tz1 = __fmul2_rn(__fadd2_rn(dz, ez), iz);
+    const float2 tn = make_float2(fmaxf(fmaxf(fminf(tx0.x, tx1.x), fminf(ty0.x, ty1.x)), fminf(tz0.x, tz1.x)),
+                                  fmaxf(fmaxf(fminf(tx0.y, tx1.y), fminf(ty0.y, ty1.y)), fminf(tz0.y, tz1.y)));
+    const float2 tf = make_float2(fminf(fminf(fmaxf(tx0.x, tx1.x), fmaxf(ty0.x, ty1.x)), fmaxf(tz0.x, tz1.x)),
+                                  fminf(fminf(fmaxf(tx0.y, tx1.y), fmaxf(ty0.y, ty1.y)), fmaxf(tz0.y, tz1.y)));
     // slack on the slab distances themselves: relative 1e-5 of their size
-    const float sl = 1e-5f * (fabsf(tn) + fabsf(tf)) + m;
-    if (tf + sl < 0.0f || tn - sl > tf + sl || tn - sl > limit + m) return __int_as_float(0x7f800000);
-    return tn;
+    const float2 sl = __fadd2_rn(
+        __fmul2_rn(make_float2(1e-5f, 1e-5f),
+                   __fadd2_rn(make_float2(fabsf(tn.x), fabsf(tn.y)), make_float2(fabsf(tf.x), fabsf(tf.y)))),
+        m);
+    const float inf = __int_as_float(0x7f800000);
+    t0 = (tf.x + sl.x < 0.0f || tn.x - sl.x > tf.x + sl.x || tn.x - sl.x > limit + m.x) ? inf : tn.x;
+    t1 = (tf.y + sl.y < 0.0f || tn.y - sl.y > tf.y + sl.y || tn.y - sl.y > limit + m.y) ? inf : tn.y;
 }
 
 __device__ __forceinline__ float3 safe_inv(float3 d)
@@ -103,20 +122,58 @@ __device__ __forceinline__ bool leaf_occluded(const BvhView& b, uint32_t first, 
     return false;
 }
 
-// A child of a child-pair node: (ref, count) decoded and bounds-checked.
-// Returns 1 for a leaf cluster (first, cnt set), 2 for an internal node,
-// 0 for a malformed reference (skipped).
-__device__ __forceinline__ int bvh_child(const BvhView& b, uint32_t ref, uint32_t count, uint32_t& first,
-                                         uint32_t& cnt)
+// A slot of a 4-wide node: true when its (ref, count) is well formed (a leaf
+// cluster inside the sorted spheres, or an internal node index); empty slots
+// (ref = ~0, count = 0) and malformed references are skipped.
+__device__ __forceinline__ bool bvh_slot_ok(const BvhView& b, uint32_t ref, uint32_t count)
 {
-    if (count) {
-        if (ref >= b.n_leaves || count > 32u) return 0;
-        first = ref;
-        cnt = min(count, b.n_leaves - ref);
-        return 1;
-    }
-    return ref < b.n_leaves - 1u ? 2 : 0;
+    return count ? (ref < b.n_leaves && count <= 32u) : ref < b.n_leaves - 1u;
 }
+
+// The four slot box tests of 4-wide node `node` (lbvh.cu k_pack_quads); a slot
+// that is culled, empty or malformed gets t = +inf.
+struct BvhSlots {
+    float t0, t1, t2, t3;
+    uint32_t r0, r1, r2, r3;
+    uint32_t c0, c1, c2, c3;
+};
+
+__device__ __forceinline__ BvhSlots bvh_visit(const BvhView& b, uint32_t node, float3 no, float3 inv_d, float limit)
+{
+    const float4* p = b.quad + 8 * (size_t)node;
+    const float4 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3);
+    const float4 q4 = __ldg(p + 4), q5 = __ldg(p + 5), q6 = __ldg(p + 6), q7 = __ldg(p + 7);
+    BvhSlots s;
+    bvh_boxes_enter(q0, q1, q2, no, inv_d, limit, s.t0, s.t1);
+    bvh_boxes_enter(q4, q5, q6, no, inv_d, limit, s.t2, s.t3);
+    s.r0 = __float_as_uint(q3.x); s.r1 = __float_as_uint(q3.y);
+    s.c0 = __float_as_uint(q3.z); s.c1 = __float_as_uint(q3.w);
+    s.r2 = __float_as_uint(q7.x); s.r3 = __float_as_uint(q7.y);
+    s.c2 = __float_as_uint(q7.z); s.c3 = __float_as_uint(q7.w);
+    const float inf = __int_as_float(0x7f800000);
+    if (!bvh_slot_ok(b, s.r0, s.c0)) s.t0 = inf;
+    if (!bvh_slot_ok(b, s.r1, s.c1)) s.t1 = inf;
+    if (!bvh_slot_ok(b, s.r2, s.c2)) s.t2 = inf;
+    if (!bvh_slot_ok(b, s.r3, s.c3)) s.t3 = inf;
+    return s;
+}
+
+__device__ __forceinline__ void bvh_order(float& ta, uint32_t& ra, uint32_t& ca, float& tb, uint32_t& rb,
+                                          uint32_t& cb)
+{
+    if (tb < ta) {
+        const float t = ta; ta = tb; tb = t;
+        const uint32_t r = ra; ra = rb; rb = r;
+        const uint32_t c = ca; ca = cb; cb = c;
+    }
+}
+
+// Stack depth.  Each step pops one node and pushes at most four, all one
+// 4-wide level down, so the stack holds at most three entries per level plus
+// one.  A Karras tree over 30-bit codes made distinct by the sorted position
+// is at most 30 + ceil(log2 n) binary levels deep, 62 for n = 2^32, so at most
+// 31 4-wide levels: 94 entries.
+constexpr int kBvhStack = 96;
 
 __device__ __forceinline__ int32_t bvh_nearest(const SceneView& sc, float3 o, float3 d, float& tmin)
 {
@@ -130,46 +187,38 @@ __device__ __forceinline__ int32_t bvh_nearest(const SceneView& sc, float3 o, fl
         return best;
     }
     const float3 inv_d = safe_inv(d);
+    const float3 no = mk3(-o.x, -o.y, -o.z);
     const float inf = __int_as_float(0x7f800000);
     uint32_t stack[kBvhStack];
     int sp = 0;
     stack[sp++] = b.root;
-    // every internal node is pushed at most once; the cap only guards against
-    // a malformed tree
+    // every internal node is visited at most once; the cap only guards
+    // against a malformed tree
     uint32_t budget = 2u * b.n_leaves + 8u;
     while (sp > 0 && budget-- > 0u) {
         const uint32_t node = stack[--sp];
         if (node >= b.n_leaves - 1u) continue;
-        const float4* p = b.pair + 4 * (size_t)node;
-        const float4 c0 = __ldg(p), h0 = __ldg(p + 1), c1 = __ldg(p + 2), h1 = __ldg(p + 3);
-        const float t0 = bvh_box_enter(c0, h0, o, inv_d, tm);
-        const float t1 = bvh_box_enter(c1, h1, o, inv_d, tm);
-        uint32_t f0 = 0, n0 = 0, f1 = 0, n1 = 0;
-        int k0 = t0 < inf ? bvh_child(b, __float_as_uint(c0.w), __float_as_uint(h0.w), f0, n0) : 0;
-        int k1 = t1 < inf ? bvh_child(b, __float_as_uint(c1.w), __float_as_uint(h1.w), f1, n1) : 0;
-        // leaf clusters at once, nearer first; internal children onto the stack
-        if (k0 == 1 && k1 == 1 && t1 < t0) {
-            leaf_nearest(b, f1, n1, o, d, a, tm, best);
-            leaf_nearest(b, f0, n0, o, d, a, tm, best);
-            k0 = k1 = 0;
-        }
-        if (k0 == 1) {
-            leaf_nearest(b, f0, n0, o, d, a, tm, best);
-            k0 = 0;
-        }
-        if (k1 == 1) {
-            leaf_nearest(b, f1, n1, o, d, a, tm, best);
-            k1 = 0;
-        }
-        const uint32_t r0 = __float_as_uint(c0.w), r1 = __float_as_uint(c1.w);
-        if (k0 == 2 && k1 == 2) {
-            // push the farther child first so the nearer one is popped next
-            if (sp + 2 > kBvhStack) break;
-            if (t0 <= t1) { stack[sp++] = r1; stack[sp++] = r0; }
-            else          { stack[sp++] = r0; stack[sp++] = r1; }
-        } else if (k0 == 2 || k1 == 2) {
-            if (sp + 1 > kBvhStack) break;
-            stack[sp++] = k0 == 2 ? r0 : r1;
+        BvhSlots s = bvh_visit(b, node, no, inv_d, tm);
+        // slots in order of entry distance (a sorting network), culled ones last
+        bvh_order(s.t0, s.r0, s.c0, s.t1, s.r1, s.c1);
+        bvh_order(s.t2, s.r2, s.c2, s.t3, s.r3, s.c3);
+        bvh_order(s.t0, s.r0, s.c0, s.t2, s.r2, s.c2);
+        bvh_order(s.t1, s.r1, s.c1, s.t3, s.r3, s.c3);
+        bvh_order(s.t1, s.r1, s.c1, s.t2, s.r2, s.c2);
+        // internal slots onto the stack, farthest first, so the nearest is popped next
+        if (sp + 4 > kBvhStack) break;
+        if (s.t3 < inf && s.c3 == 0u) stack[sp++] = s.r3;
+        if (s.t2 < inf && s.c2 == 0u) stack[sp++] = s.r2;
+        if (s.t1 < inf && s.c1 == 0u) stack[sp++] = s.r1;
+        if (s.t0 < inf && s.c0 == 0u) stack[sp++] = s.r0;
+        // leaf clusters, nearest first (one copy of the leaf test, slots shifted through it)
+#pragma unroll 1
+        for (int j = 0; j < 4 && s.t0 < inf; ++j) {
+            if (s.c0) leaf_nearest(b, s.r0, min(s.c0, b.n_leaves - s.r0), o, d, a, tm, best);
+            s.t0 = s.t1; s.r0 = s.r1; s.c0 = s.c1;
+            s.t1 = s.t2; s.r1 = s.r2; s.c1 = s.c2;
+            s.t2 = s.t3; s.r2 = s.r3; s.c2 = s.c3;
+            s.t3 = inf;
         }
     }
     tmin = tm;
@@ -182,6 +231,7 @@ __device__ __forceinline__ bool bvh_occluded(const SceneView& sc, float3 o, floa
     const float a = dot3(d, d);
     if (b.n_leaves < 2 || b.n_leaves <= b.leaf_size) return leaf_occluded(b, 0u, min(b.n_leaves, 32u), o, d, a, dist2);
     const float3 inv_d = safe_inv(d);
+    const float3 no = mk3(-o.x, -o.y, -o.z);
     const float inf = __int_as_float(0x7f800000);
     // any accepted t has t*t < dist2, so t < sqrt(dist2) (1 + 2^-22)
     const float limit = sqrtf(dist2) * 1.0000003f;
@@ -192,18 +242,22 @@ __device__ __forceinline__ bool bvh_occluded(const SceneView& sc, float3 o, floa
     while (sp > 0 && budget-- > 0u) {
         const uint32_t node = stack[--sp];
         if (node >= b.n_leaves - 1u) continue;
-        const float4* p = b.pair + 4 * (size_t)node;
-        const float4 c0 = __ldg(p), h0 = __ldg(p + 1), c1 = __ldg(p + 2), h1 = __ldg(p + 3);
-        uint32_t f0 = 0, n0 = 0, f1 = 0, n1 = 0;
-        const int k0 = bvh_box_enter(c0, h0, o, inv_d, limit) < inf
-                           ? bvh_child(b, __float_as_uint(c0.w), __float_as_uint(h0.w), f0, n0) : 0;
-        const int k1 = bvh_box_enter(c1, h1, o, inv_d, limit) < inf
-                           ? bvh_child(b, __float_as_uint(c1.w), __float_as_uint(h1.w), f1, n1) : 0;
-        if (k0 == 1 && leaf_occluded(b, f0, n0, o, d, a, dist2)) return true;
-        if (k1 == 1 && leaf_occluded(b, f1, n1, o, d, a, dist2)) return true;
-        if (sp + 2 > kBvhStack) break;
-        if (k0 == 2) stack[sp++] = __float_as_uint(c0.w);
-        if (k1 == 2) stack[sp++] = __float_as_uint(c1.w);
+        BvhSlots s = bvh_visit(b, node, no, inv_d, limit);
+        if (sp + 4 > kBvhStack) break;
+        if (s.t0 < inf && s.c0 == 0u) stack[sp++] = s.r0;
+        if (s.t1 < inf && s.c1 == 0u) stack[sp++] = s.r1;
+        if (s.t2 < inf && s.c2 == 0u) stack[sp++] = s.r2;
+        if (s.t3 < inf && s.c3 == 0u) stack[sp++] = s.r3;
+        // leaf clusters in slot order (any hit ends the query)
+#pragma unroll 1
+        for (int j = 0; j < 4; ++j) {
+            if (s.t0 < inf && s.c0 && leaf_occluded(b, s.r0, min(s.c0, b.n_leaves - s.r0), o, d, a, dist2))
+                return true;
+            s.t0 = s.t1; s.r0 = s.r1; s.c0 = s.c1;
+            s.t1 = s.t2; s.r1 = s.r2; s.c1 = s.c2;
+            s.t2 = s.t3; s.r2 = s.r3; s.c2 = s.c3;
+            s.t3 = inf;
+        }
     }
     return false;
 }

@@ -12,8 +12,9 @@
 //      over (code, sorted position), which makes every key distinct
 //   5. bottom-up boxes: each leaf thread climbs, the second arrival at a node
 //      forms the union of its children's boxes
-//   6. child-pair nodes for traversal (both children's boxes in one line,
-//      subtrees of at most leaf_size spheres collapsed into leaf clusters)
+//   6. 4-wide nodes for traversal (the four grandchildren's boxes in two
+//      lines, subtrees of at most leaf_size spheres collapsed into leaf
+//      clusters)
 #include <cstdint>
 
 #include "lbvh.h"
@@ -253,39 +254,66 @@ __global__ void k_refit(int n, float4* node_ctr, float4* node_half, const uint32
     }
 }
 
-// Child-pair nodes for traversal: internal node i stores both children's boxes
-// in four float4 rows (one 64-byte line), so a traversal step is one load
-// level: [4i] = (centre of child 0, ref 0), [4i+1] = (half extent of child 0,
-// count 0), [4i+2], [4i+3] the same for child 1.  A child whose subtree holds
-// at most leaf_size spheres (a single sphere included) is a leaf cluster:
-// ref = its first sorted sphere, count = its sphere count; otherwise ref = its
-// internal node index and count = 0.
-__global__ void k_pack_pairs(int n, uint32_t leaf_size, const float4* node_ctr, const float4* node_half,
-                             const uint2* range, float4* pair)
+// A node's child as the traversal sees it.  A child whose subtree holds at
+// most leaf_size spheres (a single sphere included) is a leaf cluster:
+// ref = its first sorted sphere, cnt = its sphere count; otherwise ref = its
+// internal node index and cnt = 0.
+struct PackedChild {
+    float4 ctr, half;
+    uint32_t ref, cnt;
+};
+
+__device__ PackedChild pack_child(int n, uint32_t leaf_size, const float4* node_ctr, const float4* node_half,
+                                  const uint2* range, uint32_t c)
+{
+    PackedChild r;
+    if (c >= (uint32_t)(n - 1)) {
+        r.ref = c - (uint32_t)(n - 1);
+        r.cnt = 1u;
+    } else {
+        const uint2 rg = range[c];
+        const uint32_t size = rg.y - rg.x + 1u;
+        r.ref = size <= leaf_size ? rg.x : c;
+        r.cnt = size <= leaf_size ? size : 0u;
+    }
+    r.ctr = node_ctr[c];
+    r.half = node_half[c];
+    return r;
+}
+
+// 4-wide nodes for traversal: internal node i stores the boxes of its four
+// grandchildren (a child that is a leaf cluster stands in for its own two
+// slots, with an empty second slot: ref = ~0, cnt = 0), so one traversal step
+// descends two levels of the binary tree.  Eight float4 rows (two 64-byte
+// lines); rows 4j..4j+3 hold slots 2j and 2j+1 interleaved component by
+// component, so one packed f32x2 instruction does a step of two box tests:
+// (cx_a, cx_b, cy_a, cy_b), (cz_a, cz_b, hx_a, hx_b), (hy_a, hy_b, hz_a, hz_b),
+// (ref_a, ref_b, cnt_a, cnt_b), with c the box centre and h its half extent.
+// An internal slot's ref is a binary node index, whose own 4-wide node holds
+// its grandchildren; nodes at odd depths are built but never visited.
+__global__ void k_pack_quads(int n, uint32_t leaf_size, const float4* node_ctr, const float4* node_half,
+                             const uint2* range, float4* quad)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     const uint32_t child[2] = {__float_as_uint(node_ctr[i].w), __float_as_uint(node_half[i].w)};
     for (int k = 0; k < 2; ++k) {
-        const uint32_t c = child[k];
-        uint32_t ref, cnt;
-        if (c >= (uint32_t)(n - 1)) {
-            ref = c - (uint32_t)(n - 1);
-            cnt = 1u;
+        const PackedChild c = pack_child(n, leaf_size, node_ctr, node_half, range, child[k]);
+        PackedChild a = c, b;
+        if (c.cnt == 0u) {
+            a = pack_child(n, leaf_size, node_ctr, node_half, range, __float_as_uint(node_ctr[c.ref].w));
+            b = pack_child(n, leaf_size, node_ctr, node_half, range, __float_as_uint(node_half[c.ref].w));
         } else {
-            const uint2 r = range[c];
-            const uint32_t size = r.y - r.x + 1u;
-            if (size <= leaf_size) {
-                ref = r.x;
-                cnt = size;
-            } else {
-                ref = c;
-                cnt = 0u;
-            }
+            b.ctr = b.half = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            b.ref = 0xffffffffu;
+            b.cnt = 0u;
         }
-        const float4 ctr = node_ctr[c], half = node_half[c];
-        pair[4 * i + 2 * k] = make_float4(ctr.x, ctr.y, ctr.z, __uint_as_float(ref));
-        pair[4 * i + 2 * k + 1] = make_float4(half.x, half.y, half.z, __uint_as_float(cnt));
+        float4* row = quad + 8 * (size_t)i + 4 * k;
+        row[0] = make_float4(a.ctr.x, b.ctr.x, a.ctr.y, b.ctr.y);
+        row[1] = make_float4(a.ctr.z, b.ctr.z, a.half.x, b.half.x);
+        row[2] = make_float4(a.half.y, b.half.y, a.half.z, b.half.z);
+        row[3] = make_float4(__uint_as_float(a.ref), __uint_as_float(b.ref), __uint_as_float(a.cnt),
+                             __uint_as_float(b.cnt));
     }
 }
 
@@ -300,7 +328,7 @@ struct Parts {
     float4* node_ctr;
     float4* node_half;
     uint2* range;
-    float4* pair;
+    float4* quad;
     float4* leaf_sph;
     uint32_t* leaf_id;
     uint32_t *k0, *v0, *k1, *v1;
@@ -323,7 +351,7 @@ uint64_t carve(char* base, uint32_t n, Parts* q)
     q->node_ctr = static_cast<float4*>(take(2 * nn * sizeof(float4)));
     q->node_half = static_cast<float4*>(take(2 * nn * sizeof(float4)));
     q->range = static_cast<uint2*>(take(nn * sizeof(uint2)));
-    q->pair = static_cast<float4*>(take(4 * nn * sizeof(float4)));
+    q->quad = static_cast<float4*>(take(8 * nn * sizeof(float4)));
     q->leaf_sph = static_cast<float4*>(take(nn * sizeof(float4)));
     q->leaf_id = static_cast<uint32_t*>(take(nn * sizeof(uint32_t)));
     q->k0 = static_cast<uint32_t*>(take(nn * sizeof(uint32_t)));
@@ -390,14 +418,14 @@ cudaError_t lbvh_build(const float4* sph, const float* radius, uint32_t n, uint3
         k_tree<<<gi, kT, 0, stream>>>(k0, (int)n, node_ctr, node_half, range, parent);
         k_refit<<<g, kT, 0, stream>>>((int)n, node_ctr, node_half, parent, visits);
         const uint32_t ls = leaf_size ? (leaf_size < 32u ? leaf_size : 32u) : 1u;   // clusters fit a 32-bit mask
-        k_pack_pairs<<<gi, kT, 0, stream>>>((int)n, ls, node_ctr, node_half, range, q.pair);
+        k_pack_quads<<<gi, kT, 0, stream>>>((int)n, ls, node_ctr, node_half, range, q.quad);
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     out->node_ctr = node_ctr;
     out->node_half = node_half;
     out->node_range = range;
-    out->pair = q.pair;
+    out->quad = q.quad;
     out->leaf_sph = leaf_sph;
     out->leaf_id = leaf_id;
     out->n_leaves = n;

@@ -41,7 +41,7 @@ struct BvhView {
     const float4* node_ctr;       // [2n-1] box centre xyz, w = bit-cast left child (internal nodes)
     const float4* node_half;      // [2n-1] half extent xyz, w = bit-cast right child (internal nodes)
     const uint2* node_range;      // [n-1] first, last sorted sphere under an internal node
-    const float4* pair;           // [4(n-1)] child-pair nodes (lbvh.cu k_pack_pairs), used by the traversal
+    const float4* quad;           // [8(n-1)] 4-wide nodes (lbvh.cu k_pack_quads), used by the traversal
     const float4* leaf_sph;       // [n] spheres in Morton order (cx, cy, cz, r*r)
     const uint32_t* leaf_id;      // [n] original sphere index of each sorted slot
     uint32_t n_leaves;

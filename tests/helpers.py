@@ -59,7 +59,7 @@ def job_bytes_bound(sc):
     n, nl = len(sc.spheres), len(sc.lights)
     px = sc.width * sc.height
     tables = 24 * n + 48 * len(sc.materials) + 32 * nl + 8 * 256
-    bvh = 200 * n if n >= 1025 else 0
+    bvh = 264 * n if n >= 1025 else 0
     cells = 6 * 16 * 16 * 65          # per light / per sphere: a count and 32 indices per direction cell
     cones = 6 * 16 * 16 * 20 + 4096   # build scratch: the cells' bounding cones
     lb = cells * nl + cones if n < 1025 and 1 <= nl <= 64 else 0

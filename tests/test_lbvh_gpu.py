@@ -97,3 +97,35 @@ def test_small_scenes_bvh_edge_counts(po):
         rt, ri = po.trace(sph, o, d, po.EXACT)
         assert np.array_equal(ib, ri), n
         assert bit_mismatches(tb, rt) == 0
+
+
+@pytest.mark.parametrize("leaf", [1, 8])
+def test_lbvh_axis_aligned_rays(po, leaf):
+    """Rays with zero direction components (inverse direction +-inf, slab products +-inf or NaN):
+    along the axes through sphere centres and box-aligned offsets, and diagonals in the axis planes."""
+    sc = scenes.config2()
+    rng = np.random.default_rng(7 + leaf)
+    n = 1 << 16
+    axes = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], np.float32)
+    s = np.float32(np.sqrt(0.5))
+    diag = np.array([[s, s, 0], [s, 0, -s], [0, -s, s], [-s, -s, 0]], np.float32)
+    dirs = np.concatenate([axes, diag])
+    d = dirs[rng.integers(0, len(dirs), n)]
+    k = rng.integers(0, len(sc.spheres), n)
+    c = sc.spheres["center"][k].astype(np.float32)
+    r = sc.spheres["radius"][k].astype(np.float32)
+    # start 40 units behind the target point: a centre (every third ray), a point one radius off the
+    # centre across the ray (grazing), or a random point in the scene's extent
+    off = rng.integers(0, 3, n)
+    side = np.roll(d, 1, axis=1) * r[:, None]
+    tgt = np.where(off[:, None] == 0, c, np.where(off[:, None] == 1, c + side,
+                   rng.uniform(sc.spheres["center"].min(0), sc.spheres["center"].max(0), (n, 3))))
+    o = (tgt - 40.0 * d).astype(np.float32)
+    with Renderer(bvh_threshold=1, bvh_leaf_size=leaf) as rb:
+        rb.set_scene(sc.spheres, sc.materials, sc.lights)
+        tb, ib = rb.trace_nearest(o, d)
+    sel = rng.choice(n, 4000, replace=False)
+    rt, ri = po.trace(sc.spheres, o[sel], d[sel], po.EXACT)
+    assert (ib >= 0).mean() > 0.3
+    assert np.array_equal(ib[sel], ri)
+    assert bit_mismatches(tb[sel], rt) == 0
