@@ -352,6 +352,7 @@ atx_status Renderer::set_scene(const atx_sphere* s, uint32_t n, const atx_materi
     ATX_TRY(activate());
     ATX_CUDA(cudaStreamSynchronize(stream_));
     shape_valid_ = false;
+    masks_valid_ = false;
     return scene_.upload(s, n, m, nm, l, nl, &budget_, stream_);
 }
 
@@ -396,6 +397,30 @@ atx_status Renderer::refresh_dirs()
         dirs_valid_ = true;
     }
     camv_.dirs = dirs_.as<float4>();
+    return ATX_OK;
+}
+
+atx_status Renderer::refresh_masks()
+{
+    camv_.masks = nullptr;
+    camv_.mask_words = 0;
+    const SceneView& sc = scene_.view;
+    if (sc.use_bvh || sc.n_sph == 0 || sc.n_sph > kTileMaskMaxSpheres) return ATX_OK;
+    // the masks depend on the directions (matrices, viewport), the eye and the spheres
+    const bool same = masks_valid_ && masks_cam_.width == camv_.width && masks_cam_.height == camv_.height &&
+                      std::memcmp(masks_cam_.inv_proj, camv_.inv_proj, sizeof(camv_.inv_proj)) == 0 &&
+                      std::memcmp(masks_cam_.inv_view, camv_.inv_view, sizeof(camv_.inv_view)) == 0 &&
+                      std::memcmp(masks_cam_.pos, camv_.pos, sizeof(camv_.pos)) == 0;
+    const uint32_t words = tile_mask_words(sc.n_sph);
+    if (!same) {
+        const uint64_t tiles = ((uint64_t)camv_.width * camv_.height + 31u) / 32u;
+        ATX_TRY(masks_.ensure(tiles * words * sizeof(uint32_t), &budget_, "primary tile masks"));
+        ATX_CUDA(enqueue_tile_masks(sc, camv_, masks_.as<uint32_t>(), stream_));
+        masks_cam_ = camv_;
+        masks_valid_ = true;
+    }
+    camv_.masks = masks_.as<uint32_t>();
+    camv_.mask_words = words;
     return ATX_OK;
 }
 
@@ -453,6 +478,7 @@ atx_status Renderer::render(uint32_t spp)
         wave_[l].view.totals = totals_.as<unsigned long long>();
     }
     ATX_TRY(refresh_dirs());
+    ATX_TRY(refresh_masks());
 
     if (!settings_.accumulation) frame_ = 1;
     const uint32_t f0 = frame_;

@@ -108,7 +108,8 @@ public:
 private:
     atx_status activate() const;
     atx_status refresh_camera();
-    atx_status refresh_dirs();   // the primary-direction table for camv_
+    atx_status refresh_dirs();
+    atx_status refresh_masks();   // the primary-direction table for camv_
     atx_status ensure_shape();
 
     atx_config cfg_;
@@ -143,6 +144,12 @@ private:
     DeviceBuffer dirs_;
     CameraView dirs_cam_{};
     bool dirs_valid_ = false;
+    // Primary tile masks for the camera, eye and scene they were built for
+    // (masks_cam_; scenes on the brute-force tables up to 1,024 spheres):
+    // rebuilt when any of them changes.
+    DeviceBuffer masks_;
+    CameraView masks_cam_{};
+    bool masks_valid_ = false;
     LaunchShape shape_{};
     bool shape_valid_ = false;
 

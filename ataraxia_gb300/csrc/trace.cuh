@@ -296,6 +296,33 @@ __device__ __forceinline__ int32_t nearest_cone(const float4* __restrict__ sph, 
     return best;
 }
 
+// nearest_cone with the candidates read from a tile mask row (words words,
+// bit i % 32 of word i / 32 for sphere i) built with the same cone test for
+// a cone that contains every lane's direction: the same candidates or more,
+// each decided by the same exact test in the same index order.
+template <bool SMEM>
+__device__ __forceinline__ int32_t nearest_masked(const float4* __restrict__ sph, const uint32_t* __restrict__ row,
+                                                  uint32_t words, float3 o, float3 d, bool me, float& tmin)
+{
+    const float a = dot3(d, d);
+    int32_t best = -1;
+    float tm = kFltMax;
+    for (uint32_t w = 0; w < words; ++w) {
+        uint32_t mask = __ldg(&row[w]);
+        while (mask) {   // lowest index first: ties keep it, as in the brute-force loop
+            const uint32_t i = 32u * w + (uint32_t)(__ffs(mask) - 1);
+            mask &= mask - 1u;
+            float t;
+            if (me && sphere_t(table_sphere<SMEM>(sph, i), o, d, a, t) && t > 0.0f && t < tm) {
+                tm = t;
+                best = (int32_t)i;
+            }
+        }
+    }
+    tmin = tm;
+    return best;
+}
+
 // Any hit for the shadow rays (o, d, dist2) of the lanes with me set, whose
 // segments end near the light at apex; c is the cone of the directions from
 // the apex to the origins and dmax the largest apex-to-origin distance.  All

@@ -151,8 +151,13 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
             }
         } else {
             if (me) d = primary_ray(cam, p);
+            // a warp whose 32 pixels are one aligned tile takes the camera's tile mask
+            const uint32_t tile_px = job.pixel0 + base + (threadIdx.x & ~31u);   // warp-uniform
             WarpCone cone;
-            if (IS != kIsBvh && warp_cone(me, d, cone)) id = nearest_cone<SMEM>(sph, sc.n_sph, o, d, me, cone, t);
+            if (IS != kIsBvh && cam.masks && (tile_px & 31u) == 0u)
+                id = nearest_masked<SMEM>(sph, cam.masks + (size_t)(tile_px >> 5) * cam.mask_words, cam.mask_words,
+                                          o, d, me, t);
+            else if (IS != kIsBvh && warp_cone(me, d, cone)) id = nearest_cone<SMEM>(sph, sc.n_sph, o, d, me, cone, t);
             else if (me) id = scene_nearest<IS>(sc, sph, o, d, t);
             if (me) prim[j] = make_uint2(__float_as_uint(t), (uint32_t)id);
         }
@@ -931,6 +936,40 @@ __global__ void k_dir_table(CameraView cam, float4* out)
     }
 }
 
+// Tile masks (CameraView::masks): one warp per tile of 32 pixels builds the
+// cone of their primary directions as k_primary does (warp_cone over the same
+// directions, primary_ray) and sets bit i where cone_meets passes sphere i, or
+// every bit when the cone is too wide, which is what k_primary's per-warp
+// loop would test.  A k_primary warp whose pixels are this tile, or part of
+// it, has its directions inside this cone.
+__global__ void __launch_bounds__(kThreads) k_tile_masks(SceneView sc, CameraView cam, uint32_t* masks)
+{
+    const uint64_t px = (uint64_t)cam.width * cam.height;
+    const uint64_t tiles = (px + 31u) / 32u;
+    const uint32_t words = tile_mask_words(sc.n_sph);
+    const uint32_t lane = threadIdx.x & 31u;
+    const float3 o = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32u);
+    for (uint64_t t = (uint64_t)blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u; t < tiles; t += warps) {
+        const uint64_t p = 32u * t + lane;
+        const bool me = p < px;
+        float3 d = o;
+        if (me) d = primary_ray(cam, (uint32_t)p);
+        WarpCone cone;
+        const bool ok = warp_cone(me, d, cone);
+        for (uint32_t w = 0; w < words; ++w) {
+            const uint32_t i = 32u * w + lane;
+            bool pass = false;
+            if (i < sc.n_sph) {
+                const float4 s = __ldg(&sc.sph[i]);
+                pass = !ok || cone_meets(cone, mk3(s.x - o.x, s.y - o.y, s.z - o.z), cone_radius(s.w), 0.0f, 0.0f);
+            }
+            const uint32_t bits = __ballot_sync(kFull, pass);
+            if (lane == 0u) masks[t * words + w] = bits;
+        }
+    }
+}
+
 __global__ void k_primary_dirs(CameraView cam, float* out)
 {
     const uint64_t n = (uint64_t)cam.width * cam.height;
@@ -1127,6 +1166,15 @@ cudaError_t enqueue_dir_table(const CameraView& cam, float4* out, cudaStream_t s
     const uint64_t n = (uint64_t)cam.width * cam.height;
     if (n == 0) return cudaSuccess;
     k_dir_table<<<grid_for(n, kThreads, 4096), kThreads, 0, stream>>>(cam, out);
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_tile_masks(const SceneView& sc, const CameraView& cam, uint32_t* masks, cudaStream_t stream)
+{
+    const uint64_t px = (uint64_t)cam.width * cam.height;
+    if (px == 0 || sc.n_sph == 0 || sc.n_sph > kTileMaskMaxSpheres) return cudaErrorInvalidValue;
+    const uint64_t tiles = (px + 31u) / 32u;
+    k_tile_masks<<<grid_for(tiles * 32u, kThreads, 4096), kThreads, 0, stream>>>(sc, cam, masks);
     return cudaGetLastError();
 }
 

@@ -132,6 +132,12 @@ struct CameraView {
     // (xyz, w unused), as the reference keeps them between camera changes
     // (Camera.cpp:161-195); nullptr: computed where needed.
     const float4* dirs;
+    // Optional per-tile sphere masks for this camera, eye and scene
+    // (k_tile_masks): for tile t, the 32 pixels 32t..32t+31, bit i % 32 of
+    // word t * mask_words + i / 32 is set unless sphere i certainly misses
+    // every one of their primary rays.  nullptr: culled per warp when needed.
+    const uint32_t* masks;
+    uint32_t mask_words;
 };
 
 // Per-wave path state, structure of arrays of float4 rows.
@@ -261,5 +267,11 @@ cudaError_t enqueue_primary_dirs(const CameraView& cam, float* out, cudaStream_t
 
 // Fills the camera's per-pixel direction table (W*H float4, see CameraView::dirs).
 cudaError_t enqueue_dir_table(const CameraView& cam, float4* out, cudaStream_t stream);
+
+// Tile masks (see CameraView::masks) for scenes on the brute-force tables with
+// at most kTileMaskMaxSpheres spheres: ceil(W*H/32) * ceil(n/32) words.
+constexpr uint32_t kTileMaskMaxSpheres = 1024;
+__host__ __device__ inline uint32_t tile_mask_words(uint32_t n_sph) { return (n_sph + 31u) / 32u; }
+cudaError_t enqueue_tile_masks(const SceneView& sc, const CameraView& cam, uint32_t* masks, cudaStream_t stream);
 
 }  // namespace atx
