@@ -225,6 +225,46 @@ __device__ __forceinline__ int32_t bvh_nearest(const SceneView& sc, float3 o, fl
     return best;
 }
 
+// Nearest hit among a tile's candidate list (sorted sphere indices, built by
+// k_tile_lists for a cone that holds every lane's direction): the warp reads
+// 32 entries at a time, one per lane, and hands each sphere to every lane by
+// shuffle; the brute-force filter (leaf_candidates' arithmetic) and the exact
+// test decide, and ties go to the lowest original index as in leaf_nearest,
+// so the list's order does not matter.  All 32 lanes call it.
+__device__ __forceinline__ int32_t nearest_listed(const BvhView& b, const uint32_t* __restrict__ list, uint32_t len,
+                                                  float3 o, float3 d, bool me, float& tmin)
+{
+    const float a = dot3(d, d);
+    const uint32_t lane = threadIdx.x & 31u;
+    float tm = kFltMax;
+    int32_t best = -1;
+    for (uint32_t base = 0; base < len; base += 32u) {
+        const uint32_t k = base + lane;
+        const uint32_t s = k < len ? __ldg(&list[k]) : 0u;
+        const float4 v = __ldg(&b.leaf_sph[s]);
+        const uint32_t m = min(32u, len - base);
+        for (uint32_t j = 0; j < m; ++j) {
+            const float4 q = make_float4(__shfl_sync(0xffffffffu, v.x, j), __shfl_sync(0xffffffffu, v.y, j),
+                                         __shfl_sync(0xffffffffu, v.z, j), __shfl_sync(0xffffffffu, v.w, j));
+            const uint32_t sj = __shfl_sync(0xffffffffu, s, j);
+            const float ox = o.x - q.x, oy = o.y - q.y, oz = o.z - q.z;
+            const float bb = __fmaf_rn(oz, d.z, __fmaf_rn(oy, d.y, ox * d.x));
+            const float cc = __fmaf_rn(oz, oz, __fmaf_rn(oy, oy, __fmaf_rn(ox, ox, -q.w)));
+            const float h = __fmaf_rn(bb, -fabsf(bb), -(a * cc));
+            float t;
+            if (me && (__float_as_uint(h) >> 31) == 0u && sphere_t(q, o, d, a, t) && t > 0.0f) {
+                const int32_t id = (int32_t)__ldg(&b.leaf_id[sj]);
+                if (t < tm || (t == tm && best >= 0 && id < best)) {
+                    tm = t;
+                    best = id;
+                }
+            }
+        }
+    }
+    tmin = tm;
+    return best;
+}
+
 __device__ __forceinline__ bool bvh_occluded(const SceneView& sc, float3 o, float3 d, float dist2)
 {
     const BvhView& b = sc.bvh;

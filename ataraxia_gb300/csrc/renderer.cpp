@@ -404,16 +404,37 @@ atx_status Renderer::refresh_masks()
 {
     camv_.masks = nullptr;
     camv_.mask_words = 0;
+    camv_.tile_info = nullptr;
+    camv_.tile_lists = nullptr;
     const SceneView& sc = scene_.view;
-    if (sc.use_bvh || sc.n_sph == 0 || sc.n_sph > kTileMaskMaxSpheres) return ATX_OK;
-    // the masks depend on the directions (matrices, viewport), the eye and the spheres
+    // the masks and lists depend on the directions (matrices, viewport), the eye and the spheres
     const bool same = masks_valid_ && masks_cam_.width == camv_.width && masks_cam_.height == camv_.height &&
                       std::memcmp(masks_cam_.inv_proj, camv_.inv_proj, sizeof(camv_.inv_proj)) == 0 &&
                       std::memcmp(masks_cam_.inv_view, camv_.inv_view, sizeof(camv_.inv_view)) == 0 &&
                       std::memcmp(masks_cam_.pos, camv_.pos, sizeof(camv_.pos)) == 0;
+    const uint64_t tiles = ((uint64_t)camv_.width * camv_.height + 31u) / 32u;
+    if (sc.use_bvh) {
+        if (sc.bvh.n_leaves < 2 || sc.bvh.n_leaves <= sc.bvh.leaf_size) return ATX_OK;
+        if (!same) {
+            ATX_TRY(tile_info_.ensure((tiles + 1) * sizeof(uint2), &budget_, "primary tile list heads"));
+            uint2* info = tile_info_.as<uint2>();
+            uint32_t* total = reinterpret_cast<uint32_t*>(info + tiles);
+            ATX_CUDA(enqueue_tile_list_counts(sc, camv_, info, total, stream_));
+            uint32_t n = 0;
+            ATX_CUDA(cudaMemcpyAsync(&n, total, sizeof(n), cudaMemcpyDeviceToHost, stream_));
+            ATX_CUDA(cudaStreamSynchronize(stream_));
+            ATX_TRY(tile_lists_.ensure((uint64_t)(n ? n : 1u) * sizeof(uint32_t), &budget_, "primary tile lists"));
+            ATX_CUDA(enqueue_tile_list_fill(sc, camv_, info, tile_lists_.as<uint32_t>(), stream_));
+            masks_cam_ = camv_;
+            masks_valid_ = true;
+        }
+        camv_.tile_info = tile_info_.as<uint2>();
+        camv_.tile_lists = tile_lists_.as<uint32_t>();
+        return ATX_OK;
+    }
+    if (sc.n_sph == 0 || sc.n_sph > kTileMaskMaxSpheres) return ATX_OK;
     const uint32_t words = tile_mask_words(sc.n_sph);
     if (!same) {
-        const uint64_t tiles = ((uint64_t)camv_.width * camv_.height + 31u) / 32u;
         ATX_TRY(masks_.ensure(tiles * words * sizeof(uint32_t), &budget_, "primary tile masks"));
         ATX_CUDA(enqueue_tile_masks(sc, camv_, masks_.as<uint32_t>(), stream_));
         masks_cam_ = camv_;

@@ -150,6 +150,9 @@ private:
     DeviceBuffer masks_;
     CameraView masks_cam_{};
     bool masks_valid_ = false;
+    // The same for LBVH scenes: per-tile candidate lists (tile_info_: offset
+    // and length per tile, then the total; tile_lists_: sorted sphere indices).
+    DeviceBuffer tile_info_, tile_lists_;
     LaunchShape shape_{};
     bool shape_valid_ = false;
 

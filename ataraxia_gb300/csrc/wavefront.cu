@@ -151,10 +151,18 @@ __global__ void __launch_bounds__(kThreads) k_primary(SceneView sc, CameraView c
             }
         } else {
             if (me) d = primary_ray(cam, p);
-            // a warp whose 32 pixels are one aligned tile takes the camera's tile mask
-            const uint32_t tile_px = job.pixel0 + base + (threadIdx.x & ~31u);   // warp-uniform
+            // a warp whose pixels are one aligned tile (its first pixel inside
+            // the wave, so the tile is inside the image) takes the camera's
+            // tile mask or candidate list
+            const uint32_t warp_j = base + (threadIdx.x & ~31u);                  // warp-uniform
+            const uint32_t tile_px = job.pixel0 + warp_j;
+            const bool tiled = warp_j < n && (tile_px & 31u) == 0u;
             WarpCone cone;
-            if (IS != kIsBvh && cam.masks && (tile_px & 31u) == 0u)
+            uint2 ti = make_uint2(0u, kNoTileList);
+            if (IS == kIsBvh && cam.tile_info && tiled) ti = __ldg(&cam.tile_info[tile_px >> 5]);
+            if (IS == kIsBvh && ti.y != kNoTileList)
+                id = nearest_listed(sc.bvh, cam.tile_lists + ti.x, ti.y, o, d, me, t);
+            else if (IS != kIsBvh && cam.masks && tiled)
                 id = nearest_masked<SMEM>(sph, cam.masks + (size_t)(tile_px >> 5) * cam.mask_words, cam.mask_words,
                                           o, d, me, t);
             else if (IS != kIsBvh && warp_cone(me, d, cone)) id = nearest_cone<SMEM>(sph, sc.n_sph, o, d, me, cone, t);
@@ -970,6 +978,143 @@ __global__ void __launch_bounds__(kThreads) k_tile_masks(SceneView sc, CameraVie
     }
 }
 
+// Candidate spheres of one tile of an LBVH scene: a warp-cooperative walk of
+// the 4-wide nodes (lbvh.cu k_pack_quads) with the tile's cone.  A slot is
+// entered when the cone meets the ball around its box centre through the box
+// corners, that radius also added to the distance in the float-error margin:
+// this ball, inflated by cone_meets, contains the inflated test ball of every
+// sphere inside the box, so a slot holding a sphere that passes the sphere
+// test is entered.  A leaf cluster's spheres get the sphere test the
+// brute-force masks use, one per lane.  All lanes call it and keep the same
+// stack.  Returns the number of candidates (the first cap of them written to
+// out when FILL), or kNoTileList when the walk overflows its stack or step
+// budget or the list would pass kTileListMax.
+template <bool FILL>
+__device__ uint32_t tile_walk(const BvhView& b, const WarpCone& cone, float3 o, uint32_t* out, uint32_t cap)
+{
+    const uint32_t lane = lane_id();
+    uint32_t stack[kBvhStack];
+    int sp = 0;
+    stack[sp++] = b.root;
+    uint32_t count = 0u;
+    uint32_t budget = 2u * b.n_leaves + 8u;
+    while (sp > 0) {
+        if (budget-- == 0u) return kNoTileList;
+        const uint32_t node = stack[--sp];
+        if (node >= b.n_leaves - 1u) continue;
+        bool pass = false;
+        uint32_t ref = 0u, cnt = 0u;
+        if (lane < 4u) {   // lane k tests slot k
+            const float4* p = b.quad + 8 * (size_t)node + 4 * (lane >> 1);
+            const float4 r0 = __ldg(p), r1 = __ldg(p + 1), r2 = __ldg(p + 2), r3 = __ldg(p + 3);
+            const bool hi = (lane & 1u) != 0u;
+            ref = __float_as_uint(hi ? r3.y : r3.x);
+            cnt = __float_as_uint(hi ? r3.w : r3.z);
+            if (bvh_slot_ok(b, ref, cnt)) {
+                const float cx = hi ? r0.y : r0.x, cy = hi ? r0.w : r0.z, cz = hi ? r1.y : r1.x;
+                const float hx = hi ? r1.w : r1.z, hy = hi ? r2.y : r2.x, hz = hi ? r2.w : r2.z;
+                // rounded up past the float error of the sum of squares and the root
+                const float rb = sqrtf(hx * hx + hy * hy + hz * hz) * 1.000001f + 1e-6f;
+                pass = cone_meets(cone, mk3(cx - o.x, cy - o.y, cz - o.z), rb, rb, 0.0f);
+            }
+        }
+        uint32_t inner = __ballot_sync(kFull, pass && cnt == 0u);
+        uint32_t leaves = __ballot_sync(kFull, pass && cnt != 0u);
+        while (inner) {
+            const int k = __ffs(inner) - 1;
+            inner &= inner - 1u;
+            const uint32_t r = __shfl_sync(kFull, ref, k);
+            if (sp >= kBvhStack) return kNoTileList;
+            stack[sp++] = r;
+        }
+        while (leaves) {
+            const int k = __ffs(leaves) - 1;
+            leaves &= leaves - 1u;
+            const uint32_t first = __shfl_sync(kFull, ref, k);
+            const uint32_t c = min(__shfl_sync(kFull, cnt, k), b.n_leaves - first);
+            bool meets = false;
+            if (lane < c) {
+                const float4 sp4 = __ldg(&b.leaf_sph[first + lane]);
+                meets = cone_meets(cone, mk3(sp4.x - o.x, sp4.y - o.y, sp4.z - o.z), cone_radius(sp4.w), 0.0f, 0.0f);
+            }
+            const uint32_t bits = __ballot_sync(kFull, meets);
+            if (count + (uint32_t)__popc(bits) > kTileListMax) return kNoTileList;
+            const uint32_t at = count + (uint32_t)__popc(bits & ((1u << lane) - 1u));
+            if (FILL && meets && at < cap) out[at] = first + lane;
+            count += (uint32_t)__popc(bits);
+        }
+    }
+    return count;
+}
+
+// One warp per tile: the cone of the tile's primary directions (as k_primary
+// and k_tile_masks build it) and its candidate walk.  FILL: only tiles with a
+// list, written from lists + info[t].x.
+template <bool FILL>
+__global__ void __launch_bounds__(kThreads) k_tile_lists(SceneView sc, CameraView cam, uint2* info, uint32_t* lists)
+{
+    const uint64_t px = (uint64_t)cam.width * cam.height;
+    const uint64_t tiles = (px + 31u) / 32u;
+    const uint32_t lane = lane_id();
+    const float3 o = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32u);
+    for (uint64_t t = (uint64_t)blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u; t < tiles; t += warps) {
+        uint2 ti = make_uint2(0u, 0u);
+        if (FILL) {
+            ti = info[t];
+            if (ti.y == kNoTileList || ti.y == 0u) continue;   // warp-uniform
+        }
+        const uint64_t p = 32u * t + lane;
+        const bool me = p < px;
+        float3 d = o;
+        if (me) d = primary_ray(cam, (uint32_t)p);
+        WarpCone cone;
+        const bool ok = warp_cone(me, d, cone);
+        if (FILL) {
+            if (ok) tile_walk<true>(sc.bvh, cone, o, lists + ti.x, ti.y);
+        } else {
+            const uint32_t len = ok ? tile_walk<false>(sc.bvh, cone, o, nullptr, 0u) : kNoTileList;
+            if (lane == 0u) info[t] = make_uint2(0u, len);
+        }
+    }
+}
+
+// Offsets of the tile lists: one block, chunks of kThreads tiles in order;
+// tiles past 2^31 - 1 listed entries in all lose their list.
+__global__ void __launch_bounds__(kThreads) k_tile_list_scan(uint2* info, uint64_t tiles, uint32_t* total)
+{
+    __shared__ uint32_t warp_sums[kThreads / 32];
+    __shared__ uint64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const uint32_t lane = lane_id(), w = threadIdx.x / 32u;
+    for (uint64_t base = 0; base < tiles; base += kThreads) {
+        const uint64_t i = base + threadIdx.x;
+        uint2 ti = i < tiles ? info[i] : make_uint2(0u, 0u);
+        const uint32_t v = ti.y == kNoTileList ? 0u : ti.y;
+        uint32_t x = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, x, off);
+            if (lane >= (uint32_t)off) x += y;
+        }
+        if (lane == 31u) warp_sums[w] = x;
+        __syncthreads();
+        uint64_t pre = carry;
+        for (uint32_t k = 0; k < w; ++k) pre += warp_sums[k];
+        const uint64_t at = pre + x - v;
+        if (i < tiles) {
+            if (at + v > 0x7fffffffull) ti.y = kNoTileList;
+            ti.x = ti.y == kNoTileList ? 0u : (uint32_t)at;
+            info[i] = ti;
+        }
+        __syncthreads();
+        if (threadIdx.x == kThreads - 1) carry = pre + x;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = (uint32_t)(carry < 0x7fffffffull ? carry : 0x7fffffffull);
+}
+
 __global__ void k_primary_dirs(CameraView cam, float* out)
 {
     const uint64_t n = (uint64_t)cam.width * cam.height;
@@ -1175,6 +1320,28 @@ cudaError_t enqueue_tile_masks(const SceneView& sc, const CameraView& cam, uint3
     if (px == 0 || sc.n_sph == 0 || sc.n_sph > kTileMaskMaxSpheres) return cudaErrorInvalidValue;
     const uint64_t tiles = (px + 31u) / 32u;
     k_tile_masks<<<grid_for(tiles * 32u, kThreads, 4096), kThreads, 0, stream>>>(sc, cam, masks);
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_tile_list_counts(const SceneView& sc, const CameraView& cam, uint2* info, uint32_t* total,
+                                     cudaStream_t stream)
+{
+    const uint64_t px = (uint64_t)cam.width * cam.height;
+    if (px == 0 || !sc.use_bvh || sc.bvh.n_leaves < 2) return cudaErrorInvalidValue;
+    const uint64_t tiles = (px + 31u) / 32u;
+    k_tile_lists<false><<<grid_for(tiles * 32u, kThreads, 4096), kThreads, 0, stream>>>(sc, cam, info, nullptr);
+    k_tile_list_scan<<<1, kThreads, 0, stream>>>(info, tiles, total);
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_tile_list_fill(const SceneView& sc, const CameraView& cam, const uint2* info, uint32_t* lists,
+                                   cudaStream_t stream)
+{
+    const uint64_t px = (uint64_t)cam.width * cam.height;
+    if (px == 0 || !sc.use_bvh || sc.bvh.n_leaves < 2) return cudaErrorInvalidValue;
+    const uint64_t tiles = (px + 31u) / 32u;
+    k_tile_lists<true><<<grid_for(tiles * 32u, kThreads, 4096), kThreads, 0, stream>>>(
+        sc, cam, const_cast<uint2*>(info), lists);
     return cudaGetLastError();
 }
 

@@ -138,7 +138,16 @@ struct CameraView {
     // every one of their primary rays.  nullptr: culled per warp when needed.
     const uint32_t* masks;
     uint32_t mask_words;
+    // Optional per-tile candidate lists for LBVH scenes (k_tile_lists), for
+    // the same tiles: lists[info[t].x ...] holds info[t].y sorted sphere
+    // indices (BvhView::leaf_sph) that may be hit by the tile's primary rays;
+    // info[t].y = kNoTileList: none (the rays walk the LBVH).
+    const uint2* tile_info;
+    const uint32_t* tile_lists;
 };
+
+constexpr uint32_t kNoTileList = 0xffffffffu;
+constexpr uint32_t kTileListMax = 1024;   // longer lists are not kept (the rays walk the LBVH)
 
 // Per-wave path state, structure of arrays of float4 rows.
 //   ray_o  (ox, oy, oz, seed bits)     ray_d (dx, dy, dz, -)
@@ -273,5 +282,14 @@ cudaError_t enqueue_dir_table(const CameraView& cam, float4* out, cudaStream_t s
 constexpr uint32_t kTileMaskMaxSpheres = 1024;
 __host__ __device__ inline uint32_t tile_mask_words(uint32_t n_sph) { return (n_sph + 31u) / 32u; }
 cudaError_t enqueue_tile_masks(const SceneView& sc, const CameraView& cam, uint32_t* masks, cudaStream_t stream);
+
+// Tile candidate lists (see CameraView::tile_info) for an LBVH scene, in two
+// steps: enqueue_tile_list_counts writes info[t].y (a length or kNoTileList),
+// info[t].x (the exclusive sum of the lengths) and *total; after reading
+// *total the caller provides lists of that many words to enqueue_tile_list_fill.
+cudaError_t enqueue_tile_list_counts(const SceneView& sc, const CameraView& cam, uint2* info, uint32_t* total,
+                                     cudaStream_t stream);
+cudaError_t enqueue_tile_list_fill(const SceneView& sc, const CameraView& cam, const uint2* info, uint32_t* lists,
+                                   cudaStream_t stream);
 
 }  // namespace atx

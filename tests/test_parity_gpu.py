@@ -324,16 +324,18 @@ def test_converged_image_within_3_sigma_of_float64(po):
     assert ok.mean() >= 0.995
 
 
-def test_primary_tile_masks_follow_scene_and_eye(po):
-    """The per-camera primary tile masks are rebuilt when the spheres or the eye change: renders after
-    a scene change under the same camera and after an eye move are bit-exact against fresh oracle
-    renders (stale masks would miss the moved spheres)."""
+@pytest.mark.parametrize("bvh_threshold", [0, 1])
+def test_primary_tile_masks_follow_scene_and_eye(po, bvh_threshold):
+    """The per-camera primary tile masks (brute-force tables) and tile candidate lists (LBVH, forced
+    with bvh_threshold=1) are rebuilt when the spheres or the eye change: renders after a scene change
+    under the same camera and after an eye move are bit-exact against fresh oracle renders (stale
+    masks or lists would miss the moved spheres)."""
     base = scenes.config1().with_resolution(96, 54)
     moved = scenes.SyntheticScene(**{**base.__dict__, "spheres": base.spheres.copy()})
     moved.spheres["center"] += np.array([3.0, -1.5, 2.0], dtype=np.float32)
     eye = scenes.SyntheticScene(**{**moved.__dict__, "camera_position": tuple(
         float(v) + dv for v, dv in zip(moved.camera_position, (4.0, 2.0, -3.0)))})
-    with Renderer() as r:
+    with Renderer(bvh_threshold=bvh_threshold) as r:
         r.on_resize(base.width, base.height)
         r.set_settings(Settings(accumulation=True, skyLight=False, maxBounces=base.max_bounces))
         for sc in (base, moved, eye):
@@ -345,3 +347,4 @@ def test_primary_tile_masks_follow_scene_and_eye(po):
             acc = r.get_accumulation().reshape(-1, 4).copy()
             ref, _, _ = oracle_render(sc, 3)
             assert bit_mismatches(acc, ref) == 0
+            assert r.stats()["bvh_in_use"] == (1 if bvh_threshold == 1 else 0)
