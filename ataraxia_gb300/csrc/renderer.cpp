@@ -353,6 +353,7 @@ atx_status Renderer::set_scene(const atx_sphere* s, uint32_t n, const atx_materi
     ATX_CUDA(cudaStreamSynchronize(stream_));
     shape_valid_ = false;
     masks_valid_ = false;
+    prev_cam_valid_ = false;
     return scene_.upload(s, n, m, nm, l, nl, &budget_, stream_);
 }
 
@@ -408,10 +409,18 @@ atx_status Renderer::refresh_masks()
     camv_.tile_lists = nullptr;
     const SceneView& sc = scene_.view;
     // the masks and lists depend on the directions (matrices, viewport), the eye and the spheres
-    const bool same = masks_valid_ && masks_cam_.width == camv_.width && masks_cam_.height == camv_.height &&
-                      std::memcmp(masks_cam_.inv_proj, camv_.inv_proj, sizeof(camv_.inv_proj)) == 0 &&
-                      std::memcmp(masks_cam_.inv_view, camv_.inv_view, sizeof(camv_.inv_view)) == 0 &&
-                      std::memcmp(masks_cam_.pos, camv_.pos, sizeof(camv_.pos)) == 0;
+    auto same_view = [](const CameraView& a, const CameraView& b) {
+        return a.width == b.width && a.height == b.height &&
+               std::memcmp(a.inv_proj, b.inv_proj, sizeof(a.inv_proj)) == 0 &&
+               std::memcmp(a.inv_view, b.inv_view, sizeof(a.inv_view)) == 0 &&
+               std::memcmp(a.pos, b.pos, sizeof(a.pos)) == 0;
+    };
+    const bool same = masks_valid_ && same_view(masks_cam_, camv_);
+    // built for a camera that stayed put since the previous render only
+    const bool still = prev_cam_valid_ && same_view(prev_cam_, camv_);
+    prev_cam_ = camv_;
+    prev_cam_valid_ = true;
+    if (!same && !still) return ATX_OK;
     const uint64_t tiles = ((uint64_t)camv_.width * camv_.height + 31u) / 32u;
     if (sc.use_bvh) {
         if (sc.bvh.n_leaves < 2 || sc.bvh.n_leaves <= sc.bvh.leaf_size) return ATX_OK;

@@ -153,6 +153,11 @@ private:
     // The same for LBVH scenes: per-tile candidate lists (tile_info_: offset
     // and length per tile, then the total; tile_lists_: sorted sphere indices).
     DeviceBuffer tile_info_, tile_lists_;
+    // The camera of the previous render (prev_cam_valid_: since the last
+    // scene change): masks and lists are built only for a camera that stayed
+    // put since then, so a camera that moves every frame never pays the build.
+    CameraView prev_cam_{};
+    bool prev_cam_valid_ = false;
     LaunchShape shape_{};
     bool shape_valid_ = false;
 

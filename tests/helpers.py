@@ -21,7 +21,13 @@ def gpu_render(sc, spp, *, frames_before=0, renderer=None, sky=False, max_bounce
         r.set_settings(Settings(accumulation=True, skyLight=sky, maxBounces=mb))
         if frames_before:
             r.render_frames(frames_before)
-        r.render_frames(spp)
+        if spp > 1 and not frames_before:
+            # the first render under a new camera goes without the per-camera primary tile masks or
+            # lists (built once the camera stays put), the next one with them: both paths checked
+            r.render_frames(1)
+            r.render_frames(spp - 1)
+        else:
+            r.render_frames(spp)
         acc = r.get_accumulation().reshape(-1, 4).copy()
         img = r.get_image().reshape(-1).copy()
         return acc, img

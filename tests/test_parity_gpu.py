@@ -343,7 +343,8 @@ def test_primary_tile_masks_follow_scene_and_eye(po, bvh_threshold):
             r.set_scene(sc.spheres, sc.materials, sc.lights)
             r.set_camera_matrices(np.array(view.inv_view), np.array(view.inv_proj), sc.camera_position)
             r.reset_frame_index()
-            r.render_frames(3)
+            r.render_frames(1)   # camera or scene just changed: no masks or lists yet
+            r.render_frames(2)   # the camera stayed put: built for it
             acc = r.get_accumulation().reshape(-1, 4).copy()
             ref, _, _ = oracle_render(sc, 3)
             assert bit_mismatches(acc, ref) == 0
