@@ -283,15 +283,22 @@ __device__ __forceinline__ bool bvh_occluded(const SceneView& sc, float3 o, floa
         const uint32_t node = stack[--sp];
         if (node >= b.n_leaves - 1u) continue;
         BvhSlots s = bvh_visit(b, node, no, inv_d, limit);
+        // nearest slots first: a shadow ray leaves a surface, and its likeliest
+        // occluders lie near its origin (any hit ends the query, so the order
+        // changes only how soon)
+        bvh_order(s.t0, s.r0, s.c0, s.t1, s.r1, s.c1);
+        bvh_order(s.t2, s.r2, s.c2, s.t3, s.r3, s.c3);
+        bvh_order(s.t0, s.r0, s.c0, s.t2, s.r2, s.c2);
+        bvh_order(s.t1, s.r1, s.c1, s.t3, s.r3, s.c3);
+        bvh_order(s.t1, s.r1, s.c1, s.t2, s.r2, s.c2);
         if (sp + 4 > kBvhStack) break;
-        if (s.t0 < inf && s.c0 == 0u) stack[sp++] = s.r0;
-        if (s.t1 < inf && s.c1 == 0u) stack[sp++] = s.r1;
-        if (s.t2 < inf && s.c2 == 0u) stack[sp++] = s.r2;
         if (s.t3 < inf && s.c3 == 0u) stack[sp++] = s.r3;
-        // leaf clusters in slot order (any hit ends the query)
+        if (s.t2 < inf && s.c2 == 0u) stack[sp++] = s.r2;
+        if (s.t1 < inf && s.c1 == 0u) stack[sp++] = s.r1;
+        if (s.t0 < inf && s.c0 == 0u) stack[sp++] = s.r0;
 #pragma unroll 1
-        for (int j = 0; j < 4; ++j) {
-            if (s.t0 < inf && s.c0 && leaf_occluded(b, s.r0, min(s.c0, b.n_leaves - s.r0), o, d, a, dist2))
+        for (int j = 0; j < 4 && s.t0 < inf; ++j) {
+            if (s.c0 && leaf_occluded(b, s.r0, min(s.c0, b.n_leaves - s.r0), o, d, a, dist2))
                 return true;
             s.t0 = s.t1; s.r0 = s.r1; s.c0 = s.c1;
             s.t1 = s.t2; s.r1 = s.r2; s.c1 = s.c2;
