@@ -29,8 +29,13 @@ constexpr float kBvhK = 1.2207031e-3f;
 // hold the two boxes interleaved) against the boxes inflated by M.
 // Each packed f32x2 instruction rounds its two halves as the scalar
 // instruction would, so the results are those of one scalar test per child.
-// Sets t0/t1 to the entry distance (may be negative when the origin is
-// inside) or +inf when culled.  no = -o; x - y is computed as x + (-y), or as
+// Sets t0/t1 to +inf when the slot is culled, else to its cull key
+// w = ((tn - sl) - m) rounded down, tn the entry distance (may be negative
+// when the origin is inside): w > limit' implies tn - sl > limit' + m, the
+// test's own cull condition, for any later (smaller) limit', so a slot can be
+// dropped by comparing its key with the nearest hit found since.  A slab the
+// ray never enters (tn = +inf, where sl = +inf and tn - sl is NaN) is culled,
+// so a key is finite or -inf.  no = -o; x - y is computed as x + (-y), or as
 // fma(y, -1, x): both round the exact difference once.
 __device__ __forceinline__ void bvh_boxes_enter(float4 r0, float4 r1, float4 r2, float3 no, float3 inv_d,
                                                 float limit, float& t0, float& t1)
@@ -62,8 +67,11 @@ __device__ __forceinline__ void bvh_boxes_enter(float4 r0, float4 r1, float4 r2,
                    __fadd2_rn(make_float2(fabsf(tn.x), fabsf(tn.y)), make_float2(fabsf(tf.x), fabsf(tf.y)))),
         m);
     const float inf = __int_as_float(0x7f800000);
-    t0 = (tf.x + sl.x < 0.0f || tn.x - sl.x > tf.x + sl.x || tn.x - sl.x > limit + m.x) ? inf : tn.x;
-    t1 = (tf.y + sl.y < 0.0f || tn.y - sl.y > tf.y + sl.y || tn.y - sl.y > limit + m.y) ? inf : tn.y;
+    const float e0 = tn.x - sl.x, e1 = tn.y - sl.y;
+    const bool cull0 = !(tn.x < inf) || tf.x + sl.x < 0.0f || e0 > tf.x + sl.x || e0 > limit + m.x;
+    const bool cull1 = !(tn.y < inf) || tf.y + sl.y < 0.0f || e1 > tf.y + sl.y || e1 > limit + m.y;
+    t0 = cull0 ? inf : __fsub_rd(e0, m.x);
+    t1 = cull1 ? inf : __fsub_rd(e1, m.y);
 }
 
 __device__ __forceinline__ float3 safe_inv(float3 d)
@@ -199,7 +207,7 @@ __device__ __forceinline__ int32_t bvh_nearest(const SceneView& sc, float3 o, fl
         const uint32_t node = stack[--sp];
         if (node >= b.n_leaves - 1u) continue;
         BvhSlots s = bvh_visit(b, node, no, inv_d, tm);
-        // slots in order of entry distance (a sorting network), culled ones last
+        // slots in order of cull key (a sorting network), culled ones last
         bvh_order(s.t0, s.r0, s.c0, s.t1, s.r1, s.c1);
         bvh_order(s.t2, s.r2, s.c2, s.t3, s.r3, s.c3);
         bvh_order(s.t0, s.r0, s.c0, s.t2, s.r2, s.c2);
@@ -211,9 +219,11 @@ __device__ __forceinline__ int32_t bvh_nearest(const SceneView& sc, float3 o, fl
         if (s.t2 < inf && s.c2 == 0u) stack[sp++] = s.r2;
         if (s.t1 < inf && s.c1 == 0u) stack[sp++] = s.r1;
         if (s.t0 < inf && s.c0 == 0u) stack[sp++] = s.r0;
-        // leaf clusters, nearest first (one copy of the leaf test, slots shifted through it)
+        // leaf clusters, nearest first, until a hit found in an earlier one is
+        // nearer than the next one's key (one copy of the leaf test, slots
+        // shifted through it)
 #pragma unroll 1
-        for (int j = 0; j < 4 && s.t0 < inf; ++j) {
+        for (int j = 0; j < 4 && s.t0 <= tm; ++j) {
             if (s.c0) leaf_nearest(b, s.r0, min(s.c0, b.n_leaves - s.r0), o, d, a, tm, best);
             s.t0 = s.t1; s.r0 = s.r1; s.c0 = s.c1;
             s.t1 = s.t2; s.r1 = s.r2; s.c1 = s.c2;
