@@ -17,7 +17,18 @@ enum : int { kIsGlobal = 0, kIsSmem = 1, kIsBvh = 2 };
 
 // Camera.cpp:173-187 for pixel (x, y): NDC without a pixel-centre offset, y = 0
 // the bottom row; target = invProj * (cx, cy, 1, 1); direction =
-// normalize(invView * (normalize(target.xyz / target.w), 0)).
+// normalize(invView * (normalize(target.xyz / target.w), 0)).  The reference
+// computes these on the host in IEEE single precision without contraction
+// (Camera::UpdateRayDirection), so this evaluates the same expressions in the
+// same order with nothing fused: matrix-vector products as pairwise column
+// sums, and the two normalisations with dot products (x*x + y*y) + z*z.  The
+// directions are then the reference's host-computed ones bit for bit.
+__device__ __forceinline__ float3 normalize3_host(float3 v)
+{
+    const float d = (v.x * v.x + v.y * v.y) + v.z * v.z;
+    return muls3(v, 1.0f / sqrtf(d));
+}
+
 __device__ __forceinline__ float3 primary_dir(const CameraView& cam, uint32_t x, uint32_t y)
 {
     const float qx = __uint2float_rn(x) / __uint2float_rn(cam.width);
@@ -28,12 +39,13 @@ __device__ __forceinline__ float3 primary_dir(const CameraView& cam, uint32_t x,
 #pragma unroll
     for (int r = 0; r < 4; ++r)
         t[r] = (cam.inv_proj[r] * cx + cam.inv_proj[4 + r] * cy) + (cam.inv_proj[8 + r] + cam.inv_proj[12 + r]);
-    const float3 tv = normalize3(mk3(t[0] / t[3], t[1] / t[3], t[2] / t[3]));
+    const float3 tv = normalize3_host(mk3(t[0] / t[3], t[1] / t[3], t[2] / t[3]));
     float dv[3];
 #pragma unroll
     for (int r = 0; r < 3; ++r)
-        dv[r] = (cam.inv_view[r] * tv.x + cam.inv_view[4 + r] * tv.y) + cam.inv_view[8 + r] * tv.z;
-    return normalize3(mk3(dv[0], dv[1], dv[2]));
+        dv[r] = (cam.inv_view[r] * tv.x + cam.inv_view[4 + r] * tv.y) +
+                (cam.inv_view[8 + r] * tv.z + cam.inv_view[12 + r] * 0.0f);
+    return normalize3_host(mk3(dv[0], dv[1], dv[2]));
 }
 
 // The shared-memory sphere table in pair layout: spheres 2j and 2j+1 share

@@ -95,7 +95,17 @@ static inline REAL FN(pow5)(REAL x)
 
 /* ------------------------------------------------------------------ camera */
 
-/* Camera.cpp:161-195 for one pixel. */
+/* Camera.cpp:161-195 for one pixel.  The reference computes the directions on
+ * the host with IEEE single rounding and no contraction, so every mode
+ * evaluates its expressions in that order: pairwise column sums for the
+ * matrix-vector products and unfused dot products (x*x + y*y) + z*z in the two
+ * normalisations (the kernels do the same). */
+static inline V3 FN(normalize_host)(V3 v)
+{
+    REAL d = (v.x * v.x + v.y * v.y) + v.z * v.z;
+    return FN(muls)(v, (REAL)1 / SQRT(d));
+}
+
 static V3 FN(primary_dir)(const orc_view* v, uint32_t x, uint32_t y)
 {
     const float* P = v->inv_proj;
@@ -105,25 +115,15 @@ static V3 FN(primary_dir)(const orc_view* v, uint32_t x, uint32_t y)
     REAL cx = qx * (REAL)2 - (REAL)1;
     REAL cy = qy * (REAL)2 - (REAL)1;
     REAL t[4];
-    for (int r = 0; r < 4; ++r) {
-#if EXACT
-        t[r] = ((REAL)P[0 * 4 + r] * cx + (REAL)P[1 * 4 + r] * cy) + ((REAL)P[2 * 4 + r] + (REAL)P[3 * 4 + r]);
-#else
+    for (int r = 0; r < 4; ++r)
         t[r] = ((REAL)P[0 * 4 + r] * cx + (REAL)P[1 * 4 + r] * cy) +
                ((REAL)P[2 * 4 + r] * (REAL)1 + (REAL)P[3 * 4 + r] * (REAL)1);
-#endif
-    }
-    V3 tv = FN(normalize)(FN(mk)(t[0] / t[3], t[1] / t[3], t[2] / t[3]));
+    V3 tv = FN(normalize_host)(FN(mk)(t[0] / t[3], t[1] / t[3], t[2] / t[3]));
     REAL d[3];
-    for (int r = 0; r < 3; ++r) {
-#if EXACT
-        d[r] = ((REAL)Vw[0 * 4 + r] * tv.x + (REAL)Vw[1 * 4 + r] * tv.y) + (REAL)Vw[2 * 4 + r] * tv.z;
-#else
+    for (int r = 0; r < 3; ++r)
         d[r] = ((REAL)Vw[0 * 4 + r] * tv.x + (REAL)Vw[1 * 4 + r] * tv.y) +
                ((REAL)Vw[2 * 4 + r] * tv.z + (REAL)Vw[3 * 4 + r] * (REAL)0);
-#endif
-    }
-    return FN(normalize)(FN(mk)(d[0], d[1], d[2]));
+    return FN(normalize_host)(FN(mk)(d[0], d[1], d[2]));
 }
 
 /* ---------------------------------------------------------- intersection */

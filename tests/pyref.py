@@ -51,6 +51,12 @@ def normalize(a):
     return muls(a, inv)
 
 
+def normalize_host(a):
+    """Camera.cpp's normalisation on the host: (x*x + y*y) + z*z, nothing fused."""
+    inv = ONE / np.sqrt((a[0] * a[0] + a[1] * a[1]) + a[2] * a[2])
+    return muls(a, inv)
+
+
 def cross(a, b):
     return (a[1] * b[2] - b[1] * a[2], a[2] * b[0] - b[2] * a[0], a[0] * b[1] - b[0] * a[1])
 
@@ -99,9 +105,10 @@ def primary_dir(ip, iv, W, H, x, y):
     cx = qx * F(2.0) - ONE
     cy = qy * F(2.0) - ONE
     t = [(ip[0 * 4 + r] * cx + ip[1 * 4 + r] * cy) + (ip[2 * 4 + r] + ip[3 * 4 + r]) for r in range(4)]
-    tv = normalize((t[0] / t[3], t[1] / t[3], t[2] / t[3]))
-    d = [(iv[0 * 4 + r] * tv[0] + iv[1 * 4 + r] * tv[1]) + iv[2 * 4 + r] * tv[2] for r in range(3)]
-    return normalize(tuple(d))
+    tv = normalize_host((t[0] / t[3], t[1] / t[3], t[2] / t[3]))
+    d = [(iv[0 * 4 + r] * tv[0] + iv[1 * 4 + r] * tv[1]) + (iv[2 * 4 + r] * tv[2] + iv[3 * 4 + r] * F(0.0))
+         for r in range(3)]
+    return normalize_host(tuple(d))
 
 
 def sphere_t(c, r2, o, d, a):
