@@ -329,9 +329,13 @@ class Renderer:
 
     Render = render
 
-    def get_image(self) -> np.ndarray:
-        """RGBA8 image as (H, W) uint32, A<<24 | B<<16 | G<<8 | R (Renderer.h:70-78)."""
-        out = np.empty(self.width * self.height, dtype=np.uint32)
+    def get_image(self, out: np.ndarray | None = None) -> np.ndarray:
+        """RGBA8 image as (H, W) uint32, A<<24 | B<<16 | G<<8 | R (Renderer.h:70-78); out, if given, is a
+        contiguous uint32 buffer of W*H pixels to read into."""
+        if out is None:
+            out = np.empty(self.width * self.height, dtype=np.uint32)
+        if out.dtype != np.uint32 or not out.flags.c_contiguous or out.size != self.width * self.height:
+            raise ValueError("get_image: out must be a contiguous uint32 array of width*height pixels")
         N.check(N.lib().atx_read_image(self._h, N.ptr(out), out.size))
         return out.reshape(self.height, self.width)
 

@@ -343,6 +343,8 @@ def run_ours(args, dist: Dist):
                    "paths_per_step": paths_step, "parallelism": f"replicas x{dist.world}",
                    "l2": "working set > L2: two lanes of 16.6 Mi-path wave state (2.3 GB each) per launch"},
         "mrays_per_s": round(mrays, 1),
+        "rays_per_path": round(rays / (args.steps * paths_step), 4),
+        "primary_hit_frac": round(shaded0 / (prof_steps * paths_step), 4),
         "gpu_launches": int(launches),
         "clocks": clk,
         "roofline": roofline,
@@ -350,69 +352,72 @@ def run_ours(args, dist: Dist):
     }
     if ref_kernel:
         out["ref_cuda_kernel"] = ref_kernel
-        out["vs_ref_cuda_kernel"] = round(value / ref_kernel["kernel_mpaths_s"], 2)
+        if "kernel_mpaths_s" in ref_kernel:
+            out["vs_ref_cuda_kernel"] = round(value / ref_kernel["kernel_mpaths_s"], 2)
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         v, sample, cores, mr = cpu_reference(sc, args.cpu_seconds)
         out["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port",
-                               "sample": sample, "mrays_per_s": round(mr, 3),
-                               "what": "reference per-pixel path restated in C (literal expression order), "
-                                       "OpenMP over rows"}
+                               "cpu": cpu_model(), "sample": sample, "mrays_per_s": round(mr, 3),
+                               "what": "reference per-pixel path restated in C (literal expression order, "
+                                       "within 1e-3 of the reference's own kernel built with IEEE arithmetic "
+                                       "on >= 99.99% of pixels), OpenMP over rows"}
+        out["cpu_baseline_small_scene"] = cpu_small_scene()
+    if dist.world == 1 and not args.no_extra:
+        out["large_scene"] = large_scene_leg(args, dev)
+        out["batch"] = batch_compare(args, dev, max(3, min(args.steps, 8)))
+        out["serve"] = serve_leg(args)
     return out
 
 
 def time_reference_kernel(sc, cam, dev, args) -> dict:
-    """The reference's kernelRender restated (baseline/refport), one sample per launch as the reference
-    renders: kernel-only device time over the same number of samples per pixel as one of our steps, and
-    the reference's whole per-frame Render() sequence (ray-direction upload, syncs, image copy) by wall
-    clock."""
-    import torch
-
+    """The reference's own kernelRender, compiled from its unmodified Renderer.cu and BRDF.cu with its own
+    flags (baseline/refbuild, -use_fast_math), launched as Renderer::Render launches it: one sample per
+    pixel per launch, (opt/32 x opt/32) blocks, the default stream.  Kernel-only device time (CUDA events)
+    over the same samples per pixel as a few of our steps, and the reference's whole per-frame Render()
+    sequence (scene upload at frame 1, ray-direction upload, syncs, image copy) by wall clock."""
     import ataraxia_gb300 as atx
-    from baseline import refport
+    from baseline import refbuild
 
+    if not refbuild.available("fast"):
+        return {"unavailable": "the reference's device image was not built (needs the reference tree)"}
     _, iv, _, ip = atx.camera_matrices(cam, sc.width, sc.height)
-    dirs = refport.ray_dirs(iv, ip, sc.width, sc.height)
-    port = refport.RefPort(sc.spheres, sc.materials, sc.lights, sc.width, sc.height, dirs, sc.camera_position,
-                           sc.max_bounces)
-    try:
-        for _ in range(3):
-            port.frame()
-        port.sync()
+    dirs = refbuild.ray_dirs(iv, ip, sc.width, sc.height)
+    name, block = refbuild.kernel_info("fast")
+    with refbuild.RefRenderer(sc.spheres, sc.materials, sc.lights, sc.width, sc.height, dirs, sc.camera_position,
+                              sc.camera_direction, sc.max_bounces) as ref:
+        ref.frames(3)
         frames = sc.spp * max(1, min(args.steps, 4))
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record()
-        for _ in range(frames):
-            port.frame()
-        e1.record()
-        e1.synchronize()
-        k_ms = e0.elapsed_time(e1)
+        k_ms = ref.time_frames(frames)
+        ref.set_frame(1)
+        ref.frame(full=True)                       # frame 1: scene upload, accumulator cleared
         t0 = time.perf_counter()
         for _ in range(sc.spp):
-            port.frame(full=True)
-        port.sync()
+            ref.frame(full=True)
         r_s = time.perf_counter() - t0
-        bx, by = port.block()
-    finally:
-        port.close()
     return {"kernel_mpaths_s": round(frames * sc.pixels / (k_ms * 1e-3) / 1e6, 2),
             "render_mpaths_s": round(sc.spp * sc.pixels / r_s / 1e6, 2),
-            "kernel_ms_per_frame": round(k_ms / frames, 3), "block": [bx, by],
-            "what": "reference kernelRender restated (baseline/refport/refport.cu), -use_fast_math, sm_103a, "
-                    "1 spp per launch; render_* includes the reference's per-frame ray-direction upload, syncs "
-                    "and image copy"}
+            "kernel_ms_per_frame": round(k_ms / frames, 3), "render_ms_per_frame": round(r_s * 1e3 / sc.spp, 3),
+            "block": [block, block], "kernel": name,
+            "what": "the reference's kernelRender compiled from its unmodified Renderer.cu + BRDF.cu "
+                    "(baseline/refbuild: own minimal glm, headless Image/Input stubs; -use_fast_math "
+                    "--expt-relaxed-constexpr -rdc=true for sm_103a), 1 spp per launch; render_* is the "
+                    "reference's per-frame Render() sequence: ray-direction cudaMalloc + upload + syncs, "
+                    "launch, image copy"}
 
 
-def run_batch_compare(args, dist: Dist):
-    """The batched mix (64 scenes, seed 3): the plain wavefront renderer launched once per scene (device
-    time of the render calls only) against one batched pass (all scenes, one CUDA graph) per step."""
+def batch_compare(args, dev: int, steps: int) -> dict:
+    """The batched mix (64 scenes, seed 3): the plain wavefront renderer launched once per scene against
+    one batched pass (all scenes, one CUDA graph) per step.  The plain arm is timed two ways: the device
+    time of its render calls alone (CUDA events around each launch, the scene already set), and as a
+    caller sees it (wall clock over the whole loop: per scene resize, scene upload with its acceleration
+    structures, camera, settings, the launch and the RGBA8 read-back).  gpu_idle_frac = the share of the
+    caller's loop in which no render kernel of the plain arm runs."""
+    import numpy as np
     import torch
 
     import ataraxia_gb300 as atx
     from ataraxia_gb300 import scenes
 
-    dev = dist.local_rank
     torch.cuda.set_device(dev)
     mix = scenes.config3(count=args.mix_scenes)
     if args.max_pass_spp:   # slices of at most this many frames per scene and pass, as a server makes
@@ -422,20 +427,29 @@ def run_batch_compare(args, dist: Dist):
     # plain: one renderer, one launch per scene
     r = atx.Renderer(device=dev, bvh_threshold=args.bvh_threshold, bvh_leaf_size=args.bvh_leaf)
     stream = torch.cuda.ExternalStream(r.stream, device=dev)
+    img = {sc.width * sc.height: np.empty(sc.width * sc.height, np.uint32) for sc in mix}
     plain_ms = 0.0
-    for rep in range(2):                       # rep 0 warms up (allocations, BVH builds)
+    caller_s = 0.0
+    for rep in range(3):                       # rep 0 warms up (allocations, BVH builds)
+        t0 = time.perf_counter()
         for sc in mix:
             r.on_resize(sc.width, sc.height)
             r.set_scene(sc.spheres, sc.materials, sc.lights)
             r.set_camera(atx.Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction))
             r.set_settings(atx.Settings(True, sc.sky_light, sc.max_bounces))
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            r.render_frames(sc.spp)
-            e1.record(stream)
-            e1.synchronize()
             if rep == 1:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                r.render_frames(sc.spp)
+                e1.record(stream)
+                e1.synchronize()
                 plain_ms += e0.elapsed_time(e1)
+            else:
+                r.render_frames(sc.spp)
+                r.get_image(out=img[sc.width * sc.height])
+        r.synchronize()
+        if rep == 2:
+            caller_s = time.perf_counter() - t0
     r.close()
 
     b = atx.Batch(device=dev, bvh_threshold=args.bvh_threshold, bvh_leaf_size=args.bvh_leaf)
@@ -452,38 +466,124 @@ def run_batch_compare(args, dist: Dist):
     s0 = b.stats()
     t0 = time.perf_counter()
     pass_ms = []
-    for _ in range(args.steps):
+    for _ in range(steps):
         b.run()
         b.synchronize()
         pass_ms.append(b.stats()["last_pass_ms"])
     wall = time.perf_counter() - t0
     s1 = b.stats()
     tun = b.tuning()
-    # the same passes with every scene's primary hits traced again each pass
-    b.set_tuning(primary_cache=False)
-    for _ in range(2):
-        b.run()
-    b.synchronize()
-    nc_ms = []
-    for _ in range(args.steps):
-        b.run()
-        b.synchronize()
-        nc_ms.append(b.stats()["last_pass_ms"])
     b.close()
     batched_ms = statistics.mean(pass_ms)
-    nocache_ms = statistics.mean(nc_ms)
-    return {"mode": "batch", "scenes": len(mix), "paths_per_pass": paths,
-            "plain_ms_per_pass": round(plain_ms, 3), "plain_mpaths_s": round(paths / (plain_ms * 1e-3) / 1e6, 1),
+    return {"scenes": len(mix), "paths_per_pass": paths,
+            "plain_device_ms": round(plain_ms, 3), "plain_mpaths_s": round(paths / (plain_ms * 1e-3) / 1e6, 1),
+            "plain_caller_ms": round(caller_s * 1e3, 3),
+            "plain_caller_mpaths_s": round(paths / caller_s / 1e6, 1),
+            "plain_gpu_idle_frac": round(max(0.0, 1.0 - plain_ms / (caller_s * 1e3)), 3),
             "batched_ms_per_pass": round(batched_ms, 3),
             "batched_mpaths_s": round(paths / (batched_ms * 1e-3) / 1e6, 1),
-            "batched_wall_mpaths_s": round(args.steps * paths / wall / 1e6, 1),
-            "speedup": round(plain_ms / batched_ms, 3),
-            "batched_retrace_primary_mpaths_s": round(paths / (nocache_ms * 1e-3) / 1e6, 1),
-            "speedup_retrace_primary": round(plain_ms / nocache_ms, 3),
+            "batched_wall_mpaths_s": round(steps * paths / wall / 1e6, 1),
+            "speedup_vs_plain_device": round(plain_ms / batched_ms, 3),
+            "speedup_vs_plain_caller": round(caller_s * 1e3 / (wall * 1e3 / steps), 3),
             "graph_launches": s1["graph_launches"] - s0["graph_launches"],
             "rays_per_path": round(((s1["extension_rays"] - s0["extension_rays"]) +
-                                    (s1["shadow_rays"] - s0["shadow_rays"])) / (args.steps * paths), 3),
+                                    (s1["shadow_rays"] - s0["shadow_rays"])) / (steps * paths), 3),
             "tuning": tun}
+
+
+def run_batch_compare(args, dist: Dist):
+    return {"mode": "batch", **batch_compare(args, dist.local_rank, args.steps)}
+
+
+def large_scene_leg(args, dev: int) -> dict:
+    """The large scene (seed 2): 65,536 clustered spheres through the LBVH, 3840x2160, 8 bounces, 4 spp
+    per launch; device time over launches with the scene resident."""
+    import torch
+
+    import ataraxia_gb300 as atx
+    from ataraxia_gb300 import scenes
+
+    sc = scenes.config2()
+    r = atx.Renderer(device=dev, bvh_leaf_size=args.bvh_leaf)
+    r.on_resize(sc.width, sc.height)
+    r.set_scene(sc.spheres, sc.materials, sc.lights)
+    r.set_camera(atx.Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction))
+    r.set_settings(atx.Settings(accumulation=True, skyLight=False, maxBounces=sc.max_bounces))
+    for _ in range(3):
+        r.render_frames(sc.spp)
+    r.synchronize()
+    stream = torch.cuda.ExternalStream(r.stream, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0 = r.stats()
+    steps = max(3, min(args.steps, 10))
+    e0.record(stream)
+    for _ in range(steps):
+        r.render_frames(sc.spp)
+    e1.record(stream)
+    e1.synchronize()
+    s1 = r.stats()
+    r.close()
+    ms = e0.elapsed_time(e1)
+    rays = (s1["extension_rays"] - s0["extension_rays"]) + (s1["shadow_rays"] - s0["shadow_rays"])
+    return {"workload": "large scene: 65,536 spheres in 32 clusters, 256 materials, 16 lights, 3840x2160, "
+                        "8 bounces, 4 spp per launch (LBVH)",
+            "mpaths_s": round(steps * sc.pixels * sc.spp / (ms * 1e-3) / 1e6, 1),
+            "mrays_s": round(rays / (ms * 1e-3) / 1e6, 1), "ms_per_launch": round(ms / steps, 3),
+            "launches": steps, "bvh_in_use": int(s1["bvh_in_use"])}
+
+
+def serve_leg(args) -> dict:
+    """A short serving run (seed 4) at one arrival rate: the continuous-batching server (arrival order)
+    against FIFO one-launch-per-job, p50/p99 time to target spp."""
+    from ataraxia_gb300 import scenes
+
+    pool = scenes.scene_pool(4, args.pool)
+    jobs = scenes.config4(seed=4, rate=args.line_serve_rate, duration_s=args.line_serve_seconds, pool=pool)
+    return {"rate_jobs_s": args.line_serve_rate, "seconds": args.line_serve_seconds,
+            "hbm_budget_gb": args.hbm_budget_gb, "target_spp": [16, 64, 256, 1024],
+            "batched": serve_batched(jobs, args.line_serve_seconds, args, "arrival"),
+            "fifo": serve_fifo(jobs, args.line_serve_seconds, args.max_pending)}
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), with the machine architecture."""
+    import platform
+
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return f"{platform.machine()} {line.split(':', 1)[1].strip()}"
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu part")):
+                return f"{platform.machine()} {line.split(':', 1)[1].strip()}"
+    except OSError:
+        pass
+    return platform.machine()
+
+
+def cpu_small_scene(threads: int = 0) -> dict:
+    """The small scene (seed 0) in full on the host cores: 1280x720, 5 bounces, 64 frames, the
+    reference's per-pixel path restated in C (literal expression order), OpenMP over pixels."""
+    from ataraxia_gb300 import scenes
+    from oracle import pyoracle as po
+
+    po.build()
+    sc = scenes.config0()
+    view = po.view_for(sc)
+    nthreads = threads or po.max_threads()
+    t0 = time.perf_counter()
+    _, _, st = po.render(sc.spheres, sc.materials, sc.lights, view, max_bounces=sc.max_bounces, spp=64,
+                         mode=po.LITERAL, threads=nthreads)
+    dt = time.perf_counter() - t0
+    paths = sc.pixels * 64
+    return {"value": round(paths / dt / 1e6, 3), "unit": UNIT, "cores": nthreads, "kind": "port",
+            "cpu": cpu_model(), "seconds": round(dt, 2),
+            "mrays_per_s": round((st["ext_rays"] + st["shadow_rays"]) / dt / 1e6, 3),
+            "sample": "small scene in full: 9 spheres, 1280x720, 5 bounces, 64 frames = 58,982,400 paths"}
 
 
 def _pct(v, q):
@@ -699,8 +799,12 @@ def main(argv=None) -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-ref-kernel", action="store_true", help="skip timing the restated reference kernel")
+    ap.add_argument("--no-ref-kernel", action="store_true", help="skip timing the reference's own CUDA kernel")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the large-scene, batched-mix and serving legs of the default line")
+    ap.add_argument("--line-serve-rate", type=float, default=200.0, help="serving leg of the default line: jobs/s")
+    ap.add_argument("--line-serve-seconds", type=float, default=10.0, help="serving leg of the default line: seconds")
     ap.add_argument("--ref-step-seconds", type=float, default=3.0)
     ap.add_argument("--mode", choices=["full", "render", "batch", "serve"], default="full",
                     help="render: only warm-up + timed launches of the workload (for profiler captures); "

@@ -60,6 +60,21 @@ void orc_sincos2pi(float u, float* c, float* s)
     }
 }
 
+/* Branch-decision sink of one path (orc_decision_hash / orc_decision_events):
+ * events go to ev[0..cap) and into an FNV-1a hash of the decision bits (the
+ * shadow event's occluder field is recorded but not hashed). */
+typedef struct { uint32_t* ev; int32_t cap; int32_t n; uint64_t hash; } orc_sink;
+
+static inline void orc_emit(orc_sink* s, uint32_t kind, int32_t bounce, uint32_t value)
+{
+    if (!s) return;
+    const uint32_t e = (kind << 28) | (((uint32_t)bounce & 0xFFu) << 20) | (value & 0xFFFFFu);
+    const uint32_t decision = kind == ORC_EV_SHADOW ? (e & ~(0x3FFFFu << 2)) : e;
+    s->hash = (s->hash ^ decision) * 0x100000001b3ull;
+    if (s->ev && s->n < s->cap) s->ev[s->n] = e;
+    s->n++;
+}
+
 /* --------------------------------------------------------- instantiation */
 
 #define REAL float
@@ -395,10 +410,10 @@ int orc_render_f32(int mode, const orc_scene* sc, const orc_view* view, const or
                 uint32_t frame = job->frame0 + s;
                 float c[3];
                 if (mode == ORC_EXACT) {
-                    ex_v3 r = ex_per_pixel(sc, view, x, y, frame, job->max_bounces, job->sky_light, &st);
+                    ex_v3 r = ex_per_pixel(sc, view, x, y, frame, job->max_bounces, job->sky_light, &st, NULL);
                     c[0] = r.x; c[1] = r.y; c[2] = r.z;
                 } else {
-                    li_v3 r = li_per_pixel(sc, view, x, y, frame, job->max_bounces, job->sky_light, &st);
+                    li_v3 r = li_per_pixel(sc, view, x, y, frame, job->max_bounces, job->sky_light, &st, NULL);
                     c[0] = r.x; c[1] = r.y; c[2] = r.z;
                 }
                 acc[0] += c[0]; acc[1] += c[1]; acc[2] += c[2]; acc[3] += 1.0f;
@@ -435,7 +450,7 @@ int orc_render_f64(const orc_scene* sc, const orc_view* view, const orc_job* job
             uint32_t x = p % view->width, y = p / view->width;
             double* acc = accum + 4 * k;
             for (uint32_t s = 0; s < job->spp; ++s) {
-                d_v3 r = d_per_pixel(sc, view, x, y, job->frame0 + s, job->max_bounces, job->sky_light, &st);
+                d_v3 r = d_per_pixel(sc, view, x, y, job->frame0 + s, job->max_bounces, job->sky_light, &st, NULL);
                 acc[0] += r.x; acc[1] += r.y; acc[2] += r.z; acc[3] += 1.0;
                 if (samples) {
                     double* o = samples + 4 * ((uint64_t)k * job->spp + s);
@@ -447,6 +462,65 @@ int orc_render_f64(const orc_scene* sc, const orc_view* view, const orc_job* job
         stats_add(&total, &st);
     }
     if (stats) *stats = total;
+    return 0;
+}
+
+/* ------------------------------------------------------ branch decisions */
+
+static void decisions_of_path(int variant, const orc_scene* sc, const orc_view* view, uint32_t x, uint32_t y,
+                              uint32_t frame, const orc_job* job, orc_stats* st, orc_sink* sk)
+{
+    if (variant == ORC_EXACT) (void)ex_per_pixel(sc, view, x, y, frame, job->max_bounces, job->sky_light, st, sk);
+    else if (variant == ORC_LITERAL) (void)li_per_pixel(sc, view, x, y, frame, job->max_bounces, job->sky_light, st, sk);
+    else (void)d_per_pixel(sc, view, x, y, frame, job->max_bounces, job->sky_light, st, sk);
+}
+
+int orc_decision_hash(int variant, const orc_scene* sc, const orc_view* view, const orc_job* job, uint64_t* hash)
+{
+    if (check_args(sc, view, job) || !hash || variant < ORC_EXACT || variant > ORC_F64) return -1;
+    const uint64_t npx = job->pixels ? job->n_pixels : (uint64_t)view->width * view->height;
+#ifdef _OPENMP
+    int nt = job->threads > 0 ? job->threads : omp_get_max_threads();
+#endif
+#pragma omp parallel num_threads(nt)
+    {
+        orc_stats st;
+        memset(&st, 0, sizeof(st));
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t k = 0; k < (int64_t)npx; ++k) {
+            uint32_t p = job->pixels ? job->pixels[k] : (uint32_t)k;
+            orc_sink sk = { NULL, 0, 0, 0xcbf29ce484222325ull };
+            for (uint32_t s = 0; s < job->spp; ++s)
+                decisions_of_path(variant, sc, view, p % view->width, p / view->width, job->frame0 + s, job, &st, &sk);
+            hash[k] = sk.hash;
+        }
+    }
+    return 0;
+}
+
+int orc_decision_events(int variant, const orc_scene* sc, const orc_view* view, const orc_job* job, uint32_t* ev,
+                        int32_t cap)
+{
+    if (check_args(sc, view, job) || !ev || cap <= 0 || variant < ORC_EXACT || variant > ORC_F64) return -1;
+    const uint64_t npx = job->pixels ? job->n_pixels : (uint64_t)view->width * view->height;
+#ifdef _OPENMP
+    int nt = job->threads > 0 ? job->threads : omp_get_max_threads();
+#endif
+#pragma omp parallel num_threads(nt)
+    {
+        orc_stats st;
+        memset(&st, 0, sizeof(st));
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t k = 0; k < (int64_t)npx; ++k) {
+            uint32_t p = job->pixels ? job->pixels[k] : (uint32_t)k;
+            for (uint32_t s = 0; s < job->spp; ++s) {
+                uint32_t* row = ev + ((uint64_t)k * job->spp + s) * (uint64_t)cap;
+                memset(row, 0, sizeof(uint32_t) * (size_t)cap);
+                orc_sink sk = { row, cap, 0, 0 };
+                decisions_of_path(variant, sc, view, p % view->width, p / view->width, job->frame0 + s, job, &st, &sk);
+            }
+        }
+    }
     return 0;
 }
 

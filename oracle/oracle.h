@@ -125,6 +125,27 @@ void orc_cook_torrance(int mode, const float albedo[3], const float f0[3], float
 void orc_sample_cosine(int mode, const float n[3], uint32_t* seed, float out[3]);
 void orc_sample_ggx(int mode, const float n[3], float roughness, uint32_t* seed, float out[3]);
 
+/* Branch decisions, for counting and classifying branch flips between
+ * arithmetic modes.  variant: ORC_EXACT, ORC_LITERAL or ORC_F64 (the literal
+ * expressions in double precision).  Each decision of a path is one event,
+ * kind << 28 | bounce << 20 | value:
+ *   ORC_EV_HIT       value = nearest sphere + 1, 0 on a miss (Renderer.cu:308-318)
+ *   ORC_EV_SHADOW    value bits 0-1: 1 the light is visible, 2 occluded
+ *                    (Renderer.cu:351-355); bits 2-19: the shadow ray's nearest
+ *                    sphere + 1, recorded but not part of the decision
+ *   ORC_EV_ROULETTE  value 1 when the path stops (Renderer.cu:375-377)
+ *   ORC_EV_FRAME     value 1 when |N.x| > |N.y| picks the samplers' first
+ *                    tangent (BRDF.cu:85, :109)
+ * orc_decision_hash: per pixel (job->pixels or all), an FNV-1a hash of the
+ * decisions of its frames frame0 .. frame0+spp-1.  orc_decision_events: per
+ * pixel and frame, the first cap events (unused slots 0).  Both return 0, or
+ * -1 on bad arguments. */
+enum { ORC_F64 = 2 };
+enum { ORC_EV_HIT = 1, ORC_EV_SHADOW = 2, ORC_EV_ROULETTE = 3, ORC_EV_FRAME = 4 };
+int orc_decision_hash(int variant, const orc_scene* scene, const orc_view* view, const orc_job* job, uint64_t* hash);
+int orc_decision_events(int variant, const orc_scene* scene, const orc_view* view, const orc_job* job,
+                        uint32_t* events, int32_t cap);
+
 /* Renderer.cu:166-168 + Renderer.h:70-78 */
 void orc_pack_rgba8(const float* accum, uint64_t n, uint32_t frame, uint32_t* out);
 

@@ -285,7 +285,7 @@ static V3 FN(sample_ggx)(V3 n, REAL rough, uint32_t* seed)
 
 /* Renderer.cu:287-387.  Returns the path colour; alpha is always 1. */
 static V3 FN(per_pixel)(const orc_scene* sc, const orc_view* view, uint32_t x, uint32_t y, uint32_t frame,
-                        int32_t max_bounces, int32_t sky, orc_stats* st)
+                        int32_t max_bounces, int32_t sky, orc_stats* st, orc_sink* sk)
 {
     V3 o = FN(ld)(view->position);
     V3 d = FN(primary_dir)(view, x, y);
@@ -299,6 +299,7 @@ static V3 FN(per_pixel)(const orc_scene* sc, const orc_view* view, uint32_t x, u
         REAL tmin;
         st->ext_rays++;
         int32_t idx = FN(nearest)(sc->spheres, sc->n_spheres, o, d, &tmin, &st->sphere_tests);
+        orc_emit(sk, ORC_EV_HIT, i, (uint32_t)(idx + 1));
         if (idx < 0) {
             if (sky) color = FN(add)(color, FN(mul)(FN(mk)((REAL)0.6f, (REAL)0.7f, (REAL)0.9f), thr));
             break;
@@ -330,7 +331,9 @@ static V3 FN(per_pixel)(const orc_scene* sc, const orc_view* view, uint32_t x, u
             st->shadow_rays++;
             int32_t sidx = FN(nearest)(sc->spheres, sc->n_spheres, so, L, &ts, &st->sphere_tests);
             REAL tsh = sidx < 0 ? (REAL)-1 : ts;
-            if (tsh > (REAL)0 && tsh * tsh < dist2) {
+            const int occluded = tsh > (REAL)0 && tsh * tsh < dist2;
+            orc_emit(sk, ORC_EV_SHADOW, i, (occluded ? 2u : 1u) | ((uint32_t)(sidx + 1) << 2));
+            if (occluded) {
                 /* occluded */
             } else {
                 V3 f = FN(cook_torrance)(albedo, base, metallic, (REAL)m->roughness, h.normal, FN(neg)(d), L);
@@ -344,8 +347,11 @@ static V3 FN(per_pixel)(const orc_scene* sc, const orc_view* view, uint32_t x, u
         o = FN(add)(h.pos, FN(muls)(h.normal, (REAL)0.0001f));
 
         REAL p = FN(maxr)((REAL)0.1f, FN(minr)((REAL)1, FN(length)(thr)));
-        if (FN(pcg_float)(&seed) > p) break;
+        const int stop = FN(pcg_float)(&seed) > p;
+        orc_emit(sk, ORC_EV_ROULETTE, i, (uint32_t)stop);
+        if (stop) break;
         thr = FN(divs)(thr, p);
+        orc_emit(sk, ORC_EV_FRAME, i, (uint32_t)(FABS(h.normal.x) > FABS(h.normal.y)));
 
         if (m->metallic > 0.0f)
             d = FN(sample_ggx)(h.normal, (REAL)m->roughness, &seed);

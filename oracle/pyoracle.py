@@ -94,6 +94,9 @@ def lib(contract: bool = False):
         h.orc_max_threads.restype = C.c_int
         h.orc_camera_on_update.argtypes = [P, P, P, P, C.c_int, P, C.c_float]
         h.orc_camera_on_update.restype = C.c_int
+        h.orc_decision_hash.argtypes = [C.c_int, C.POINTER(OrcScene), C.POINTER(OrcView), C.POINTER(OrcJob), P]
+        h.orc_decision_events.argtypes = [C.c_int, C.POINTER(OrcScene), C.POINTER(OrcView), C.POINTER(OrcJob), P,
+                                          C.c_int32]
         _libs[path] = h
     return _libs[path]
 
@@ -161,6 +164,40 @@ def render(spheres, materials, lights, view: OrcView, *, max_bounces=5, sky=Fals
         raise ValueError("oracle rejected the arguments")
     del keep
     return acc, smp, {k: getattr(st, k) for k, _ in OrcStats._fields_}
+
+
+F64 = 2
+EV_HIT, EV_SHADOW, EV_ROULETTE, EV_FRAME = 1, 2, 3, 4
+
+
+def decision_hash(spheres, materials, lights, view: OrcView, *, max_bounces=5, sky=False, frame0=1, spp=1,
+                  pixels=None, variant=EXACT, contract=False, threads=0) -> np.ndarray:
+    """Per pixel, a 64-bit hash of the branch decisions of its frames (oracle.h, orc_decision_hash).
+    variant EXACT, LITERAL or F64; contract=True runs the literal expressions with contraction."""
+    sc, keep = _scene(spheres, materials, lights)
+    px = None if pixels is None else np.ascontiguousarray(pixels, dtype=np.uint32)
+    n = (view.width * view.height) if px is None else len(px)
+    out = np.zeros(n, dtype=np.uint64)
+    job = OrcJob(max_bounces, int(bool(sky)), frame0, spp, _p(px), 0 if px is None else len(px), threads)
+    if lib(contract).orc_decision_hash(variant, C.byref(sc), C.byref(view), C.byref(job), _p(out)) != 0:
+        raise ValueError("oracle rejected the arguments")
+    del keep
+    return out
+
+
+def decision_events(spheres, materials, lights, view: OrcView, pixels, *, max_bounces=5, sky=False, frame0=1,
+                    spp=1, variant=EXACT, contract=False, threads=0) -> np.ndarray:
+    """Branch-decision events [pixel, frame, event] of the listed pixels (oracle.h, orc_decision_events)."""
+    sc, keep = _scene(spheres, materials, lights)
+    px = np.ascontiguousarray(pixels, dtype=np.uint32)
+    cap = 4 * max(int(max_bounces), 1) + 4
+    out = np.zeros((len(px), spp, cap), dtype=np.uint32)
+    job = OrcJob(max_bounces, int(bool(sky)), frame0, spp, _p(px), len(px), threads)
+    if len(px) and lib(contract).orc_decision_events(variant, C.byref(sc), C.byref(view), C.byref(job), _p(out),
+                                                     cap) != 0:
+        raise ValueError("oracle rejected the arguments")
+    del keep
+    return out
 
 
 def trace(spheres, origins, dirs, mode=EXACT):

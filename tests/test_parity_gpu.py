@@ -286,8 +286,9 @@ def test_literal_reference_order_within_fma_contraction_spread(po):
     """Counted and reported: pixels outside 1e-3 against the reference's expressions evaluated
     literally.  The reference's quadratic loses ~1e-4 in t at camera distance ~60 (cancellation in
     b^2 - a c), more than its 1e-4 surface offset, so the literal expressions compiled with and
-    without FMA contraction already disagree on a few percent of pixels; the kernels must not do
-    worse than that spread."""
+    without FMA contraction already disagree on a few percent of pixels; the kernels stay within 1.25
+    times that spread plus 0.1% (measured: 0.09% vs 0.05% on the small scene, 2.05% vs 1.87% on the
+    medium one)."""
     for sc, spp in [(scenes.config0().with_resolution(160, 90), 4), (scenes.config1().with_resolution(192, 108), 4)]:
         acc, _ = gpu_render(sc, spp)
         lit, _, _ = oracle_render(sc, spp, mode=po.LITERAL)
@@ -295,15 +296,18 @@ def test_literal_reference_order_within_fma_contraction_spread(po):
         ours = frac_outside(acc, lit)
         spread = frac_outside(con, lit)
         print(f"{sc.name}: outside 1e-3 vs literal {ours:.4%}; contraction spread {spread:.4%}")
-        assert ours <= 2.0 * spread + 0.005
+        assert ours <= 1.25 * spread + 0.001
 
 
 def test_converged_image_within_3_sigma_of_float64(po):
-    """4096 frames of the medium scene on the GPU against the reference's expressions evaluated in
-    float64 with the same random stream: each pixel's mean lies within 3 standard errors (estimated
-    from the float64 per-frame samples) on at least 99.5% of (pixel, channel) pairs.  Pixels whose
-    primary ray hits a sphere are compared (the others are exact closed forms)."""
-    sc = scenes.config1().with_resolution(192, 108)
+    """4096 frames of the medium scene at its full 1920x1080 on the GPU against the reference's
+    expressions evaluated in float64 with the same random stream: each pixel's mean lies within 3
+    standard errors (estimated from the float64 per-frame samples) on at least 99.5% of (pixel,
+    channel) pairs, over 2,000 pixels drawn from those whose primary ray hits a sphere (the others are
+    exact closed forms).  The random stream is the same, so the differences are the float32
+    evaluation's own: a glossy lobe amplifies the quadratic's cancellation error into a percent of
+    radiance on a few pixels (measured: 99.77% of 6,000 pairs within 3 sigma)."""
+    sc = scenes.config1()
     spp = 4096
     view = po.view_for(sc)
     dirs = po.ray_dirs(view)
@@ -311,7 +315,7 @@ def test_converged_image_within_3_sigma_of_float64(po):
     _, ids = po.trace(sc.spheres, origins, dirs)
     hit_px = np.flatnonzero(ids >= 0)
     rng = np.random.default_rng(0)
-    px = np.sort(rng.choice(hit_px, size=min(400, len(hit_px)), replace=False)).astype(np.uint32)
+    px = np.sort(rng.choice(hit_px, size=min(2000, len(hit_px)), replace=False)).astype(np.uint32)
     acc, _ = gpu_render(sc, spp)
     ref, smp, _ = po.render(sc.spheres, sc.materials, sc.lights, view, max_bounces=sc.max_bounces, spp=spp,
                             pixels=px, f64=True, samples=True)
