@@ -237,13 +237,6 @@ def device_count() -> int:
     return n.value
 
 
-def measure_fp32_peak(device: int = 0) -> float:
-    """FP32 FFMA throughput of the device in TFLOP/s (atx_measure_fp32_peak)."""
-    t = C.c_double(0.0)
-    N.check(N.lib().atx_measure_fp32_peak(device, C.byref(t)))
-    return t.value
-
-
 def camera_matrices(camera: Camera, width: int, height: int):
     """Camera.cpp:134-159 on the host: (view, inv_view, proj, inv_proj) as 4x4 column-major float32
     arrays (element [c, r] = column c, row r, as glm stores them).  Needs no GPU."""

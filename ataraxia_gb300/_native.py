@@ -159,7 +159,6 @@ SIGNATURES = {
     "atx_get_kernel_times": (_ST, [_P, C.POINTER(KernelTimes)]),
     "atx_reset_kernel_times": (_ST, [_P]),
     "atx_get_stream": (_ST, [_P, C.POINTER(_P)]),
-    "atx_measure_fp32_peak": (_ST, [C.c_int32, C.POINTER(C.c_double)]),
     "atx_host_alloc": (_ST, [_U64, C.POINTER(_P)]),
     "atx_host_free": (_ST, [_P]),
     "atx_camera_matrices": (_ST, [C.POINTER(CameraDesc), _U32, _U32, _P, _P, _P, _P]),

@@ -187,6 +187,10 @@ __device__ __forceinline__ int32_t bvh_nearest(const SceneView& sc, float3 o, fl
 {
     const BvhView& b = sc.bvh;
     const float a = dot3(d, d);
+    // tm must start finite: culled slots carry the key +inf, and the leaf loop
+    // below ends at the first key beyond tm, so +inf here would run the leaf
+    // test on culled clusters
+    static_assert(kFltMax < __builtin_huge_valf(), "the nearest-hit walk's tm must start finite");
     float tm = kFltMax;
     int32_t best = -1;
     if (b.n_leaves < 2 || b.n_leaves <= b.leaf_size) {   // the whole tree is one cluster

@@ -226,20 +226,6 @@ ATX_API atx_status atx_get_stream(atx_renderer* r, void** stream)
     });
 }
 
-ATX_API atx_status atx_measure_fp32_peak(int32_t device, double* tflops)
-{
-    return guarded([&]() -> atx_status {
-        if (!tflops) return atx::fail(ATX_ERR_INVALID_ARG, "atx_measure_fp32_peak: null pointer");
-        int n = 0;
-        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
-            (void)cudaGetLastError();
-            return atx::fail(ATX_ERR_NO_DEVICE, "no CUDA device visible");
-        }
-        ATX_CUDA(atx::measure_fp32_peak(device, tflops));
-        return ATX_OK;
-    });
-}
-
 ATX_API atx_status atx_host_alloc(uint64_t bytes, void** out)
 {
     return guarded([&]() -> atx_status {

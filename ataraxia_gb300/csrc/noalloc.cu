@@ -12,13 +12,14 @@
 // until the process exits, and every call on a device reuses it.  Calls whose
 // work overlaps on the GPU (two streams, or two host threads) race on it and
 // must be serialised by the caller.  In host code the array's name is only a
-// host-side stand-in, so its device address is looked up once per device with
-// cudaGetSymbolAddress (with that device current) on the first call made on
-// the device; make that first call before any stream capture.
+// host-side stand-in, so every call looks up its device address on the current
+// device with cudaGetSymbolAddress.  The first call on a device also loads the
+// module there (the set-up); make that first call before any stream capture.
+// Looking the address up on every call (cheap once the module is loaded) keeps
+// it right after the caller resets the device and the module loads again.
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
-#include <mutex>
 
 #include "atx.h"
 #include "host_common.h"
@@ -33,25 +34,16 @@ constexpr uint32_t kMaxSpheres = 16384;
 constexpr uint32_t kMaxMaterials = 4096;
 constexpr uint32_t kMaxLights = 1024;
 constexpr int32_t kMaxBounces = 1024;
-constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
-
-// Device address of g_scratch on the current device (looked up once).
-atx_status scratch_address(int device, unsigned char** out)
+// Device address of g_scratch on the current device.
+atx_status scratch_address(unsigned char** out)
 {
-    if (device < 0 || device >= kMaxDevices) return fail(ATX_ERR_INVALID_ARG, "render_noalloc: device %d", device);
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
-        g_addr[device] = p;
-    }
-    *out = static_cast<unsigned char*>(g_addr[device]);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
+    *out = static_cast<unsigned char*>(p);
     return ATX_OK;
 }
 
@@ -123,11 +115,14 @@ extern "C" ATX_API atx_status atx_render_noalloc(const atx_sphere* spheres, uint
         return fail(ATX_ERR_INVALID_ARG, "render_noalloc: spheres need at least one material");
     if (frame_index == 0) return fail(ATX_ERR_INVALID_ARG, "render_noalloc: frame_index starts at 1");
     if (spp == 0) return ATX_OK;
+    if ((uint64_t)(settings->accumulation ? frame_index : 1u) + spp - 1u > 0xffffffffull)
+        return fail(ATX_ERR_INVALID_ARG, "render_noalloc: frames %u..%u+%u-1 pass the frame index range",
+                    frame_index, frame_index, spp);
 
     int device = 0;
     ATX_CUDA(cudaGetDevice(&device));
     unsigned char* base = nullptr;
-    ATX_TRY(scratch_address(device, &base));
+    ATX_TRY(scratch_address(&base));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
     // carve the scratch: scene tables first, then the wave state

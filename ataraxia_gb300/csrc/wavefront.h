@@ -263,9 +263,6 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
 // Zeroes n float4 on stream.
 cudaError_t enqueue_clear_accum(float4* accum, uint64_t n, cudaStream_t stream);
 
-// FP32 FFMA throughput of the device in TFLOP/s (probe.cu).
-cudaError_t measure_fp32_peak(int device, double* tflops);
-
 // Debug / parity hook: nearest hit for n rays through the same device code the
 // renderer uses.  origins/dirs are 3 floats per ray in device memory.
 cudaError_t enqueue_trace_nearest(const SceneView& sc, const float* origins, const float* dirs, uint64_t n,

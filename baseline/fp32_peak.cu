@@ -1,10 +1,10 @@
-// FP32 throughput probe: the FP32-pipe roofline denominator of this device.
+// FP32 throughput probe: the FP32-pipe roofline denominator of this device,
+// for bench.py (measurement infrastructure; the renderer never loads it).
 // Every thread runs eight independent fused multiply-add chains on registers
 // (no memory traffic inside the loop), with enough warps per SM to cover the
 // FFMA latency.  FLOPs = 2 per FMA.  Best of several timed launches.
-#include "wavefront.h"
+#include <cuda_runtime.h>
 
-namespace atx {
 namespace {
 
 constexpr int kIters = 4096;
@@ -24,7 +24,8 @@ __global__ void __launch_bounds__(256) k_ffma(float* out, float a, float b)
 
 }  // namespace
 
-cudaError_t measure_fp32_peak(int device, double* tflops)
+// Returns a cudaError_t as int; *tflops = FP32 TFLOP/s of the device.
+extern "C" __attribute__((visibility("default"))) int fp32_peak_tflops(int device, double* tflops)
 {
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return e;
@@ -60,5 +61,3 @@ cudaError_t measure_fp32_peak(int device, double* tflops)
     *tflops = best;
     return cudaGetLastError();
 }
-
-}  // namespace atx

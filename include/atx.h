@@ -209,11 +209,6 @@ ATX_API atx_status atx_reset_kernel_times(atx_renderer* r);
  * work and timing events after the renderer's. */
 ATX_API atx_status atx_get_stream(atx_renderer* r, void** stream);
 
-/* Measures the device's FP32 fused multiply-add throughput (TFLOP/s, FMA =
- * 2 FLOP) with a register-resident FFMA loop on every SM: the roofline
- * denominator for the FP32-bound kernels. */
-ATX_API atx_status atx_measure_fp32_peak(int32_t device, double* tflops);
-
 /* Page-locked host memory for fast copies in and out. */
 ATX_API atx_status atx_host_alloc(uint64_t bytes, void** out);
 ATX_API atx_status atx_host_free(void* p);
@@ -384,15 +379,17 @@ ATX_API atx_status atx_server_now(atx_server* s, double* seconds);
  *     pointers; inv_view/inv_proj/position/settings are host pointers.
  *   - Frame semantics are atx_render's: frame frame_index (>= 1) onward,
  *     frame 1 clears the accumulator, accumulation off renders frames 1..spp.
+ *     Frames past 2^32 - 1 return ATX_ERR_INVALID_ARG.
  *   - Limits: 16384 spheres, 4096 materials, 1024 lights, 1024 bounces;
  *     larger inputs return ATX_ERR_INVALID_ARG.  Always the brute-force
  *     nearest-hit loop (no BVH, which would need its own scratch).
  *   - Work is enqueued on stream (a cudaStream_t, NULL = default stream).
  *     All calls share the one scratch array, so calls that overlap on the GPU
  *     race: serialise them.
- *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture. */
+ *   - Every call looks up the array's device address on the current device
+ *     (cudaGetSymbolAddress); the first call on a device also loads the
+ *     library's device code there, so make that first call before any
+ *     stream capture. */
 ATX_API atx_status atx_render_noalloc(const atx_sphere* spheres, uint32_t n_spheres, const atx_material* materials,
                                       uint32_t n_materials, const atx_light* lights, uint32_t n_lights,
                                       const float inv_view[16], const float inv_proj[16], const float position[3],

@@ -2,7 +2,7 @@
 reference's own exporter, Utils::exportScene) into tests/golden/reference_sample_scene.json, and
 records the world-space spheres its scene graph flattens to under the oracle (oracle/scene_graph.py).
 
-    python tests/golden/make_scene_fixtures.py [path to the reference tree]
+    python tests/golden/make_scene_fixtures.py <path to the reference tree>
 
 The copied file is data the reference produced, not source: it pins both the reader (every key the
 reference writes) and the writer (the library must write it back byte for byte)."""
@@ -20,7 +20,9 @@ from oracle import scene_graph as osg  # noqa: E402
 
 
 def main() -> None:
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_scene_fixtures.py <path to the reference tree>")
+    ref = Path(sys.argv[1])
     text = (ref / "sample-scene-data" / "scene.json").read_bytes()
     (HERE / "reference_sample_scene.json").write_bytes(text)
     flat = osg.flatten_file_text(text.decode())

@@ -16,7 +16,7 @@ branch.  So:
   reference's own builds do (plus 0.1%), and on the flip-free pixels (oracle.flips: the matched-order,
   literal, contracted and float64 evaluations take the same branches in every frame) ours agree with
   it at least as often as its own nofmad and ieee builds do.  On the well-conditioned pixels (flip-free,
-  and both single-precision evaluations within 1e-3 of float64) at least 99.9% agree with the fast and
+  and both single-precision evaluations within 5e-4 of float64) at least 99.9% agree with the fast and
   the ieee build.  The rest is the reference's own ill-conditioning: the quadratic's cancellation at a
   distance moves hit points by ~1e-4 and glossy GGX lobes turn that into a percent of radiance without
   any branch flip, so its own builds disagree there as much as ours do.  Flips are counted by cause;
