@@ -330,6 +330,32 @@ def run_ours(args, dist: Dist):
                 roofline["traffic"] = int(line.split(":", 1)[1])
                 roofline["traffic_source"] = "profiles/render_traffic_medium_scene.txt (ncu)"
 
+    # FP32 roofline: FP32 work executed by the same launch's kernels (ncu instruction counts, summarised in
+    # profiles/) over the launch's device time, against the FP32 pipe peak measured on this GPU
+    fp32_file = ROOT / "profiles" / "fp32_ops_medium_scene.md"
+    flops = None
+    if fp32_file.exists():
+        for line in fp32_file.read_text().splitlines():
+            if line.startswith("fp32_flops_per_launch:"):
+                flops = int(line.split(":", 1)[1])
+    if flops:
+        from baseline import fp32
+
+        fpeak = fp32.peak_tflops(dev)
+        f_ach = flops / (launch_ms * 1e-3) / 1e12
+        f_step = flops / (ms_local / args.steps * 1e-3) / 1e12
+        out_fp32 = {"bound": "fp32", "achieved": round(f_ach, 2), "peak": round(fpeak, 1), "unit": "TFLOP/s",
+                    "frac": round(f_ach / fpeak, 4) if fpeak else None,
+                    "achieved_over_bench_step": round(f_step, 2),
+                    "frac_over_bench_step": round(f_step / fpeak, 4) if fpeak else None,
+                    "flops_per_launch": flops,
+                    "flops_source": "profiles/fp32_ops_medium_scene.md (ncu: FADD + FMUL + 2 FFMA + 2 FADD2 + "
+                                    "2 FMUL2 + 4 FFMA2 thread instructions of one launch's kernels)",
+                    "peak_source": "baseline/fp32_peak.cu: register-resident FFMA chains on every SM of this GPU, "
+                                   "best of five launches"}
+    else:
+        out_fp32 = None
+
     ref_kernel = None
     if dist.world == 1 and not args.no_ref_kernel:
         ref_kernel = time_reference_kernel(sc, cam, dev, args)
@@ -348,6 +374,7 @@ def run_ours(args, dist: Dist):
         "gpu_launches": int(launches),
         "clocks": clk,
         "roofline": roofline,
+        "fp32_roofline": out_fp32,
         "e2e": e2e,
     }
     if ref_kernel:
