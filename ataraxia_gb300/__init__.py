@@ -388,6 +388,23 @@ class Renderer:
         N.check(N.lib().atx_get_kernel_times(self._h, C.byref(t)))
         return {k: getattr(t, k) for k, _ in N.KernelTimes._fields_}
 
+    def autotune(self, spp: int, passes: int = 2, use_cache: bool = True) -> dict:
+        """Times launch settings (LBVH leaf size, lanes, path state, block size, wave shape) on the current
+        scene, camera and viewport and keeps the fastest (atx_autotune); every setting renders the same
+        frames bit for bit.  The renderer is left at frame 1."""
+        t = N.Tuning()
+        N.check(N.lib().atx_autotune(self._h, spp, passes, int(bool(use_cache)), C.byref(t)))
+        return {k: getattr(t, k) for k, _ in N.Tuning._fields_}
+
+    def tuning(self) -> dict:
+        t = N.Tuning()
+        N.check(N.lib().atx_get_tuning(self._h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in N.Tuning._fields_}
+
+    def set_tuning(self, bvh_leaf_size=0, lanes=0, wave_paths=0, threads=0, wave_spp=0):
+        t = N.Tuning(bvh_leaf_size, lanes, wave_paths, threads, wave_spp, 0, 0.0)
+        N.check(N.lib().atx_set_tuning(self._h, C.byref(t)))
+
     def reset_kernel_times(self):
         N.check(N.lib().atx_reset_kernel_times(self._h))
 

@@ -73,6 +73,11 @@ class Stats(C.Structure):
                 ("shaded_first", C.c_uint64)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("bvh_leaf_size", C.c_uint32), ("lanes", C.c_uint32), ("wave_paths", C.c_uint32),
+                ("threads", C.c_uint32), ("wave_spp", C.c_uint32), ("from_cache", C.c_uint32), ("ms", C.c_double)]
+
+
 class KernelTimes(C.Structure):
     _fields_ = [("extend_ms", C.c_double), ("shadow_ms", C.c_double), ("accumulate_ms", C.c_double),
                 ("other_ms", C.c_double), ("extend_launches", C.c_uint64), ("shadow_launches", C.c_uint64),
@@ -159,6 +164,9 @@ SIGNATURES = {
     "atx_get_kernel_times": (_ST, [_P, C.POINTER(KernelTimes)]),
     "atx_reset_kernel_times": (_ST, [_P]),
     "atx_get_stream": (_ST, [_P, C.POINTER(_P)]),
+    "atx_autotune": (_ST, [_P, _U32, _U32, C.c_int32, C.POINTER(Tuning)]),
+    "atx_get_tuning": (_ST, [_P, C.POINTER(Tuning)]),
+    "atx_set_tuning": (_ST, [_P, C.POINTER(Tuning)]),
     "atx_host_alloc": (_ST, [_U64, C.POINTER(_P)]),
     "atx_host_free": (_ST, [_P]),
     "atx_camera_matrices": (_ST, [C.POINTER(CameraDesc), _U32, _U32, _P, _P, _P, _P]),

@@ -227,7 +227,19 @@ atx_status Batch::set_tuning(const atx_batch_tuning& t)
             if (p) p->prim_valid = false;
     }
     if (t.bvh_threshold) tuning_.bvh_threshold = t.bvh_threshold;   // scenes added from now on
-    if (t.bvh_leaf_size) tuning_.bvh_leaf_size = t.bvh_leaf_size;
+    if (t.bvh_leaf_size && t.bvh_leaf_size != tuning_.bvh_leaf_size) {
+        // resident LBVH scenes are rebuilt with the new leaf size (their frames do not change: the walk is
+        // exact for any leaf size); the next pass captures a new graph with their new tree views
+        if (t.bvh_leaf_size > 64u) return fail(ATX_ERR_INVALID_ARG, "batch tuning: leaf size above 64");
+        tuning_.bvh_leaf_size = t.bvh_leaf_size;
+        ATX_CUDA(cudaStreamSynchronize(stream_));
+        for (auto& p : slots_)
+            if (p && p->scene.view.use_bvh) {
+                p->scene.bvh_leaf = t.bvh_leaf_size;
+                ATX_TRY(p->scene.rebuild_bvh(t.bvh_leaf_size, up_stream_));
+            }
+        drop_graph();
+    }
     return ATX_OK;
 }
 
@@ -263,6 +275,47 @@ atx_status Batch::autotune(uint32_t passes, atx_batch_tuning* chosen)
             best = ms;
             pick = tuning_;
         }
+    }
+    ATX_TRY(set_tuning(pick));
+    // then the LBVH leaf size (when the mix has LBVH scenes) and the block size
+    // of the primary and shadow kernels, one at a time from the pick
+    auto trial = [&](atx_batch_tuning t) -> atx_status {
+        ATX_TRY(set_tuning(t));
+        ATX_TRY(run());
+        ATX_TRY(run());
+        double ms = 0.0;
+        for (uint32_t k = 0; k < passes; ++k) {
+            ATX_TRY(run());
+            atx_batch_stats st;
+            ATX_TRY(stats(&st));
+            ms += st.last_pass_ms;
+        }
+        reset_frames();
+        if (ms < best) {
+            best = ms;
+            pick = tuning_;
+        }
+        return ATX_OK;
+    };
+    bool any_bvh = false;
+    for (auto& p : slots_)
+        if (p && p->scene.view.use_bvh) any_bvh = true;
+    // explicit values, so that putting the pick back restores them
+    if (!pick.bvh_leaf_size) pick.bvh_leaf_size = 16;
+    if (!pick.threads) pick.threads = 256;
+    ATX_TRY(set_tuning(pick));
+    if (any_bvh)
+        for (uint32_t leaf : {8u, 12u, 24u, 32u}) {
+            atx_batch_tuning t = pick;
+            t.bvh_leaf_size = leaf;
+            ATX_TRY(trial(t));
+            ATX_TRY(set_tuning(pick));
+        }
+    for (uint32_t threads : {128u, 256u}) {
+        atx_batch_tuning t = pick;
+        t.threads = threads;
+        ATX_TRY(trial(t));
+        ATX_TRY(set_tuning(pick));
     }
     ATX_TRY(set_tuning(pick));
     reset_frames();

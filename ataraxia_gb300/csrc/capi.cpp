@@ -226,6 +226,33 @@ ATX_API atx_status atx_get_stream(atx_renderer* r, void** stream)
     });
 }
 
+ATX_API atx_status atx_autotune(atx_renderer* r, uint32_t spp, uint32_t passes, int32_t use_cache, atx_tuning* out)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        if (!out) return atx::fail(ATX_ERR_INVALID_ARG, "atx_autotune: null pointer");
+        return r->impl.autotune(spp, passes, use_cache != 0, out);
+    });
+}
+
+ATX_API atx_status atx_get_tuning(atx_renderer* r, atx_tuning* out)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        if (!out) return atx::fail(ATX_ERR_INVALID_ARG, "atx_get_tuning: null pointer");
+        return r->impl.tuning(out);
+    });
+}
+
+ATX_API atx_status atx_set_tuning(atx_renderer* r, const atx_tuning* t)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        if (!t) return atx::fail(ATX_ERR_INVALID_ARG, "atx_set_tuning: null pointer");
+        return r->impl.set_tuning(*t);
+    });
+}
+
 ATX_API atx_status atx_host_alloc(uint64_t bytes, void** out)
 {
     return guarded([&]() -> atx_status {

@@ -4,7 +4,11 @@
 #include "renderer.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "lbvh.h"
 #include "light_buffer.h"
@@ -117,6 +121,23 @@ atx_status SceneStore::upload(const atx_sphere* s, uint32_t n, const atx_materia
     return ATX_OK;
 }
 
+uint32_t SceneStore::leaf_size() const
+{
+    return view.use_bvh ? view.bvh.leaf_size : 0u;
+}
+
+atx_status SceneStore::rebuild_bvh(uint32_t leaf, cudaStream_t stream)
+{
+    if (!view.use_bvh) return ATX_OK;
+    if (leaf == 0) leaf = bvh_leaf ? bvh_leaf : kDefaultBvhLeaf;
+    if (leaf == view.bvh.leaf_size) return ATX_OK;
+    BvhView bv{};
+    ATX_CUDA(lbvh_build(view.sph, sph_rad.as<float>(), view.n_sph, leaf, bvh.get(), bvh.bytes(), &bv, stream));
+    view.bvh = bv;
+    ATX_CUDA(cudaStreamSynchronize(stream));
+    return ATX_OK;
+}
+
 // ------------------------------------------------------------------ waves
 
 uint64_t WaveStore::bytes_for(uint32_t capacity, uint32_t max_bounces)
@@ -158,11 +179,12 @@ atx_status WaveStore::ensure(uint32_t capacity, uint32_t max_bounces, Budget* bu
     return ATX_OK;
 }
 
-WavePlan plan_waves(uint64_t pixels, uint32_t spp, uint32_t capacity)
+WavePlan plan_waves(uint64_t pixels, uint32_t spp, uint32_t capacity, uint32_t cap_spp)
 {
     WavePlan p;
     // keep at least 256 pixels per wave so the first bounce fills the GPU
-    const uint32_t max_spp = std::max<uint32_t>(1, capacity / 256);
+    uint32_t max_spp = std::max<uint32_t>(1, capacity / 256);
+    if (cap_spp) max_spp = std::min(max_spp, cap_spp);
     p.spp_per_wave = std::min(spp, max_spp);
     uint64_t ppw = capacity / p.spp_per_wave;
     if (ppw < 1) ppw = 1;
@@ -233,12 +255,12 @@ atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore&
                           uint32_t frame0, uint32_t spp, int32_t max_bounces, int32_t sky, float4* accum,
                           uint32_t* image, uint32_t capacity, cudaStream_t stream, uint32_t* launches,
                           KernelTimer* timer, uint64_t* primary_rays, uint64_t pix_begin, uint64_t pix_end,
-                          uint2* prim_cache, bool prim_cached)
+                          uint2* prim_cache, bool prim_cached, uint32_t wave_spp)
 {
     const uint64_t all = (uint64_t)cam.width * cam.height;
     const uint64_t pend = std::min(pix_end, all);
     const uint64_t pbeg = std::min(pix_begin, pend);
-    const WavePlan plan = plan_waves(pend - pbeg, spp, capacity);
+    const WavePlan plan = plan_waves(pend - pbeg, spp, capacity, wave_spp);
     const uint32_t last_frame = frame0 + spp - 1;
     for (uint64_t p0 = pbeg; p0 < pend; p0 += plan.pixels_per_wave) {
         const uint32_t np = (uint32_t)std::min<uint64_t>(plan.pixels_per_wave, pend - p0);
@@ -354,6 +376,7 @@ atx_status Renderer::set_scene(const atx_sphere* s, uint32_t n, const atx_materi
     shape_valid_ = false;
     masks_valid_ = false;
     prev_cam_valid_ = false;
+    scene_.bvh_leaf = tune_.bvh_leaf_size ? tune_.bvh_leaf_size : cfg_.bvh_leaf_size;
     return scene_.upload(s, n, m, nm, l, nl, &budget_, stream_);
 }
 
@@ -471,7 +494,7 @@ atx_status Renderer::refresh_camera()
 atx_status Renderer::ensure_shape()
 {
     if (shape_valid_) return ATX_OK;
-    ATX_CUDA(plan_launch(scene_.view, cfg_.device, (int)cfg_.threads, &shape_));
+    ATX_CUDA(plan_launch(scene_.view, cfg_.device, (int)(tune_.threads ? tune_.threads : cfg_.threads), &shape_));
     shape_valid_ = true;
     return ATX_OK;
 }
@@ -492,11 +515,13 @@ atx_status Renderer::render(uint32_t spp)
     // scenes use all four (large scene: 4 lanes +11% over 2).
     const uint64_t px = (uint64_t)width_ * height_;
     const bool profile = (cfg_.flags & ATX_FLAG_PROFILE_KERNELS) != 0;
-    const uint32_t max_lanes = (!scene_.view.use_bvh && scene_.view.lb.n_lights) ? kBufferedLanes : kLanes;
-    const uint32_t lanes = (cfg_.wave_paths || profile || px < (uint64_t)max_lanes ||
+    uint32_t max_lanes = (!scene_.view.use_bvh && scene_.view.lb.n_lights) ? kBufferedLanes : kLanes;
+    if (tune_.lanes) max_lanes = std::min<uint32_t>(tune_.lanes, kLanes);
+    const uint32_t wave_paths = tune_.wave_paths ? tune_.wave_paths : cfg_.wave_paths;
+    const uint32_t lanes = ((cfg_.wave_paths && !tune_.lanes) || profile || px < (uint64_t)max_lanes ||
                             px * spp < (4ull << 20) * max_lanes) ? 1u : max_lanes;
     const uint64_t lane_px = (px + lanes - 1) / lanes;
-    uint32_t capacity = cfg_.wave_paths;
+    uint32_t capacity = wave_paths;
     if (!capacity) {
         const uint64_t lane_paths = lane_px * spp;
         const uint64_t want = (lane_paths + (1u << 20) - 1) & ~uint64_t((1u << 20) - 1);
@@ -531,7 +556,7 @@ atx_status Renderer::render(uint32_t spp)
         const uint64_t b = std::min(px, l * lane_px), e = std::min(px, (l + 1) * lane_px);
         ATX_TRY(enqueue_frames(scene_.view, camv_, wave_[l], shape_, f0, spp, bounces, sky, accum_.as<float4>(),
                                image_.as<uint32_t>(), capacity, lane_stream_[l], &launches, l == 0 ? timer : nullptr,
-                               &primary_rays, b, e));
+                               &primary_rays, b, e, nullptr, false, tune_.wave_spp));
     }
     for (uint32_t l = 1; l < lanes; ++l) {
         ATX_CUDA(cudaEventRecord(join_[l], lane_stream_[l]));
@@ -609,6 +634,171 @@ atx_status Renderer::kernel_times(atx_kernel_times* out)
     ATX_TRY(timer_.collect(&ktimes_));
     *out = ktimes_;
     return ATX_OK;
+}
+
+// ------------------------------------------------------------- autotuner
+
+namespace {
+
+// Tuned settings kept per process, keyed by the GPU (SM count and compute
+// capability) and a bucket of the workload: log2 of the sphere count, the
+// nearest-hit structure (LBVH, or brute force with light buffer or without),
+// log2 of the paths per launch and the bounce depth.
+struct TuneKey {
+    int sms, cc;
+    int sph_bucket, kind, path_bucket, bounces;
+    bool operator<(const TuneKey& o) const
+    {
+        return std::tie(sms, cc, sph_bucket, kind, path_bucket, bounces) <
+               std::tie(o.sms, o.cc, o.sph_bucket, o.kind, o.path_bucket, o.bounces);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, atx_tuning> g_tune_cache;
+
+int log2_bucket(uint64_t x)
+{
+    int b = 0;
+    while (x > 1) {
+        x >>= 1;
+        ++b;
+    }
+    return b;
+}
+
+}  // namespace
+
+atx_status Renderer::set_tuning(const atx_tuning& t)
+{
+    if (t.lanes > (uint32_t)kLanes) return fail(ATX_ERR_INVALID_ARG, "tuning: at most %d lanes", kLanes);
+    if (t.threads && (t.threads % 32u || t.threads > 256u))
+        return fail(ATX_ERR_INVALID_ARG, "tuning: threads must be a multiple of 32 up to 256");
+    if (t.bvh_leaf_size > 64u) return fail(ATX_ERR_INVALID_ARG, "tuning: leaf size above 64");
+    ATX_TRY(activate());
+    ATX_CUDA(cudaStreamSynchronize(stream_));
+    for (int l = 1; l < kLanes; ++l)
+        if (lane_stream_[l]) ATX_CUDA(cudaStreamSynchronize(lane_stream_[l]));
+    if (t.bvh_leaf_size != tune_.bvh_leaf_size && scene_.view.use_bvh) {
+        ATX_TRY(scene_.rebuild_bvh(t.bvh_leaf_size, stream_));
+        masks_valid_ = false;       // the tile candidate lists walk the tree
+        prev_cam_valid_ = false;
+    }
+    if (t.threads != tune_.threads) shape_valid_ = false;
+    tune_ = t;
+    tune_.from_cache = 0;
+    tune_.ms = 0.0;
+    return ATX_OK;
+}
+
+atx_status Renderer::tuning(atx_tuning* out)
+{
+    *out = tune_;
+    out->bvh_leaf_size = scene_.leaf_size();
+    return ATX_OK;
+}
+
+atx_status Renderer::time_renders(uint32_t spp, uint32_t passes, double* ms)
+{
+    frame_ = 1;
+    ATX_TRY(render(spp));   // the per-camera tables are built on the second render of a camera
+    ATX_TRY(render(spp));
+    double total = 0.0;
+    for (uint32_t k = 0; k < passes; ++k) {
+        ATX_TRY(render(spp));
+        ATX_CUDA(cudaEventSynchronize(ev_stop_));
+        float t = 0.0f;
+        ATX_CUDA(cudaEventElapsedTime(&t, ev_start_, ev_stop_));
+        total += t;
+    }
+    *ms = total / passes;
+    return ATX_OK;
+}
+
+atx_status Renderer::autotune(uint32_t spp, uint32_t passes, bool use_cache, atx_tuning* out)
+{
+    if (!width_ || !height_ || !accum_.get()) return fail(ATX_ERR_INVALID_ARG, "autotune: call atx_resize first");
+    if (!spp) return fail(ATX_ERR_INVALID_ARG, "autotune: spp must be positive");
+    if (!passes) passes = 2;
+    ATX_TRY(activate());
+    ATX_TRY(refresh_camera());
+    int sms = 0, major = 0, minor = 0;
+    ATX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg_.device));
+    ATX_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, cfg_.device));
+    ATX_CUDA(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, cfg_.device));
+    const SceneView& sv = scene_.view;
+    const int kind = sv.use_bvh ? 2 : (sv.lb.n_lights ? 1 : 0);
+    const TuneKey key{sms, 10 * major + minor, log2_bucket(sv.n_sph + 1ull), kind,
+                      log2_bucket((uint64_t)width_ * height_ * spp), settings_.max_bounces};
+    if (use_cache) {
+        atx_tuning hit{};
+        bool found = false;
+        {
+            std::lock_guard<std::mutex> lock(g_tune_mu);
+            auto it = g_tune_cache.find(key);
+            if (it != g_tune_cache.end()) {
+                hit = it->second;
+                found = true;
+            }
+        }
+        if (found) {
+            ATX_TRY(set_tuning(hit));
+            tune_.from_cache = 1;
+            tune_.ms = hit.ms;
+            frame_ = 1;
+            return tuning(out);
+        }
+    }
+    // coordinate descent from the defaults: leaf size, then lanes, path state,
+    // block size and the wave's tile shape, each keeping the best so far
+    atx_tuning best{};
+    ATX_TRY(set_tuning(best));
+    double best_ms = 0.0;
+    ATX_TRY(time_renders(spp, passes, &best_ms));
+    auto trial = [&](atx_tuning t) -> atx_status {
+        ATX_TRY(set_tuning(t));
+        double ms = 0.0;
+        ATX_TRY(time_renders(spp, passes, &ms));
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = t;
+        }
+        return ATX_OK;
+    };
+    if (sv.use_bvh)
+        for (uint32_t leaf : {4u, 8u, 12u, 24u, 32u}) {
+            atx_tuning t = best;
+            t.bvh_leaf_size = leaf;
+            ATX_TRY(trial(t));
+        }
+    for (uint32_t lanes : {1u, 2u, 4u}) {
+        atx_tuning t = best;
+        t.lanes = lanes;
+        ATX_TRY(trial(t));
+    }
+    for (uint32_t mi : {4u, 16u}) {
+        atx_tuning t = best;
+        t.wave_paths = mi << 20;
+        ATX_TRY(trial(t));
+    }
+    for (uint32_t threads : {128u}) {
+        atx_tuning t = best;
+        t.threads = threads;
+        ATX_TRY(trial(t));
+    }
+    for (uint32_t wspp : {1u, 4u}) {
+        if (wspp >= spp) continue;
+        atx_tuning t = best;
+        t.wave_spp = wspp;
+        ATX_TRY(trial(t));
+    }
+    ATX_TRY(set_tuning(best));
+    tune_.ms = best_ms;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache[key] = tune_;
+    }
+    frame_ = 1;
+    return tuning(out);
 }
 
 atx_status Renderer::trace_nearest(const float* o, const float* d, uint64_t n, float* t, int32_t* id)

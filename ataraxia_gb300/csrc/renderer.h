@@ -23,6 +23,10 @@ struct SceneStore {
     // Validates, converts and uploads on stream (Renderer.cu:25-57).
     atx_status upload(const atx_sphere* s, uint32_t n, const atx_material* m, uint32_t nm, const atx_light* l,
                       uint32_t nl, Budget* budget, cudaStream_t stream);
+    // Rebuilds the LBVH (when the scene uses one) with another leaf size from
+    // the resident sphere table; results are unchanged (the walk is exact).
+    atx_status rebuild_bvh(uint32_t leaf, cudaStream_t stream);
+    uint32_t leaf_size() const;
     uint64_t device_bytes() const
     {
         return sph.bytes() + sph_mat.bytes() + sph_rad.bytes() + mat.bytes() + lights.bytes() + bvh.bytes() +
@@ -46,7 +50,9 @@ struct WavePlan {
     uint32_t pixels_per_wave;
     uint32_t spp_per_wave;
 };
-WavePlan plan_waves(uint64_t pixels, uint32_t spp, uint32_t capacity);
+// max_spp (0: no cap) bounds the samples per wave: the wave's tile shape
+// (pixels x samples) for a fixed capacity.
+WavePlan plan_waves(uint64_t pixels, uint32_t spp, uint32_t capacity, uint32_t max_spp = 0);
 
 // Enqueues frames [frame0, frame0 + spp) for pixels [pix_begin, pix_end) of
 // the view (default: all of them).  prim_cache (W*H entries, optional) keeps
@@ -56,7 +62,8 @@ atx_status enqueue_frames(const SceneView& sc, const CameraView& cam, WaveStore&
                           uint32_t frame0, uint32_t spp, int32_t max_bounces, int32_t sky, float4* accum,
                           uint32_t* image, uint32_t capacity, cudaStream_t stream, uint32_t* launches,
                           KernelTimer* timer = nullptr, uint64_t* primary_rays = nullptr, uint64_t pix_begin = 0,
-                          uint64_t pix_end = ~uint64_t(0), uint2* prim_cache = nullptr, bool prim_cached = false);
+                          uint64_t pix_end = ~uint64_t(0), uint2* prim_cache = nullptr, bool prim_cached = false,
+                          uint32_t wave_spp = 0);
 
 // Records a pair of CUDA events around each kernel and sums their durations
 // per kernel family when collected.
@@ -101,6 +108,11 @@ public:
     atx_status primary_directions(float* host, uint64_t n);
     atx_status kernel_times(atx_kernel_times* out);
     void reset_kernel_times() { ktimes_ = atx_kernel_times{}; }
+    // Launch tuning (atx_tuning): the fields in use, and the autotuner that
+    // times candidates on the current scene, camera and viewport.
+    atx_status set_tuning(const atx_tuning& t);
+    atx_status tuning(atx_tuning* out);
+    atx_status autotune(uint32_t spp, uint32_t passes, bool use_cache, atx_tuning* out);
     cudaStream_t stream() const { return stream_; }
     uint32_t width() const { return width_; }
     uint32_t height() const { return height_; }
@@ -160,6 +172,10 @@ private:
     bool prev_cam_valid_ = false;
     LaunchShape shape_{};
     bool shape_valid_ = false;
+    // 0 fields: the defaults (lanes by scene kind, path state sized to the
+    // launch, the config's threads, as many samples per wave as fit)
+    atx_tuning tune_{};
+    atx_status time_renders(uint32_t spp, uint32_t passes, double* ms);
 
     atx_stats st_{};
     uint64_t totals_host_[2] = {0, 0};

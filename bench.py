@@ -438,7 +438,9 @@ def batch_compare(args, dev: int, steps: int) -> dict:
     time of its render calls alone (CUDA events around each launch, the scene already set), and as a
     caller sees it (wall clock over the whole loop: per scene resize, scene upload with its acceleration
     structures, camera, settings, the launch and the RGBA8 read-back).  gpu_idle_frac = the share of the
-    caller's loop in which no render kernel of the plain arm runs."""
+    caller's loop in which no render kernel of the plain arm runs.  saturated_ceiling = the mix's paths
+    over the device time they take when every scene is rendered alone in launches of at least 64 Mi
+    paths: what a launch structure that keeps each path's work can approach."""
     import numpy as np
     import torch
 
@@ -479,6 +481,26 @@ def batch_compare(args, dev: int, steps: int) -> dict:
             caller_s = time.perf_counter() - t0
     r.close()
 
+    # ceiling for any launch structure that keeps each path's work: every scene rendered alone in launches
+    # of >= 64 Mi paths (its tail amortised), device time per path summed over the mix's paths
+    r = atx.Renderer(device=dev, bvh_threshold=args.bvh_threshold, bvh_leaf_size=args.bvh_leaf)
+    stream = torch.cuda.ExternalStream(r.stream, device=dev)
+    ideal_ms = 0.0
+    for sc in mix:
+        r.on_resize(sc.width, sc.height)
+        r.set_scene(sc.spheres, sc.materials, sc.lights)
+        r.set_camera(atx.Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction))
+        r.set_settings(atx.Settings(True, sc.sky_light, sc.max_bounces))
+        big = max(sc.spp, -(-(64 << 20) // (sc.width * sc.height)))
+        r.render_frames(sc.spp)                # warm: per-camera tables built
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r.render_frames(big)
+        e1.record(stream)
+        e1.synchronize()
+        ideal_ms += e0.elapsed_time(e1) * sc.spp / big
+    r.close()
+
     b = atx.Batch(device=dev, bvh_threshold=args.bvh_threshold, bvh_leaf_size=args.bvh_leaf)
     if args.lanes or args.lane_wave:
         b.set_tuning(lanes=args.lanes, lane_wave_paths=args.lane_wave << 20)
@@ -510,6 +532,8 @@ def batch_compare(args, dev: int, steps: int) -> dict:
             "batched_ms_per_pass": round(batched_ms, 3),
             "batched_mpaths_s": round(paths / (batched_ms * 1e-3) / 1e6, 1),
             "batched_wall_mpaths_s": round(steps * paths / wall / 1e6, 1),
+            "saturated_ceiling_mpaths_s": round(paths / (ideal_ms * 1e-3) / 1e6, 1),
+            "batched_frac_of_ceiling": round(ideal_ms / batched_ms, 3),
             "speedup_vs_plain_device": round(plain_ms / batched_ms, 3),
             "speedup_vs_plain_caller": round(caller_s * 1e3 / (wall * 1e3 / steps), 3),
             "graph_launches": s1["graph_launches"] - s0["graph_launches"],
@@ -536,6 +560,9 @@ def large_scene_leg(args, dev: int) -> dict:
     r.set_scene(sc.spheres, sc.materials, sc.lights)
     r.set_camera(atx.Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction))
     r.set_settings(atx.Settings(accumulation=True, skyLight=False, maxBounces=sc.max_bounces))
+    t0 = time.perf_counter()
+    tuned = r.autotune(sc.spp, passes=2, use_cache=False) if not args.bvh_leaf else r.tuning()
+    tune_s = time.perf_counter() - t0
     for _ in range(3):
         r.render_frames(sc.spp)
     r.synchronize()
@@ -556,7 +583,10 @@ def large_scene_leg(args, dev: int) -> dict:
                         "8 bounces, 4 spp per launch (LBVH)",
             "mpaths_s": round(steps * sc.pixels * sc.spp / (ms * 1e-3) / 1e6, 1),
             "mrays_s": round(rays / (ms * 1e-3) / 1e6, 1), "ms_per_launch": round(ms / steps, 3),
-            "launches": steps, "bvh_in_use": int(s1["bvh_in_use"])}
+            "launches": steps, "bvh_in_use": int(s1["bvh_in_use"]),
+            "tuning": {k: tuned[k] for k in ("bvh_leaf_size", "lanes", "wave_paths", "threads", "wave_spp")},
+            "tuning_source": "atx_autotune on this scene, camera and GPU" if not args.bvh_leaf else "--bvh-leaf",
+            "autotune_s": round(tune_s, 2)}
 
 
 def serve_leg(args) -> dict:

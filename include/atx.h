@@ -100,7 +100,7 @@ typedef struct atx_config {
     uint32_t wave_paths;       /* paths in flight per wave; 0 = autotuned default */
     uint32_t threads;          /* threads per block; 0 = default */
     uint32_t bvh_threshold;    /* sphere count at which the LBVH replaces the brute-force tables; 0 = 1025 */
-    uint32_t bvh_leaf_size;    /* spheres per BVH leaf; 0 = autotuned */
+    uint32_t bvh_leaf_size;    /* spheres per BVH leaf; 0 = 16, or what atx_autotune picks */
     uint32_t flags;            /* ATX_FLAG_* */
     uint64_t hbm_budget_bytes; /* device bytes this renderer may hold; 0 = unlimited */
 } atx_config;
@@ -208,6 +208,34 @@ ATX_API atx_status atx_reset_kernel_times(atx_renderer* r);
 /* The renderer's CUDA stream (a cudaStream_t), so callers can order their own
  * work and timing events after the renderer's. */
 ATX_API atx_status atx_get_stream(atx_renderer* r, void** stream);
+
+/* Launch tuning of one renderer.  No counterpart in the reference, which
+ * launches one fixed (opt/32 x opt/32) grid per frame (Renderer.cu:190-207).
+ * Every setting renders the same frames bit for bit; only speed changes.  A
+ * zero field means the default. */
+typedef struct atx_tuning {
+    uint32_t bvh_leaf_size;    /* spheres per LBVH leaf cluster (LBVH scenes; default 16) */
+    uint32_t lanes;            /* concurrent lanes (streams with their own path state) a launch is split over */
+    uint32_t wave_paths;       /* path state per lane, paths (default: sized to the launch, up to 64 Mi) */
+    uint32_t threads;          /* threads per block of the primary and shadow kernels (multiple of 32, <= 256) */
+    uint32_t wave_spp;         /* samples per wave at most: the wave's tile shape of pixels x samples */
+    uint32_t from_cache;       /* atx_autotune: 1 when the setting came from the process-wide cache */
+    double ms;                 /* atx_autotune: device time of one render with the chosen setting */
+} atx_tuning;
+
+/* Times candidate settings on the renderer's current scene, camera,
+ * viewport and bounce depth, rendering spp frames per trial (passes timed
+ * renders each, after two untimed ones), by coordinate descent over the leaf
+ * size, lanes, path state, block size and wave shape, and keeps the fastest.
+ * Results are cached per process, keyed by the GPU (SM count, compute
+ * capability) and the workload's bucket (log2 spheres, nearest-hit structure,
+ * log2 paths per launch, bounces); use_cache = 1 takes a cached result
+ * without timing.  The renderer is left at frame 1 (its accumulator holds
+ * tuning frames until the next render clears it). */
+ATX_API atx_status atx_autotune(atx_renderer* r, uint32_t spp, uint32_t passes, int32_t use_cache,
+                                atx_tuning* out);
+ATX_API atx_status atx_get_tuning(atx_renderer* r, atx_tuning* out);
+ATX_API atx_status atx_set_tuning(atx_renderer* r, const atx_tuning* t);
 
 /* Page-locked host memory for fast copies in and out. */
 ATX_API atx_status atx_host_alloc(uint64_t bytes, void** out);

@@ -162,3 +162,25 @@ def test_autotune_leaves_no_trace():
         b.run()
         with pytest.raises(Exception):
             b.autotune()                       # scenes have rendered frames now
+
+
+def test_leaf_size_change_rebuilds_resident_trees():
+    """A new LBVH leaf size rebuilds the resident LBVH scenes' trees (the autotuner's leaf trials): the
+    next passes still equal rendering each scene alone."""
+    big = scenes.config2()
+    lbvh = scenes.SyntheticScene(**{**big.__dict__, "spheres": big.spheres[:3000].copy(), "width": 160,
+                                    "height": 90, "max_bounces": 5, "spp": 3})
+    mix = [lbvh] + small_mix(2)
+    with Batch() as b:
+        ids = [b.add_synthetic(sc) for sc in mix]
+        for i, sc in zip(ids, mix):
+            b.set_spp(i, 3)
+        for leaf in (8, 24):
+            b.set_tuning(bvh_leaf_size=leaf)
+            assert b.tuning()["bvh_leaf_size"] == leaf
+            for i in ids:
+                b.reset(i)
+            b.run()
+            for i, sc in zip(ids, mix):
+                ref, _ = alone(sc, 3)
+                assert bit_mismatches(b.get_accumulation(i), ref) == 0, (leaf, sc.name)
