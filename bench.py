@@ -14,7 +14,9 @@ than L2, so every step streams its working set through HBM; no explicit flush.
 
 `--impl reference` times the reference's per-pixel path restated on the CPU
 (the oracle's literal-order build, OpenMP over all host cores) on a bounded
-sample of the same workload; the reference's own code cannot be built here.
+sample of the same workload: the reference's perPixel is device code only, so
+it has no CPU path of its own; its own CUDA kernel, built from its sources, is
+timed in the main line's ref_cuda_kernel.
 """
 from __future__ import annotations
 

@@ -1,9 +1,8 @@
 """ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU-baseline legs of bench.py, never by the product.  Parity unpinned: the
-reference has no golden vectors and cannot be compiled here (oracle.h says
-why).
+CPU-baseline legs of bench.py, never by the product.  Pinned to the
+reference's own kernel built from its sources (oracle.h says how).
 """
 from __future__ import annotations
 
