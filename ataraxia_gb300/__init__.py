@@ -368,6 +368,11 @@ class Renderer:
     def render_frames(self, spp: int = 1):
         N.check(N.lib().atx_render(self._h, spp))
 
+    def join(self):
+        """Orders the renderer's stream after every render so far (atx_join; with
+        FLAG_OVERLAP_RENDERS renders are not joined into it until then)."""
+        N.check(N.lib().atx_join(self._h))
+
     def synchronize(self):
         N.check(N.lib().atx_synchronize(self._h))
 

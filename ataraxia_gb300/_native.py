@@ -130,6 +130,7 @@ JOB_STATES = {0: "queued", 1: "active", 2: "done", 3: "cancelled", 4: "failed"}
 FLAG_NO_GRAPHS = 1
 FLAG_PROFILE_KERNELS = 2
 FLAG_HOST_EXECUTOR = 4
+FLAG_OVERLAP_RENDERS = 8
 
 assert C.sizeof(Settings) == 8 and C.sizeof(CameraDesc) == 36
 
@@ -157,6 +158,7 @@ SIGNATURES = {
     "atx_set_camera_matrices": (_ST, [_P, _P, _P, _P]),
     "atx_render": (_ST, [_P, _U32]),
     "atx_synchronize": (_ST, [_P]),
+    "atx_join": (_ST, [_P]),
     "atx_read_accumulation": (_ST, [_P, _P, _U64]),
     "atx_read_image": (_ST, [_P, _P, _U64]),
     "atx_device_buffers": (_ST, [_P, C.POINTER(_P), C.POINTER(_P)]),

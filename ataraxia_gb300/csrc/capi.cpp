@@ -167,6 +167,14 @@ ATX_API atx_status atx_render(atx_renderer* r, uint32_t spp)
     return guarded([&]() -> atx_status { NEED(r); return r->impl.render(spp); });
 }
 
+ATX_API atx_status atx_join(atx_renderer* r)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        return r->impl.join();
+    });
+}
+
 ATX_API atx_status atx_synchronize(atx_renderer* r)
 {
     return guarded([&]() -> atx_status { NEED(r); return r->impl.synchronize(); });

@@ -296,15 +296,16 @@ Renderer::~Renderer()
 {
     if (cudaSetDevice(cfg_.device) == cudaSuccess) {
         if (stream_) cudaStreamSynchronize(stream_);
-        for (int l = 1; l < kLanes; ++l)
+        for (int l = 0; l < kLanes; ++l)
             if (lane_stream_[l]) cudaStreamSynchronize(lane_stream_[l]);
         scene_ = SceneStore();
         for (WaveStore& w : wave_) w.buf.reset();
         if (fork_) cudaEventDestroy(fork_);
-        for (int l = 1; l < kLanes; ++l) {
+        for (int l = 0; l < kLanes; ++l) {
             if (join_[l]) cudaEventDestroy(join_[l]);
-            if (lane_stream_[l]) cudaStreamDestroy(lane_stream_[l]);
+            if (lane_stream_[l] && lane_stream_[l] != stream_) cudaStreamDestroy(lane_stream_[l]);
         }
+        if (time_stream_) cudaStreamDestroy(time_stream_);
         accum_.reset();
         image_.reset();
         totals_.reset();
@@ -332,11 +333,13 @@ atx_status Renderer::init()
         return fail(ATX_ERR_INVALID_ARG, "device %d out of range (%d visible)", cfg_.device, count);
     ATX_TRY(activate());
     ATX_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    overlap_ = (cfg_.flags & ATX_FLAG_OVERLAP_RENDERS) != 0;
     lane_stream_[0] = stream_;
-    for (int l = 1; l < kLanes; ++l) {
+    for (int l = overlap_ ? 0 : 1; l < kLanes; ++l) {
         ATX_CUDA(cudaStreamCreateWithFlags(&lane_stream_[l], cudaStreamNonBlocking));
         ATX_CUDA(cudaEventCreateWithFlags(&join_[l], cudaEventDisableTiming));
     }
+    if (overlap_) ATX_CUDA(cudaStreamCreateWithFlags(&time_stream_, cudaStreamNonBlocking));
     ATX_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
     ATX_CUDA(cudaEventCreate(&ev_start_));
     ATX_CUDA(cudaEventCreate(&ev_stop_));
@@ -355,6 +358,7 @@ atx_status Renderer::resize(uint32_t w, uint32_t h)
     if ((uint64_t)w * h > 0xffffffffull) return fail(ATX_ERR_INVALID_ARG, "resize: more than 2^32 pixels");
     if (w == width_ && h == height_ && accum_.get()) return ATX_OK;  // Renderer.cu:100-101
     ATX_TRY(activate());
+    ATX_TRY(join());
     ATX_CUDA(cudaStreamSynchronize(stream_));
     const uint64_t px = (uint64_t)w * h;
     accum_.reset();
@@ -372,6 +376,7 @@ atx_status Renderer::set_scene(const atx_sphere* s, uint32_t n, const atx_materi
                                const atx_light* l, uint32_t nl)
 {
     ATX_TRY(activate());
+    ATX_TRY(join());
     ATX_CUDA(cudaStreamSynchronize(stream_));
     shape_valid_ = false;
     masks_valid_ = false;
@@ -417,6 +422,7 @@ atx_status Renderer::refresh_dirs()
         const uint64_t px = (uint64_t)camv_.width * camv_.height;
         ATX_TRY(dirs_.ensure(px * sizeof(float4), &budget_, "primary directions"));
         ATX_CUDA(enqueue_dir_table(camv_, dirs_.as<float4>(), stream_));
+        stream_dirty_ = true;
         dirs_cam_ = camv_;
         dirs_valid_ = true;
     }
@@ -457,6 +463,7 @@ atx_status Renderer::refresh_masks()
             ATX_CUDA(cudaStreamSynchronize(stream_));
             ATX_TRY(tile_lists_.ensure((uint64_t)(n ? n : 1u) * sizeof(uint32_t), &budget_, "primary tile lists"));
             ATX_CUDA(enqueue_tile_list_fill(sc, camv_, info, tile_lists_.as<uint32_t>(), stream_));
+            stream_dirty_ = true;
             masks_cam_ = camv_;
             masks_valid_ = true;
         }
@@ -469,11 +476,44 @@ atx_status Renderer::refresh_masks()
     if (!same) {
         ATX_TRY(masks_.ensure(tiles * words * sizeof(uint32_t), &budget_, "primary tile masks"));
         ATX_CUDA(enqueue_tile_masks(sc, camv_, masks_.as<uint32_t>(), stream_));
+        stream_dirty_ = true;
         masks_cam_ = camv_;
         masks_valid_ = true;
     }
     camv_.masks = masks_.as<uint32_t>();
     camv_.mask_words = words;
+    return ATX_OK;
+}
+
+// Whether render() would put no work on stream_ for the per-camera tables:
+// the directions are those of the current matrices and viewport, and the
+// primary tile masks or lists (where the scene has them) those of the
+// current camera, eye and scene.
+bool Renderer::tables_current() const
+{
+    auto same_view = [](const CameraView& a, const CameraView& b) {
+        return a.width == b.width && a.height == b.height &&
+               std::memcmp(a.inv_proj, b.inv_proj, sizeof(a.inv_proj)) == 0 &&
+               std::memcmp(a.inv_view, b.inv_view, sizeof(a.inv_view)) == 0 &&
+               std::memcmp(a.pos, b.pos, sizeof(a.pos)) == 0;
+    };
+    const bool dirs = dirs_valid_ && dirs_cam_.width == camv_.width && dirs_cam_.height == camv_.height &&
+                      std::memcmp(dirs_cam_.inv_proj, camv_.inv_proj, sizeof(camv_.inv_proj)) == 0 &&
+                      std::memcmp(dirs_cam_.inv_view, camv_.inv_view, sizeof(camv_.inv_view)) == 0;
+    if (!dirs) return false;
+    const SceneView& sc = scene_.view;
+    const bool has_tables = sc.use_bvh ? (sc.bvh.n_leaves >= 2 && sc.bvh.n_leaves > sc.bvh.leaf_size)
+                                       : (sc.n_sph >= 1 && sc.n_sph <= kTileMaskMaxSpheres);
+    return !has_tables || (masks_valid_ && same_view(masks_cam_, camv_));
+}
+
+atx_status Renderer::join()
+{
+    if (!joins_pending_) return ATX_OK;
+    ATX_TRY(activate());
+    for (uint32_t l = 0; l < pending_lanes_; ++l) ATX_CUDA(cudaStreamWaitEvent(stream_, join_[l], 0));
+    joins_pending_ = false;
+    stream_dirty_ = true;   // what follows on stream_ comes before the next render's lanes
     return ATX_OK;
 }
 
@@ -507,19 +547,25 @@ atx_status Renderer::render(uint32_t spp)
     ATX_TRY(refresh_camera());
     ATX_TRY(ensure_shape());
     // One wave per lane when it fits: fewer, fuller kernels (the state is
-    // allocated for this launch's paths, rounded up to 1 Mi, and kept).  All
-    // lanes unless the caller fixed the wave size, kernels are being timed
-    // one by one, or the launch is too small to fill them.  Scenes with light
-    // and direction buffers run their late bounces in one persistent launch
-    // and overlap best on two lanes (medium scene: 2 lanes +4% over 4); LBVH
-    // scenes use all four (large scene: 4 lanes +11% over 2).
+    // allocated for this launch's paths, rounded up to 1 Mi, and kept).  Up
+    // to the lane count for the scene (at least 4 Mi paths each), one lane
+    // when the caller fixed the wave size or kernels are being timed one by
+    // one.  Scenes with light and direction buffers run their late bounces in
+    // one persistent launch and, with each render joined, overlap best on two
+    // lanes; LBVH scenes, and every scene with overlapped renders (whose lanes
+    // run on from one render into the next), use four (large scene: 4 lanes
+    // +11% over 2; medium scene overlapped: 4 lanes +12% over 2).
     const uint64_t px = (uint64_t)width_ * height_;
     const bool profile = (cfg_.flags & ATX_FLAG_PROFILE_KERNELS) != 0;
-    uint32_t max_lanes = (!scene_.view.use_bvh && scene_.view.lb.n_lights) ? kBufferedLanes : kLanes;
+    uint32_t max_lanes = (!overlap_ && !scene_.view.use_bvh && scene_.view.lb.n_lights) ? kBufferedLanes
+                                                                                         : kDefaultLanes;
     if (tune_.lanes) max_lanes = std::min<uint32_t>(tune_.lanes, kLanes);
     const uint32_t wave_paths = tune_.wave_paths ? tune_.wave_paths : cfg_.wave_paths;
-    const uint32_t lanes = ((cfg_.wave_paths && !tune_.lanes) || profile || px < (uint64_t)max_lanes ||
-                            px * spp < (4ull << 20) * max_lanes) ? 1u : max_lanes;
+    // at least 4 Mi paths per lane
+    const uint64_t fill = std::max<uint64_t>(1, px * spp / (4ull << 20));
+    const uint32_t lanes = ((cfg_.wave_paths && !tune_.lanes) || profile)
+                               ? 1u
+                               : (uint32_t)std::min<uint64_t>({(uint64_t)max_lanes, fill, px});
     const uint64_t lane_px = (px + lanes - 1) / lanes;
     uint32_t capacity = wave_paths;
     if (!capacity) {
@@ -528,6 +574,17 @@ atx_status Renderer::render(uint32_t spp)
         capacity = (uint32_t)std::min<uint64_t>(want, kDefaultWavePaths);
     }
     const int32_t bounces = settings_.max_bounces;
+    if (!settings_.accumulation) frame_ = 1;
+    const uint32_t f0 = frame_;
+    // overlapped renders: the lanes of earlier renders must be done before
+    // this one puts work on stream_ (a clear, camera tables) or moves pixels
+    // to another lane, and before a lane's path state is reallocated
+    if (overlap_ && joins_pending_) {
+        bool grow = false;
+        for (uint32_t l = 0; l < lanes; ++l)
+            grow = grow || wave_[l].view.capacity < capacity || wave_[l].bounces < (uint32_t)std::max(bounces, 0);
+        if (f0 == 1 || !tables_current() || lanes != last_lanes_ || lane_px != last_lane_px_ || grow) ATX_TRY(join());
+    }
     for (uint32_t l = 0; l < lanes; ++l) {
         ATX_TRY(wave_[l].ensure(capacity, bounces > 0 ? (uint32_t)bounces : 0u, &budget_));
         wave_[l].view.totals = totals_.as<unsigned long long>();
@@ -535,34 +592,50 @@ atx_status Renderer::render(uint32_t spp)
     ATX_TRY(refresh_dirs());
     ATX_TRY(refresh_masks());
 
-    if (!settings_.accumulation) frame_ = 1;
-    const uint32_t f0 = frame_;
     uint32_t launches = 0;
     KernelTimer* timer = profile ? &timer_ : nullptr;
-    ATX_CUDA(cudaEventRecord(ev_start_, stream_));
+    if (!overlap_) ATX_CUDA(cudaEventRecord(ev_start_, stream_));
     if (f0 == 1) {  // Renderer.cu:181-182
         if (timer) timer->begin(kFamOther, stream_);
         ATX_CUDA(enqueue_clear_accum(accum_.as<float4>(), px, stream_));
         if (timer) timer->end(kFamOther, stream_);
         ++launches;
+        stream_dirty_ = true;
     }
     uint64_t primary_rays = 0;
     const int32_t sky = settings_.sky_light ? 1 : 0;
-    if (lanes > 1) {
+    if (!overlap_ && lanes > 1) {
         ATX_CUDA(cudaEventRecord(fork_, stream_));
         for (uint32_t l = 1; l < lanes; ++l) ATX_CUDA(cudaStreamWaitEvent(lane_stream_[l], fork_, 0));
+    } else if (overlap_ && stream_dirty_) {
+        ATX_CUDA(cudaEventRecord(fork_, stream_));
+        for (uint32_t l = 0; l < lanes; ++l) ATX_CUDA(cudaStreamWaitEvent(lane_stream_[l], fork_, 0));
+        stream_dirty_ = false;
     }
+    if (overlap_) ATX_CUDA(cudaEventRecord(ev_start_, lane_stream_[0]));
     for (uint32_t l = 0; l < lanes; ++l) {
         const uint64_t b = std::min(px, l * lane_px), e = std::min(px, (l + 1) * lane_px);
         ATX_TRY(enqueue_frames(scene_.view, camv_, wave_[l], shape_, f0, spp, bounces, sky, accum_.as<float4>(),
                                image_.as<uint32_t>(), capacity, lane_stream_[l], &launches, l == 0 ? timer : nullptr,
                                &primary_rays, b, e, nullptr, false, tune_.wave_spp));
     }
-    for (uint32_t l = 1; l < lanes; ++l) {
-        ATX_CUDA(cudaEventRecord(join_[l], lane_stream_[l]));
-        ATX_CUDA(cudaStreamWaitEvent(stream_, join_[l], 0));
+    if (overlap_) {
+        for (uint32_t l = 0; l < lanes; ++l) {
+            ATX_CUDA(cudaEventRecord(join_[l], lane_stream_[l]));
+            ATX_CUDA(cudaStreamWaitEvent(time_stream_, join_[l], 0));
+        }
+        ATX_CUDA(cudaEventRecord(ev_stop_, time_stream_));
+        joins_pending_ = true;
+        pending_lanes_ = lanes;
+        last_lanes_ = lanes;
+        last_lane_px_ = lane_px;
+    } else {
+        for (uint32_t l = 1; l < lanes; ++l) {
+            ATX_CUDA(cudaEventRecord(join_[l], lane_stream_[l]));
+            ATX_CUDA(cudaStreamWaitEvent(stream_, join_[l], 0));
+        }
+        ATX_CUDA(cudaEventRecord(ev_stop_, stream_));
     }
-    ATX_CUDA(cudaEventRecord(ev_stop_, stream_));
     timed_ = true;
     frame_ = settings_.accumulation ? f0 + spp : 1u;  // Renderer.cu:245-248
     st_.frames += spp;
@@ -575,6 +648,7 @@ atx_status Renderer::render(uint32_t spp)
 atx_status Renderer::synchronize()
 {
     ATX_TRY(activate());
+    ATX_TRY(join());
     ATX_CUDA(cudaStreamSynchronize(stream_));
     return ATX_OK;
 }
@@ -585,6 +659,7 @@ atx_status Renderer::read_accumulation(float* host, uint64_t n)
     if (n > (uint64_t)width_ * height_) return fail(ATX_ERR_INVALID_ARG, "read_accumulation: %llu pixels > image",
                                                     (unsigned long long)n);
     ATX_TRY(activate());
+    ATX_TRY(join());
     ATX_CUDA(cudaMemcpyAsync(host, accum_.get(), n * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
     ATX_CUDA(cudaStreamSynchronize(stream_));
     return ATX_OK;
@@ -596,6 +671,7 @@ atx_status Renderer::read_image(uint32_t* host, uint64_t n)
     if (n > (uint64_t)width_ * height_) return fail(ATX_ERR_INVALID_ARG, "read_image: %llu pixels > image",
                                                     (unsigned long long)n);
     ATX_TRY(activate());
+    ATX_TRY(join());
     ATX_CUDA(cudaMemcpyAsync(host, image_.get(), n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
     ATX_CUDA(cudaStreamSynchronize(stream_));
     return ATX_OK;
@@ -603,6 +679,7 @@ atx_status Renderer::read_image(uint32_t* host, uint64_t n)
 
 atx_status Renderer::device_buffers(void** accum, void** image)
 {
+    ATX_TRY(join());
     if (accum) *accum = accum_.get();
     if (image) *image = image_.get();
     return ATX_OK;
@@ -611,6 +688,7 @@ atx_status Renderer::device_buffers(void** accum, void** image)
 atx_status Renderer::stats(atx_stats* out)
 {
     ATX_TRY(activate());
+    ATX_TRY(join());
     ATX_CUDA(cudaStreamSynchronize(stream_));
     unsigned long long dev[3] = {0, 0, 0};
     ATX_CUDA(cudaMemcpy(dev, totals_.get(), sizeof(dev), cudaMemcpyDeviceToHost));
@@ -675,8 +753,9 @@ atx_status Renderer::set_tuning(const atx_tuning& t)
         return fail(ATX_ERR_INVALID_ARG, "tuning: threads must be a multiple of 32 up to 256");
     if (t.bvh_leaf_size > 64u) return fail(ATX_ERR_INVALID_ARG, "tuning: leaf size above 64");
     ATX_TRY(activate());
+    ATX_TRY(join());
     ATX_CUDA(cudaStreamSynchronize(stream_));
-    for (int l = 1; l < kLanes; ++l)
+    for (int l = 0; l < kLanes; ++l)
         if (lane_stream_[l]) ATX_CUDA(cudaStreamSynchronize(lane_stream_[l]));
     if (t.bvh_leaf_size != tune_.bvh_leaf_size && scene_.view.use_bvh) {
         ATX_TRY(scene_.rebuild_bvh(t.bvh_leaf_size, stream_));
@@ -770,7 +849,7 @@ atx_status Renderer::autotune(uint32_t spp, uint32_t passes, bool use_cache, atx
             t.bvh_leaf_size = leaf;
             ATX_TRY(trial(t));
         }
-    for (uint32_t lanes : {1u, 2u, 4u}) {
+    for (uint32_t lanes : {1u, 2u, 4u, 6u, 8u}) {
         atx_tuning t = best;
         t.lanes = lanes;
         ATX_TRY(trial(t));
@@ -806,6 +885,7 @@ atx_status Renderer::trace_nearest(const float* o, const float* d, uint64_t n, f
     if (n == 0) return ATX_OK;
     if (!o || !d || !t || !id) return fail(ATX_ERR_INVALID_ARG, "trace_nearest: null array");
     ATX_TRY(activate());
+    ATX_TRY(join());
     DeviceBuffer buf;
     ATX_TRY(buf.ensure(n * 8 * sizeof(float) + 1024, &budget_, "trace scratch"));
     float* dorg = buf.as<float>();
@@ -827,6 +907,7 @@ atx_status Renderer::primary_directions(float* host, uint64_t n)
     const uint64_t px = (uint64_t)width_ * height_;
     if (!host || n < px) return fail(ATX_ERR_INVALID_ARG, "primary_directions: buffer smaller than W*H");
     ATX_TRY(activate());
+    ATX_TRY(join());
     ATX_TRY(refresh_camera());
     DeviceBuffer buf;
     ATX_TRY(buf.ensure(px * 3 * sizeof(float), &budget_, "direction scratch"));

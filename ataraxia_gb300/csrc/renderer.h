@@ -100,6 +100,10 @@ public:
     atx_status set_camera_matrices(const float inv_view[16], const float inv_proj[16], const float pos[3]);
     atx_status render(uint32_t spp);
     atx_status synchronize();
+    // Makes the renderer's stream wait for every render enqueued so far (with
+    // ATX_FLAG_OVERLAP_RENDERS the lanes of a render are not joined into it
+    // until then; otherwise a no-op).
+    atx_status join();
     atx_status read_accumulation(float* host, uint64_t n);
     atx_status read_image(uint32_t* host, uint64_t n);
     atx_status device_buffers(void** accum, void** image);
@@ -145,11 +149,25 @@ private:
     // many streams with their own path state, so one range's last, sparse
     // bounces overlap the others' work instead of leaving SMs idle.  Lane 0
     // is the renderer's stream.
-    static constexpr int kLanes = 4;
-    static constexpr int kBufferedLanes = 2;   // lanes for scenes with light and direction buffers
+    static constexpr int kLanes = 8;
+    static constexpr int kDefaultLanes = 4;    // LBVH scenes, and any scene with overlapped renders
+    static constexpr int kBufferedLanes = 2;   // scenes with light and direction buffers, renders joined
     WaveStore wave_[kLanes];
     cudaStream_t lane_stream_[kLanes] = {};
     cudaEvent_t fork_ = nullptr, join_[kLanes] = {};
+    // ATX_FLAG_OVERLAP_RENDERS: lane 0 is a stream of its own too, and a
+    // render's lanes are joined into stream_ only by join(); the next render's
+    // lanes then continue on their own streams (same pixel range per lane, so
+    // each pixel's frames stay in order) and wait for stream_ only after work
+    // was put on it (stream_dirty_) or the lane split changed.
+    bool overlap_ = false;
+    bool joins_pending_ = false;
+    bool stream_dirty_ = true;
+    uint32_t pending_lanes_ = 0;
+    uint32_t last_lanes_ = 0;
+    uint64_t last_lane_px_ = 0;
+    cudaStream_t time_stream_ = nullptr;   // records the end of a render after all its lanes
+    bool tables_current() const;
     DeviceBuffer accum_, image_, totals_;
     // Primary directions for the camera they were computed for (dirs_cam_):
     // rebuilt when the camera's matrices or the viewport change.

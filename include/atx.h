@@ -108,6 +108,15 @@ typedef struct atx_config {
 #define ATX_FLAG_NO_GRAPHS 1u       /* launch kernels directly instead of replaying a CUDA graph */
 #define ATX_FLAG_PROFILE_KERNELS 2u /* record CUDA events around every kernel (atx_get_kernel_times) */
 #define ATX_FLAG_HOST_EXECUTOR 4u   /* server only: simulate the GPU on the host (scheduling tests, no device) */
+/* Consecutive atx_render calls may overlap on the GPU: a render's lanes are
+ * not joined into the renderer's stream at its end, so the next render's
+ * lanes start while the last, sparse bounces of the previous one finish
+ * (each lane keeps its pixel range, so every pixel's frames stay in order).
+ * The library's own calls (reads, atx_synchronize, stats, scene, camera-table
+ * and size changes) join first; a caller that orders its own work on
+ * atx_get_stream's stream, or uses atx_device_buffers' pointers, calls
+ * atx_join (or atx_synchronize) first.  Results are unchanged. */
+#define ATX_FLAG_OVERLAP_RENDERS 8u
 
 typedef struct atx_stats {
     uint64_t frames;           /* reference frames rendered (samples per pixel) since creation */
@@ -177,6 +186,11 @@ ATX_API atx_status atx_set_camera_matrices(atx_renderer* r, const float inv_view
  * packed for the last frame (Renderer.cu:166-168).  Asynchronous. */
 ATX_API atx_status atx_render(atx_renderer* r, uint32_t spp);
 ATX_API atx_status atx_synchronize(atx_renderer* r);
+/* Makes the renderer's stream wait for every render enqueued so far, without
+ * blocking the host (needed only with ATX_FLAG_OVERLAP_RENDERS; otherwise a
+ * no-op).  No counterpart in the reference, whose Render() synchronises the
+ * device every frame (Renderer.cu:233). */
+ATX_API atx_status atx_join(atx_renderer* r);
 
 /* Reads n_pixels float4 of the accumulator (sum of (r, g, b, 1) per frame). */
 ATX_API atx_status atx_read_accumulation(atx_renderer* r, float* host_rgba, uint64_t n_pixels);
