@@ -368,6 +368,18 @@ class Renderer:
     def render_frames(self, spp: int = 1):
         N.check(N.lib().atx_render(self._h, spp))
 
+    def read_image_async(self, out: np.ndarray) -> int:
+        """Starts reading the last render's RGBA8 image into out (contiguous uint32, W*H; best page-locked)
+        and returns a ticket for wait_read (atx_read_image_async); out must not be used before."""
+        if out.dtype != np.uint32 or not out.flags.c_contiguous or out.size != self.width * self.height:
+            raise ValueError("read_image_async: out must be a contiguous uint32 array of width*height pixels")
+        t = C.c_uint64()
+        N.check(N.lib().atx_read_image_async(self._h, N.ptr(out), out.size, C.byref(t)))
+        return t.value
+
+    def wait_read(self, ticket: int):
+        N.check(N.lib().atx_wait_read(self._h, ticket))
+
     def join(self):
         """Orders the renderer's stream after every render so far (atx_join; with
         FLAG_OVERLAP_RENDERS renders are not joined into it until then)."""

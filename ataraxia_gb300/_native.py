@@ -159,6 +159,8 @@ SIGNATURES = {
     "atx_render": (_ST, [_P, _U32]),
     "atx_synchronize": (_ST, [_P]),
     "atx_join": (_ST, [_P]),
+    "atx_read_image_async": (_ST, [_P, _P, _U64, C.POINTER(_U64)]),
+    "atx_wait_read": (_ST, [_P, _U64]),
     "atx_read_accumulation": (_ST, [_P, _P, _U64]),
     "atx_read_image": (_ST, [_P, _P, _U64]),
     "atx_device_buffers": (_ST, [_P, C.POINTER(_P), C.POINTER(_P)]),

@@ -167,6 +167,22 @@ ATX_API atx_status atx_render(atx_renderer* r, uint32_t spp)
     return guarded([&]() -> atx_status { NEED(r); return r->impl.render(spp); });
 }
 
+ATX_API atx_status atx_read_image_async(atx_renderer* r, uint32_t* host_rgba8, uint64_t n_pixels, uint64_t* ticket)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        return r->impl.read_image_async(host_rgba8, n_pixels, ticket);
+    });
+}
+
+ATX_API atx_status atx_wait_read(atx_renderer* r, uint64_t ticket)
+{
+    return guarded([&]() -> atx_status {
+        NEED(r);
+        return r->impl.wait_read(ticket);
+    });
+}
+
 ATX_API atx_status atx_join(atx_renderer* r)
 {
     return guarded([&]() -> atx_status {

@@ -306,8 +306,16 @@ Renderer::~Renderer()
             if (lane_stream_[l] && lane_stream_[l] != stream_) cudaStreamDestroy(lane_stream_[l]);
         }
         if (time_stream_) cudaStreamDestroy(time_stream_);
+        if (copy_stream_) cudaStreamSynchronize(copy_stream_);
         accum_.reset();
         image_.reset();
+        image_alt_.reset();
+        for (cudaEvent_t& e : read_done_)
+            if (e) cudaEventDestroy(e);
+        for (cudaEvent_t& e : ticket_ev_)
+            if (e) cudaEventDestroy(e);
+        if (src_ready_) cudaEventDestroy(src_ready_);
+        if (copy_stream_) cudaStreamDestroy(copy_stream_);
         totals_.reset();
         if (ev_start_) cudaEventDestroy(ev_start_);
         if (ev_stop_) cudaEventDestroy(ev_stop_);
@@ -340,6 +348,10 @@ atx_status Renderer::init()
         ATX_CUDA(cudaEventCreateWithFlags(&join_[l], cudaEventDisableTiming));
     }
     if (overlap_) ATX_CUDA(cudaStreamCreateWithFlags(&time_stream_, cudaStreamNonBlocking));
+    ATX_CUDA(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : read_done_) ATX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (cudaEvent_t& e : ticket_ev_) ATX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ATX_CUDA(cudaEventCreateWithFlags(&src_ready_, cudaEventDisableTiming));
     ATX_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
     ATX_CUDA(cudaEventCreate(&ev_start_));
     ATX_CUDA(cudaEventCreate(&ev_stop_));
@@ -360,11 +372,16 @@ atx_status Renderer::resize(uint32_t w, uint32_t h)
     ATX_TRY(activate());
     ATX_TRY(join());
     ATX_CUDA(cudaStreamSynchronize(stream_));
+    ATX_CUDA(cudaStreamSynchronize(copy_stream_));
+    read_pending_[0] = read_pending_[1] = false;
     const uint64_t px = (uint64_t)w * h;
     accum_.reset();
     image_.reset();
+    image_alt_.reset();
     ATX_TRY(accum_.ensure(px * sizeof(float4), &budget_, "accumulation buffer"));
     ATX_TRY(image_.ensure(px * sizeof(uint32_t), &budget_, "image buffer"));
+    if (overlap_) ATX_TRY(image_alt_.ensure(px * sizeof(uint32_t), &budget_, "second image buffer"));
+    img_last_ = img_next_ = 0;
     width_ = w;
     height_ = h;
     frame_ = 1;  // Renderer.cu:145
@@ -604,6 +621,16 @@ atx_status Renderer::render(uint32_t spp)
     }
     uint64_t primary_rays = 0;
     const int32_t sky = settings_.sky_light ? 1 : 0;
+    // the image buffer this render packs; an asynchronous read of its previous
+    // contents must have landed first
+    const int ib = overlap_ ? img_next_ : 0;
+    if (read_pending_[ib]) {
+        if (overlap_)
+            for (uint32_t l = 0; l < lanes; ++l) ATX_CUDA(cudaStreamWaitEvent(lane_stream_[l], read_done_[ib], 0));
+        else
+            ATX_CUDA(cudaStreamWaitEvent(stream_, read_done_[ib], 0));
+        read_pending_[ib] = false;
+    }
     if (!overlap_ && lanes > 1) {
         ATX_CUDA(cudaEventRecord(fork_, stream_));
         for (uint32_t l = 1; l < lanes; ++l) ATX_CUDA(cudaStreamWaitEvent(lane_stream_[l], fork_, 0));
@@ -616,7 +643,7 @@ atx_status Renderer::render(uint32_t spp)
     for (uint32_t l = 0; l < lanes; ++l) {
         const uint64_t b = std::min(px, l * lane_px), e = std::min(px, (l + 1) * lane_px);
         ATX_TRY(enqueue_frames(scene_.view, camv_, wave_[l], shape_, f0, spp, bounces, sky, accum_.as<float4>(),
-                               image_.as<uint32_t>(), capacity, lane_stream_[l], &launches, l == 0 ? timer : nullptr,
+                               image_buf(ib), capacity, lane_stream_[l], &launches, l == 0 ? timer : nullptr,
                                &primary_rays, b, e, nullptr, false, tune_.wave_spp));
     }
     if (overlap_) {
@@ -637,6 +664,8 @@ atx_status Renderer::render(uint32_t spp)
         ATX_CUDA(cudaEventRecord(ev_stop_, stream_));
     }
     timed_ = true;
+    img_last_ = ib;
+    img_next_ = overlap_ ? 1 - ib : 0;
     frame_ = settings_.accumulation ? f0 + spp : 1u;  // Renderer.cu:245-248
     st_.frames += spp;
     st_.paths += (uint64_t)width_ * height_ * spp;
@@ -672,8 +701,44 @@ atx_status Renderer::read_image(uint32_t* host, uint64_t n)
                                                     (unsigned long long)n);
     ATX_TRY(activate());
     ATX_TRY(join());
-    ATX_CUDA(cudaMemcpyAsync(host, image_.get(), n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+    ATX_CUDA(cudaMemcpyAsync(host, image_buf(img_last_), n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
     ATX_CUDA(cudaStreamSynchronize(stream_));
+    return ATX_OK;
+}
+
+atx_status Renderer::read_image_async(uint32_t* host, uint64_t n, uint64_t* ticket)
+{
+    if (!host || !ticket) return fail(ATX_ERR_INVALID_ARG, "read_image_async: null pointer");
+    if (n > (uint64_t)width_ * height_) return fail(ATX_ERR_INVALID_ARG, "read_image_async: %llu pixels > image",
+                                                    (unsigned long long)n);
+    ATX_TRY(activate());
+    // after the last render's lanes (without joining them into stream_), or
+    // after stream_'s work when renders are joined
+    if (overlap_ && joins_pending_) {
+        for (uint32_t l = 0; l < pending_lanes_; ++l) ATX_CUDA(cudaStreamWaitEvent(copy_stream_, join_[l], 0));
+    } else {
+        ATX_CUDA(cudaEventRecord(src_ready_, stream_));
+        ATX_CUDA(cudaStreamWaitEvent(copy_stream_, src_ready_, 0));
+    }
+    ATX_CUDA(cudaMemcpyAsync(host, image_buf(img_last_), n * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                             copy_stream_));
+    ATX_CUDA(cudaEventRecord(read_done_[img_last_], copy_stream_));
+    read_pending_[img_last_] = true;
+    const int slot = (int)(tickets_ % kTickets);
+    if (tickets_ >= (uint64_t)kTickets) ATX_CUDA(cudaEventSynchronize(ticket_ev_[slot]));   // the ticket it replaces
+    ATX_CUDA(cudaEventRecord(ticket_ev_[slot], copy_stream_));
+    *ticket = tickets_++;
+    return ATX_OK;
+}
+
+atx_status Renderer::wait_read(uint64_t ticket)
+{
+    if (ticket >= tickets_) return fail(ATX_ERR_INVALID_ARG, "wait_read: unknown ticket %llu",
+                                        (unsigned long long)ticket);
+    // a ticket whose slot was reused was waited for when it was
+    if (ticket + kTickets < tickets_) return ATX_OK;
+    ATX_TRY(activate());
+    ATX_CUDA(cudaEventSynchronize(ticket_ev_[ticket % kTickets]));
     return ATX_OK;
 }
 
@@ -681,7 +746,7 @@ atx_status Renderer::device_buffers(void** accum, void** image)
 {
     ATX_TRY(join());
     if (accum) *accum = accum_.get();
-    if (image) *image = image_.get();
+    if (image) *image = image_buf(img_last_);
     return ATX_OK;
 }
 

@@ -106,6 +106,10 @@ public:
     atx_status join();
     atx_status read_accumulation(float* host, uint64_t n);
     atx_status read_image(uint32_t* host, uint64_t n);
+    // Starts copying the last render's RGBA8 image into host memory on a copy
+    // stream and returns at once; wait_read(ticket) blocks until it landed.
+    atx_status read_image_async(uint32_t* host, uint64_t n, uint64_t* ticket);
+    atx_status wait_read(uint64_t ticket);
     atx_status device_buffers(void** accum, void** image);
     atx_status stats(atx_stats* out);
     atx_status trace_nearest(const float* o, const float* d, uint64_t n, float* t, int32_t* id);
@@ -169,6 +173,20 @@ private:
     cudaStream_t time_stream_ = nullptr;   // records the end of a render after all its lanes
     bool tables_current() const;
     DeviceBuffer accum_, image_, totals_;
+    // With overlapped renders, renders alternate between image_ and
+    // image_alt_, so an asynchronous read of one render's image runs while
+    // the next render packs the other; a render waits only for the last read
+    // of the buffer it is about to overwrite.
+    DeviceBuffer image_alt_;
+    int img_last_ = 0, img_next_ = 0;
+    cudaStream_t copy_stream_ = nullptr;
+    cudaEvent_t read_done_[2] = {};
+    bool read_pending_[2] = {false, false};
+    cudaEvent_t src_ready_ = nullptr;
+    static constexpr int kTickets = 8;
+    cudaEvent_t ticket_ev_[kTickets] = {};
+    uint64_t tickets_ = 0;
+    uint32_t* image_buf(int i) { return (i ? image_alt_ : image_).as<uint32_t>(); }
     // Primary directions for the camera they were computed for (dirs_cam_):
     // rebuilt when the camera's matrices or the viewport change.
     DeviceBuffer dirs_;

@@ -197,7 +197,19 @@ ATX_API atx_status atx_read_accumulation(atx_renderer* r, float* host_rgba, uint
 /* Reads the RGBA8 image (Renderer::getImage, Renderer.h:26; the reference
  * copies it to the host every frame, Renderer.cu:240). */
 ATX_API atx_status atx_read_image(atx_renderer* r, uint32_t* host_rgba8, uint64_t n_pixels);
-/* Device pointers of the accumulator (float4) and image (uint32) for zero-copy consumers. */
+/* Starts reading the last render's RGBA8 image into host memory (best
+ * page-locked: atx_host_alloc) on the renderer's copy stream and returns at
+ * once with a ticket; atx_wait_read(r, ticket) blocks until the pixels have
+ * landed, and the host buffer must not be used before.  With
+ * ATX_FLAG_OVERLAP_RENDERS, renders alternate between two device images, so
+ * the next render runs while the read is in flight (a render waits only for
+ * the last read of the image it is about to overwrite).  No counterpart in
+ * the reference, whose Render() copies the image synchronously every frame
+ * (Renderer.cu:240). */
+ATX_API atx_status atx_read_image_async(atx_renderer* r, uint32_t* host_rgba8, uint64_t n_pixels, uint64_t* ticket);
+ATX_API atx_status atx_wait_read(atx_renderer* r, uint64_t ticket);
+/* Device pointers of the accumulator (float4) and of the last render's image
+ * (uint32) for zero-copy consumers. */
 ATX_API atx_status atx_device_buffers(atx_renderer* r, void** accumulation, void** image);
 
 ATX_API atx_status atx_get_stats(const atx_renderer* r, atx_stats* stats);

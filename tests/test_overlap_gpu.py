@@ -77,3 +77,35 @@ def test_overlapped_accumulation_off_resize_and_join():
             x.render_frames(16)
         assert bit_mismatches(r.get_accumulation().reshape(-1, 4), ref.get_accumulation().reshape(-1, 4)) == 0
         assert np.array_equal(r.get_image(), ref.get_image())
+
+
+@pytest.mark.parametrize("flags", [0, N.FLAG_OVERLAP_RENDERS])
+def test_async_image_reads_double_buffered(flags):
+    """atx_read_image_async after every render into two alternating host buffers, each waited for one
+    render later (while the next render runs): every image equals a synchronous read of the joined
+    renderer after the same render."""
+    sc = scenes.config1().with_resolution(1280, 720)
+    want = []
+    with Renderer() as ref:
+        _setup(ref, sc)
+        for k in range(6):
+            ref.render_frames(16 if k % 3 else 8)
+            want.append(ref.get_image().reshape(-1).copy())
+    got = []
+    with Renderer(flags=flags) as r:
+        _setup(r, sc)
+        bufs = [np.zeros(sc.width * sc.height, np.uint32) for _ in range(2)]
+        tickets = []
+        for k in range(6):
+            r.render_frames(16 if k % 3 else 8)
+            tickets.append(r.read_image_async(bufs[k % 2]))
+            if k >= 1:
+                r.wait_read(tickets[k - 1])
+                got.append(bufs[(k - 1) % 2].copy())
+        r.wait_read(tickets[-1])
+        got.append(bufs[5 % 2].copy())
+        r.wait_read(tickets[0])                  # an old ticket: already landed
+        with pytest.raises(Exception):
+            r.wait_read(len(tickets))            # never issued
+    for a, b in zip(got, want):
+        assert np.array_equal(a, b)
