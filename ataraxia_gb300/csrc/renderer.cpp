@@ -551,7 +551,8 @@ atx_status Renderer::refresh_camera()
 atx_status Renderer::ensure_shape()
 {
     if (shape_valid_) return ATX_OK;
-    ATX_CUDA(plan_launch(scene_.view, cfg_.device, (int)(tune_.threads ? tune_.threads : cfg_.threads), &shape_));
+    ATX_CUDA(plan_launch(scene_.view, cfg_.device, (int)(tune_.threads ? tune_.threads : cfg_.threads), &shape_,
+                         (int)tune_.path_kernel));
     shape_valid_ = true;
     return ATX_OK;
 }
@@ -817,6 +818,7 @@ atx_status Renderer::set_tuning(const atx_tuning& t)
     if (t.threads && (t.threads % 32u || t.threads > 256u))
         return fail(ATX_ERR_INVALID_ARG, "tuning: threads must be a multiple of 32 up to 256");
     if (t.bvh_leaf_size > 64u) return fail(ATX_ERR_INVALID_ARG, "tuning: leaf size above 64");
+    if (t.path_kernel > 2u) return fail(ATX_ERR_INVALID_ARG, "tuning: path_kernel is 0, 1 or 2");
     ATX_TRY(activate());
     ATX_TRY(join());
     ATX_CUDA(cudaStreamSynchronize(stream_));
@@ -827,7 +829,7 @@ atx_status Renderer::set_tuning(const atx_tuning& t)
         masks_valid_ = false;       // the tile candidate lists walk the tree
         prev_cam_valid_ = false;
     }
-    if (t.threads != tune_.threads) shape_valid_ = false;
+    if (t.threads != tune_.threads || t.path_kernel != tune_.path_kernel) shape_valid_ = false;
     tune_ = t;
     tune_.from_cache = 0;
     tune_.ms = 0.0;
@@ -929,6 +931,12 @@ atx_status Renderer::autotune(uint32_t spp, uint32_t passes, bool use_cache, atx
         t.threads = threads;
         ATX_TRY(trial(t));
     }
+    if (!sv.use_bvh && sv.n_sph <= 256u)   // whole paths in one thread against the wavefront stages
+        for (uint32_t pk : {1u, 2u}) {
+            atx_tuning t = best;
+            t.path_kernel = pk;
+            ATX_TRY(trial(t));
+        }
     for (uint32_t wspp : {1u, 4u}) {
         if (wspp >= spp) continue;
         atx_tuning t = best;

@@ -51,6 +51,9 @@ constexpr int kPathsFrom = 2;
 
 // k_shadow's blocks per SM: the shared-memory variant fits 40 registers
 // without spilling (6 blocks of 256 threads); the others take up to 64 (4).
+// k_fused's blocks per SM (whole paths in one thread: 64 registers).
+constexpr int kFusedBlocksPerSm = 4;
+
 template <int IS>
 constexpr int kShadowBlocksPerSm = IS == kIsSmem ? 6 : 4;
 
@@ -906,6 +909,134 @@ __global__ void __launch_bounds__(kThreads) k_accumulate(WaveState ws, WaveJob j
     }
 }
 
+// Whole paths in one thread, for small scenes on the brute-force table
+// (Renderer.cu:150-171 and :287-387 in their own structure): one thread per
+// pixel of the wave traces the pixel's primary ray once (its samples share
+// it), then each sample's path through all its bounces, and adds the
+// samples to the accumulator in frame order.  A few spheres make every
+// nearest-hit and shadow test cheap, and nothing goes through memory between
+// bounces, where the wavefront kernels write and read the path state and pay
+// a launch per stage: for one or a few samples per pixel and call (the
+// reference's interactive loop renders one) this is faster; with many, the
+// wavefront's shared first-bounce work wins.  The bounce-0 light visibility
+// is kept per pixel (the samples share the primary hit, so a light's shadow
+// ray is the same for all of them).  Every float is computed by the
+// functions the wavefront kernels use, in the same order, so the results are
+// theirs bit for bit.
+template <int IS>
+__global__ void __launch_bounds__(kThreads, kFusedBlocksPerSm) k_fused(SceneView sc, CameraView cam, WaveState ws,
+                                                                        WaveJob job, float4* accum, uint32_t* image)
+{
+    constexpr bool SMEM = IS == kIsSmem;
+    extern __shared__ float4 s_sph[];
+    if (blockIdx.x * blockDim.x >= job.n_pixels) return;
+    if (SMEM) stage_spheres(sc, s_sph);
+    const float4* sph = SMEM ? s_sph : sc.sph;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const float fpack = __uint2float_rn(job.pack_frame);
+    const float3 o0 = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
+    const float3 sky = mk3(0.6f, 0.7f, 0.9f);
+    const bool cache_vis = sc.n_lights <= 32u;
+    uint32_t n_ext = 0u, n_sh = 0u, n_first = 0u;   // rays traced, for the renderer's statistics
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < job.n_pixels; j += stride) {
+        const uint32_t p = job.pixel0 + j;
+        const float3 d0 = primary_ray(cam, p);
+        float t0 = 0.0f;
+        int32_t h0 = -1;
+        if (job.max_bounces > 0) {
+            if (job.prim_cache && job.prim_cached) {
+                const uint2 pr = job.prim_cache[p];
+                t0 = __uint_as_float(pr.x);
+                h0 = (int32_t)pr.y;
+            } else {
+                h0 = scene_nearest<IS>(sc, sph, o0, d0, t0);
+                if (job.prim_cache) job.prim_cache[p] = make_uint2(__float_as_uint(t0), (uint32_t)h0);
+            }
+        }
+        float4 a = accum[p];
+        uint32_t known = 0u, seen = 0u;   // bounce-0 lights tested from this pixel's hit, and the visible ones
+        for (uint32_t s = 0; s < job.spp; ++s) {
+            float3 c = mk3(0.f, 0.f, 0.f);
+            float3 o = o0, d = d0, thr = mk3(1.f, 1.f, 1.f);
+            uint32_t seed = p * (job.frame0 + s);
+            for (int32_t i = 0; i < job.max_bounces; ++i) {   // Renderer.cu:304-385
+                seed += (uint32_t)i;
+                float tmin = t0;
+                int32_t hit = h0;
+                if (i > 0) {
+                    hit = scene_nearest<IS>(sc, sph, o, d, tmin);
+                    ++n_ext;
+                } else if (hit >= 0) {
+                    ++n_first;
+                }
+                if (hit < 0) {   // Renderer.cu:309-318
+                    if (job.sky) c = add3(c, mul3(sky, thr));
+                    break;
+                }
+                const float4 sp = table_sphere<SMEM>(sph, (uint32_t)hit);
+                float3 pos, nrm;
+                ray_hit(sp, o, d, tmin, pos, nrm);
+                const int32_t mi = __ldg(&sc.sph_mat[hit]);
+                const float4* mrow = reinterpret_cast<const float4*>(sc.mat + mi);
+                const float4 m0 = __ldg(mrow), m1 = __ldg(mrow + 1), m2 = __ldg(mrow + 2);
+                const float3 albedo = mk3(m0.x, m0.y, m0.z);
+                const float rough = m0.w;
+                const float metallic = m1.w;
+                if (m2.w > 0.0f) c = add3(c, mul3(mk3(m2.x, m2.y, m2.z), thr));   // Renderer.cu:329-333
+                const float3 base = add3(muls3(mk3(m1.x, m1.y, m1.z), 1.0f - metallic), muls3(albedo, metallic));
+                if (sc.n_lights > 0u) {   // Renderer.cu:338-369
+                    const uint32_t li = light_pick(sc, seed);
+                    float3 L;
+                    float dist2;
+                    const float4 l1 = light_dir(sc, li, pos, L, dist2);
+                    const float3 f = cook_torrance(albedo, base, metallic, rough, nrm, neg3(d), L);
+                    const float3 lc = mul3(mul3(mk3(l1.x, l1.y, l1.z), f), thr);
+                    bool lit;
+                    const uint32_t bit = 1u << (li & 31u);
+                    if (i == 0 && cache_vis && (known & bit)) {
+                        lit = (seen & bit) != 0u;
+                    } else {
+                        const float3 so = add3(pos, muls3(nrm, kOffset));
+                        lit = sc.n_sph == 0u || !scene_occluded<IS>(sc, sph, so, L, dist2);
+                        ++n_sh;
+                        if (i == 0 && cache_vis) {
+                            known |= bit;
+                            if (lit) seen |= bit;
+                        }
+                    }
+                    if (lit) c = add3(c, lc);
+                }
+                if (i + 1 >= job.max_bounces) break;   // Renderer.cu:371-384 change nothing after the last
+                thr = mul3(thr, albedo);
+                o = add3(pos, muls3(nrm, kOffset));
+                const float pr = gmax(0.1f, gmin(1.0f, length3(thr)));
+                if (pcg_float(seed) > pr) break;
+                thr = divs3(thr, pr);
+                d = (metallic > 0.0f) ? sample_ggx(nrm, rough, seed) : sample_cosine(nrm, seed);
+            }
+            a.x = a.x + c.x;
+            a.y = a.y + c.y;
+            a.z = a.z + c.z;
+            a.w = a.w + 1.0f;
+        }
+        accum[p] = a;
+        if (job.pack_frame) image[p] = pack_rgba8(a, fpack);
+    }
+    if (ws.totals) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            n_ext += __shfl_down_sync(kFull, n_ext, off);
+            n_sh += __shfl_down_sync(kFull, n_sh, off);
+            n_first += __shfl_down_sync(kFull, n_first, off);
+        }
+        if (lane_id() == 0u) {
+            if (n_ext) atomicAdd(&ws.totals[0], (unsigned long long)n_ext);
+            if (n_sh) atomicAdd(&ws.totals[1], (unsigned long long)n_sh);
+            if (n_first) atomicAdd(&ws.totals[2], (unsigned long long)n_first);
+        }
+    }
+}
+
 __global__ void k_clear(float4* p, uint64_t n)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -1177,7 +1308,7 @@ cudaError_t occupancy(int threads, size_t bytes, int* ext, int* sh, int* pr)
 
 }  // namespace
 
-cudaError_t plan_launch(const SceneView& sc, int device, int threads, LaunchShape* out)
+cudaError_t plan_launch(const SceneView& sc, int device, int threads, LaunchShape* out, int path_kernel)
 {
     if (threads <= 0 || threads > kThreads) threads = kThreads;
     int sms = 0;
@@ -1194,6 +1325,7 @@ cudaError_t plan_launch(const SceneView& sc, int device, int threads, LaunchShap
     out->blocks_primary = sms * (pr > 0 ? pr : 1);
     out->smem_spheres = bytes;
     out->mode = mode;
+    out->fused = mode == kIsBvh ? 0 : path_kernel == 2 ? 2 : (path_kernel == 0 && sc.n_sph <= kFusedMaxSpheres) ? 1 : 0;
     return cudaSuccess;
 }
 
@@ -1207,6 +1339,16 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
     const uint64_t paths = (uint64_t)job.n_pixels * job.spp;
     auto begin = [&](int fam) { if (timer) timer->begin(fam, stream); };
     auto end = [&](int fam) { if (timer) timer->end(fam, stream); };
+    if (shape.mode != kIsBvh && (shape.fused == 2 || (shape.fused == 1 && job.spp <= kFusedMaxSpp))) {
+        // whole paths in one thread per pixel
+        const int g = grid_for(job.n_pixels, kThreads, 1 << 20);
+        begin(kFamExtend);
+        if (shape.mode == kIsSmem) k_fused<kIsSmem><<<g, kThreads, sm, stream>>>(sc, cam, ws, job, accum, image);
+        else k_fused<kIsGlobal><<<g, kThreads, 0, stream>>>(sc, cam, ws, job, accum, image);
+        end(kFamExtend);
+        if (launches) *launches += 1;
+        return cudaGetLastError();
+    }
     if (bounces > 0) {
         cudaError_t e = cudaMemsetAsync(ws.counters, 0, sizeof(uint32_t) * wave_counter_words(bounces), stream);
         if (e != cudaSuccess) return e;

@@ -248,10 +248,22 @@ struct LaunchShape {
     int threads;
     size_t smem_spheres;      // dynamic shared memory for the sphere table (0: read from global)
     int mode;                 // nearest-hit structure: 0 brute force from global, 1 from shared memory, 2 LBVH
+    int fused;                // whole paths in one thread (k_fused): 0 never, 1 for waves of at most
+                              // kFusedMaxSpp samples per pixel, 2 always (brute-force tables only)
 };
 
+// Scenes of at most this many spheres on the brute-force tables render waves
+// of at most kFusedMaxSpp samples per pixel with whole paths in one thread
+// unless told otherwise (small scene: 1 sample per call +38%, 8 about even,
+// 64 -16% against the wavefront stages, whose shared first-bounce work pays
+// with many samples).
+constexpr uint32_t kFusedMaxSpheres = 24;
+constexpr uint32_t kFusedMaxSpp = 8;
+
 // Fills in grid sizes for this device and scene (occupancy-derived).
-cudaError_t plan_launch(const SceneView& sc, int device, int threads, LaunchShape* out);
+// path_kernel: 0 by scene size, 1 the wavefront stages, 2 whole paths in one
+// thread (brute-force tables only; the wavefront for LBVH scenes).
+cudaError_t plan_launch(const SceneView& sc, int device, int threads, LaunchShape* out, int path_kernel = 0);
 
 // Enqueues one wave on stream: 2*max_bounces + 1 kernels plus a counter reset.
 // accum is W*H float4, image W*H uint32 (may be null when pack_frame == 0).

@@ -421,6 +421,7 @@ def run_ours(args, dist: Dist):
                                        "on >= 99.99% of pixels), OpenMP over rows"}
         out["cpu_baseline_small_scene"] = cpu_small_scene()
     if dist.world == 1 and not args.no_extra:
+        out["small_scene"] = small_scene_leg(args, dev)
         out["large_scene"] = large_scene_leg(args, dev)
         out["batch"] = batch_compare(args, dev, max(3, min(args.steps, 8)))
         out["serve"] = serve_leg(args)
@@ -618,9 +619,70 @@ def large_scene_leg(args, dev: int) -> dict:
             "mpaths_s": round(steps * sc.pixels * sc.spp / (ms * 1e-3) / 1e6, 1),
             "mrays_s": round(rays / (ms * 1e-3) / 1e6, 1), "ms_per_launch": round(ms / steps, 3),
             "launches": steps, "bvh_in_use": int(s1["bvh_in_use"]),
-            "tuning": {k: tuned[k] for k in ("bvh_leaf_size", "lanes", "wave_paths", "threads", "wave_spp")},
+            "tuning": {k: tuned[k] for k in ("bvh_leaf_size", "lanes", "wave_paths", "threads", "wave_spp",
+                                              "path_kernel")},
             "tuning_source": "atx_autotune on this scene, camera and GPU" if not args.bvh_leaf else "--bvh-leaf",
             "autotune_s": round(tune_s, 2)}
+
+
+def small_scene_leg(args, dev: int) -> dict:
+    """The small scene (seed 0) as its workload states it: 1280x720, 5 bounces, 64 accumulated frames.
+    Ours renders the 64 frames in one launch and, as the reference's interactive loop does, one frame per
+    call (overlapped renders); the reference's own kernelRender renders them one frame per launch
+    (kernel-only device time, and with its per-frame Render() sequence)."""
+    import torch
+
+    import ataraxia_gb300 as atx
+    from ataraxia_gb300 import _native as N
+    from ataraxia_gb300 import scenes
+    from baseline import refbuild
+
+    sc = scenes.config0()
+    frames = sc.frames
+    cam = atx.Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction)
+    out = {"workload": "small scene: 8 spheres + ground, 8 materials, 1 light, 1280x720, 5 bounces, 64 frames"}
+    r = atx.Renderer(device=dev, flags=N.FLAG_OVERLAP_RENDERS)
+    r.on_resize(sc.width, sc.height)
+    r.set_scene(sc.spheres, sc.materials, sc.lights)
+    r.set_camera(cam)
+    r.set_settings(atx.Settings(accumulation=True, skyLight=False, maxBounces=sc.max_bounces))
+    stream = torch.cuda.ExternalStream(r.stream, device=dev)
+    for label, per_call in (("one_launch", frames), ("frame_per_call", 1)):
+        for _ in range(3):
+            r.reset_frame_index()
+            for _ in range(frames // per_call):
+                r.render_frames(per_call)
+        r.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r.reset_frame_index()
+        e0.record(stream)
+        for _ in range(frames // per_call):
+            r.render_frames(per_call)
+        r.join()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[f"ours_{label}_mpaths_s"] = round(sc.pixels * frames / (ms * 1e-3) / 1e6, 1)
+        out[f"ours_{label}_ms"] = round(ms, 3)
+    r.close()
+    if refbuild.available("fast"):
+        _, iv, _, ip = atx.camera_matrices(cam, sc.width, sc.height)
+        dirs = refbuild.ray_dirs(iv, ip, sc.width, sc.height)
+        with refbuild.RefRenderer(sc.spheres, sc.materials, sc.lights, sc.width, sc.height, dirs,
+                                  sc.camera_position, sc.camera_direction, sc.max_bounces) as ref:
+            ref.frames(3)
+            ref.set_frame(1)
+            k_ms = ref.time_frames(frames)
+            ref.set_frame(1)
+            t0 = time.perf_counter()
+            ref.frames(frames, full=True)
+            r_s = time.perf_counter() - t0
+        out["ref_kernel_mpaths_s"] = round(sc.pixels * frames / (k_ms * 1e-3) / 1e6, 1)
+        out["ref_render_mpaths_s"] = round(sc.pixels * frames / r_s / 1e6, 1)
+        out["vs_ref_kernel_one_launch"] = round(out["ours_one_launch_mpaths_s"] / out["ref_kernel_mpaths_s"], 2)
+        out["vs_ref_render_frame_per_call"] = round(out["ours_frame_per_call_mpaths_s"] /
+                                                     out["ref_render_mpaths_s"], 2)
+    return out
 
 
 def serve_leg(args) -> dict:

@@ -245,6 +245,9 @@ typedef struct atx_tuning {
     uint32_t wave_paths;       /* path state per lane, paths (default: sized to the launch, up to 64 Mi) */
     uint32_t threads;          /* threads per block of the primary and shadow kernels (multiple of 32, <= 256) */
     uint32_t wave_spp;         /* samples per wave at most: the wave's tile shape of pixels x samples */
+    uint32_t path_kernel;      /* 0: by scene size (whole paths in one thread up to 24 spheres), 1: the wavefront
+                                  stages, 2: whole paths in one thread (brute-force tables; LBVH scenes keep the
+                                  wavefront) */
     uint32_t from_cache;       /* atx_autotune: 1 when the setting came from the process-wide cache */
     double ms;                 /* atx_autotune: device time of one render with the chosen setting */
 } atx_tuning;

@@ -12,6 +12,7 @@ pytestmark = pytest.mark.gpu
 
 SETTINGS = [dict(), dict(bvh_leaf_size=4), dict(bvh_leaf_size=8), dict(bvh_leaf_size=32), dict(lanes=1),
             dict(lanes=2), dict(lanes=4), dict(wave_paths=1 << 20), dict(threads=128), dict(wave_spp=1),
+            dict(path_kernel=1), dict(path_kernel=2),
             dict(bvh_leaf_size=12, lanes=4, wave_paths=4 << 20, threads=128, wave_spp=4)]
 
 
@@ -78,5 +79,5 @@ def test_autotune_picks_a_setting_and_caches_it():
         assert bit_mismatches(acc, ref_acc) == 0
         t2 = r.autotune(spp, passes=1, use_cache=True)
         assert t2["from_cache"] == 1
-        assert {k: t2[k] for k in ("bvh_leaf_size", "lanes", "wave_paths", "threads", "wave_spp")} == \
-               {k: t1[k] for k in ("bvh_leaf_size", "lanes", "wave_paths", "threads", "wave_spp")}
+        assert {k: t2[k] for k in ("bvh_leaf_size", "lanes", "wave_paths", "threads", "wave_spp", "path_kernel")} == \
+               {k: t1[k] for k in ("bvh_leaf_size", "lanes", "wave_paths", "threads", "wave_spp", "path_kernel")}
