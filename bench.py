@@ -892,8 +892,11 @@ def run_render_only(args, dist: Dist):
     sc = {"medium": scenes.config1, "large": scenes.config2, "small": scenes.config0}[args.workload]()
     if args.width and args.height:
         sc = sc.with_resolution(args.width, args.height)
+    from ataraxia_gb300 import _native as N
+
+    # the bench's own renderer: overlapped renders (4 lanes)
     r = atx.Renderer(device=dist.local_rank, bvh_threshold=args.bvh_threshold, bvh_leaf_size=args.bvh_leaf,
-                     wave_paths=args.wave_paths)
+                     wave_paths=args.wave_paths, flags=N.FLAG_OVERLAP_RENDERS)
     r.on_resize(sc.width, sc.height)
     r.set_scene(sc.spheres, sc.materials, sc.lights)
     r.set_camera(atx.Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction))
