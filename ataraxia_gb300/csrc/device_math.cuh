@@ -202,6 +202,33 @@ __device__ __forceinline__ float3 sample_ggx(float3 n, float rough, uint32_t& se
     return to_world(sin_t * c, sin_t * s, cos_t, t, b, n);
 }
 
+// Renderer.cu:381-384: the next direction, sample_ggx for a metallic surface
+// and sample_cosine otherwise, with their shared steps written once: only the
+// polar terms differ (GGX: sin and cos of the sampled half-vector angle;
+// cosine: sqrt(u1) and sqrt(1 - u1)), so a warp whose lanes take both kinds
+// runs the random numbers, the sin/cos of 2*pi*u2, the tangent frame and the
+// change of basis once.  Every value is computed as in the two functions.
+__device__ __forceinline__ float3 sample_next(float3 n, float rough, float metallic, uint32_t& seed)
+{
+    const float u1 = pcg_float(seed);
+    const float u2 = pcg_float(seed);
+    float radial, z;
+    if (metallic > 0.0f) {
+        const float a = rough * rough;
+        const float cos_t = sqrtf((1.0f - u1) / (1.0f + (a * a - 1.0f) * u1));
+        radial = sqrtf(1.0f - cos_t * cos_t);
+        z = cos_t;
+    } else {
+        radial = sqrtf(u1);
+        z = sqrtf(1.0f - u1);
+    }
+    float c, s;
+    sincos_2pi(u2, c, s);
+    float3 t, b;
+    tangent_frame(n, t, b);
+    return to_world(radial * c, radial * s, z, t, b, n);
+}
+
 // Renderer.cu:166-168 + Renderer.h:70-78: accum / frame, clamp to [0, 1],
 // truncating x*255 per channel, packed A<<24 | B<<16 | G<<8 | R.
 __device__ __forceinline__ uint32_t pack_rgba8(float4 acc, float frame)

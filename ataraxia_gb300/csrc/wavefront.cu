@@ -283,7 +283,7 @@ __device__ __forceinline__ void shade_hit(const SceneView& sc, const float4* sph
         const float p = gmax(0.1f, gmin(1.0f, length3(thr)));
         if (!(pcg_float(seed) > p)) {
             thr = divs3(thr, p);
-            d = (metallic > 0.0f) ? sample_ggx(nrm, rough, seed) : sample_cosine(nrm, seed);
+            d = sample_next(nrm, rough, metallic, seed);
             // the next ray leaves this sphere (~0u: beyond the direction buffer's reach)
             own = db_reaches(sc, (uint32_t)hit, s, o) ? (uint32_t)hit : ~0u;
             r.push_next = true;
@@ -1012,7 +1012,7 @@ __global__ void __launch_bounds__(kThreads, kFusedBlocksPerSm) k_fused(SceneView
                 const float pr = gmax(0.1f, gmin(1.0f, length3(thr)));
                 if (pcg_float(seed) > pr) break;
                 thr = divs3(thr, pr);
-                d = (metallic > 0.0f) ? sample_ggx(nrm, rough, seed) : sample_cosine(nrm, seed);
+                d = sample_next(nrm, rough, metallic, seed);
             }
             a.x = a.x + c.x;
             a.y = a.y + c.y;
