@@ -6,9 +6,13 @@
 // written __fmaf_rn(), division and sqrtf are IEEE round-to-nearest and there
 // is no flush to zero.  Fused operations are used in exactly four places:
 // vector dot products (z*z' + (y*y' + x*x')), the half-b ray-sphere quadratic,
-// the sincos polynomial and the quarter-turn reduction.  Everything else
-// evaluates the reference's expressions as written (BRDF.cu, Renderer.cu), so
-// a CPU evaluation in the same order gives the same bits.
+// the sincos polynomial and the quarter-turn reduction.  Three quotients are
+// regrouped: a vector divided by a scalar is multiplied by the scalar's IEEE
+// reciprocal (the tangent frame, the roulette's throughput), the diffuse term
+// multiplies by 1/pi rounded to float, and the specular term's D * G / denom
+// is one quotient.  Everything else evaluates the reference's expressions as
+// written (BRDF.cu, Renderer.cu), so a CPU evaluation in the same order gives
+// the same bits.
 #pragma once
 
 #include <cstdint>
@@ -23,7 +27,12 @@ ATX_HD float3 add3(float3 a, float3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + 
 ATX_HD float3 sub3(float3 a, float3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
 ATX_HD float3 mul3(float3 a, float3 b) { return mk3(a.x * b.x, a.y * b.y, a.z * b.z); }
 ATX_HD float3 muls3(float3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
-ATX_HD float3 divs3(float3 a, float s) { return mk3(a.x / s, a.y / s, a.z / s); }
+// a / s as a * (1 / s): one IEEE division for the three components
+ATX_HD float3 mul_rcp3(float3 a, float s)
+{
+    const float r = 1.0f / s;
+    return mk3(a.x * r, a.y * r, a.z * r);
+}
 ATX_HD float3 neg3(float3 a) { return mk3(-a.x, -a.y, -a.z); }
 
 __device__ __forceinline__ float dot3(float3 a, float3 b)
@@ -86,6 +95,7 @@ __device__ __forceinline__ void sincos_2pi(float u, float& c, float& s)
 }
 
 constexpr float kPi = 0x1.921fb6p+1f;   // glm::pi<float>()
+constexpr float kInvPi = 1.0f / kPi;    // rounded to float
 constexpr float kOffset = 0.0001f;      // Renderer.cu:348, :372
 constexpr float kFltMax = 3.402823466e+38f;
 
@@ -115,13 +125,12 @@ __device__ __forceinline__ void ray_hit(float4 sph, float3 o, float3 d, float t,
 }
 
 // BRDF.cu:9-34 with fresnelSchlick (:36-40), distributionGGX (:42-53) and
-// geometrySmith / geometrySchlickGGX (:55-70) inlined.
-__device__ __forceinline__ float schlick_g(float ndotv, float rough)
-{
-    const float r = rough + 1.0f;
-    const float k = (r * r) / 8.0f;
-    return ndotv / (ndotv * (1.0f - k) + k);
-}
+// geometrySmith / geometrySchlickGGX (:55-70) inlined.  The specular term
+// F * (D * G) / denom, D = a2 / den and G = ndotv / g_v * ndotl / g_l, is
+// evaluated as F * X with X = (a2 * ndotv * ndotl) / (den * g_v * g_l * denom):
+// one division for five.  The factors stay in range for roughness >= 1e-4
+// (den >= pi a2^2, g >= 1/8, denom >= 0.001), so the regrouping changes X by
+// a few units in the last place; the diffuse term's / pi is * (1 / pi).
 
 __device__ __forceinline__ float3 cook_torrance(float3 albedo, float3 f0, float metallic, float rough, float3 n,
                                                 float3 v, float3 l)
@@ -144,15 +153,17 @@ __device__ __forceinline__ float3 cook_torrance(float3 albedo, float3 f0, float 
     float nh2 = ndoth * ndoth;
     float den = nh2 * (a2 - 1.0f) + 1.0f;
     den = kPi * den * den;
-    float D = a2 / den;
-    float G = schlick_g(ndotv, rough) * schlick_g(ndotl, rough);
+    const float r = rough + 1.0f;
+    const float k = (r * r) * 0.125f;
+    const float gv = ndotv * (1.0f - k) + k;
+    const float gl = ndotl * (1.0f - k) + k;
+    float denom = 4.0f * ndotl * ndotv + 0.001f;
+    const float X = ((a2 * ndotv) * ndotl) / (((den * gv) * gl) * denom);
 
     float3 one_f = sub3(mk3(1.0f, 1.0f, 1.0f), F);
     float3 kd = muls3(one_f, 1.0f - metallic);
-    float3 num = muls3(F, D * G);
-    float denom = 4.0f * ndotl * ndotv + 0.001f;
-    float3 spec = divs3(num, denom);
-    float3 diffuse = divs3(mul3(one_f, albedo), kPi);
+    float3 spec = muls3(F, X);
+    float3 diffuse = muls3(mul3(one_f, albedo), kInvPi);
     return muls3(add3(mul3(kd, diffuse), spec), ndotl);
 }
 
@@ -160,9 +171,9 @@ __device__ __forceinline__ float3 cook_torrance(float3 albedo, float3 f0, float 
 __device__ __forceinline__ void tangent_frame(float3 n, float3& t, float3& b)
 {
     if (fabsf(n.x) > fabsf(n.y))
-        t = divs3(mk3(-n.z, 0.0f, n.x), sqrtf(n.x * n.x + n.z * n.z));
+        t = mul_rcp3(mk3(-n.z, 0.0f, n.x), sqrtf(n.x * n.x + n.z * n.z));
     else
-        t = divs3(mk3(0.0f, -n.z, n.y), sqrtf(n.y * n.y + n.z * n.z));
+        t = mul_rcp3(mk3(0.0f, -n.z, n.y), sqrtf(n.y * n.y + n.z * n.z));
     b = cross3(n, t);
 }
 

@@ -282,7 +282,7 @@ __device__ __forceinline__ void shade_hit(const SceneView& sc, const float4* sph
         o = add3(pos, muls3(nrm, kOffset));
         const float p = gmax(0.1f, gmin(1.0f, length3(thr)));
         if (!(pcg_float(seed) > p)) {
-            thr = divs3(thr, p);
+            thr = mul_rcp3(thr, p);
             d = sample_next(nrm, rough, metallic, seed);
             // the next ray leaves this sphere (~0u: beyond the direction buffer's reach)
             own = db_reaches(sc, (uint32_t)hit, s, o) ? (uint32_t)hit : ~0u;
@@ -1011,7 +1011,7 @@ __global__ void __launch_bounds__(kThreads, kFusedBlocksPerSm) k_fused(SceneView
                 o = add3(pos, muls3(nrm, kOffset));
                 const float pr = gmax(0.1f, gmin(1.0f, length3(thr)));
                 if (pcg_float(seed) > pr) break;
-                thr = divs3(thr, pr);
+                thr = mul_rcp3(thr, pr);
                 d = sample_next(nrm, rough, metallic, seed);
             }
             a.x = a.x + c.x;

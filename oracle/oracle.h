@@ -33,8 +33,12 @@
  *   ORC_EXACT    FP32 in the evaluation order the CUDA kernels use: vector dot
  *                products as fused multiply-add chains, the ray-sphere
  *                quadratic in its half-b form with fused terms, x^5 as three
- *                products and sin/cos(2*pi*u) from a Taylor polynomial after
- *                exact quarter-turn reduction.  Every other expression is the
+ *                products, sin/cos(2*pi*u) from a Taylor polynomial after
+ *                exact quarter-turn reduction, a vector over a scalar as a
+ *                product with the scalar's reciprocal (tangent frame, the
+ *                roulette's throughput), / pi as * (1 / pi) and the specular
+ *                F * D * G / denom with one quotient for D * G / denom.
+ *                Every other expression is the
  *                reference's, evaluated with IEEE single rounding and no
  *                contraction.  The kernels must equal this mode bit for bit.
  *   ORC_LITERAL  FP32 following the reference's expressions as written

@@ -7,7 +7,9 @@
  *   REAL     float or double
  *   FN(x)    mode-prefixed name
  *   EXACT    1: the kernels' evaluation order (fused dot chains, half-b
- *               quadratic, polynomial sincos, x^5 by products)
+ *               quadratic, polynomial sincos, x^5 by products, reciprocal
+ *               products for a vector over a scalar and for / pi, one
+ *               quotient for the specular D * G / denom)
  *            0: the reference's expressions as written
  *   F64      1 in the double-precision build
  * The file is compiled with -ffp-contract=off, so every a*b+c below rounds
@@ -23,6 +25,16 @@ static inline V3 FN(sub)(V3 a, V3 b) { return FN(mk)(a.x - b.x, a.y - b.y, a.z -
 static inline V3 FN(mul)(V3 a, V3 b) { return FN(mk)(a.x * b.x, a.y * b.y, a.z * b.z); }
 static inline V3 FN(muls)(V3 a, REAL s) { return FN(mk)(a.x * s, a.y * s, a.z * s); }
 static inline V3 FN(divs)(V3 a, REAL s) { return FN(mk)(a.x / s, a.y / s, a.z / s); }
+/* a / s where the kernels multiply by the reciprocal (the tangent frame, the
+ * roulette's throughput); the reference's a / s otherwise. */
+static inline V3 FN(div_v)(V3 a, REAL s)
+{
+#if EXACT
+    return FN(muls)(a, (REAL)1 / s);
+#else
+    return FN(divs)(a, s);
+#endif
+}
 static inline V3 FN(neg)(V3 a) { return FN(mk)(-a.x, -a.y, -a.z); }
 static inline V3 FN(ld)(const float* p) { return FN(mk)((REAL)p[0], (REAL)p[1], (REAL)p[2]); }
 
@@ -223,14 +235,29 @@ static V3 FN(cook_torrance)(V3 albedo, V3 f0, REAL metallic, REAL rough, V3 n, V
     REAL vdoth = FN(maxr)(FN(dot)(v, h), (REAL)0);
 
     V3 F = FN(fresnel)(f0, vdoth);
+    V3 kd = FN(muls)(FN(sub)(FN(mk)(1, 1, 1), F), (REAL)1 - metallic);
+    REAL denom = (REAL)4 * ndotl * ndotv + (REAL)0.001f;
+#if EXACT
+    /* The kernels' grouping: F * (D * G) / denom as F * X, X = (a2 * ndotv *
+     * ndotl) / (den * g_v * g_l * denom), one division; / pi as * (1 / pi). */
+    const REAL a = rough * rough;
+    const REAL a2 = a * a;
+    REAL den = (ndoth * ndoth) * (a2 - (REAL)1) + (REAL)1;
+    den = PI_R * den * den;
+    const REAL r = rough + (REAL)1;
+    const REAL k = (r * r) * (REAL)0.125f;
+    const REAL gv = ndotv * ((REAL)1 - k) + k;
+    const REAL gl = ndotl * ((REAL)1 - k) + k;
+    const REAL X = ((a2 * ndotv) * ndotl) / (((den * gv) * gl) * denom);
+    V3 spec = FN(muls)(F, X);
+    V3 diffuse = FN(muls)(FN(mul)(FN(sub)(FN(mk)(1, 1, 1), F), albedo), (REAL)1 / PI_R);
+#else
     REAL D = FN(ggx_d)(ndoth, rough);
     REAL G = FN(schlick_g)(ndotv, rough) * FN(schlick_g)(ndotl, rough);
-
-    V3 kd = FN(muls)(FN(sub)(FN(mk)(1, 1, 1), F), (REAL)1 - metallic);
     V3 num = FN(muls)(F, D * G);
-    REAL denom = (REAL)4 * ndotl * ndotv + (REAL)0.001f;
     V3 spec = FN(divs)(num, denom);
     V3 diffuse = FN(divs)(FN(mul)(FN(sub)(FN(mk)(1, 1, 1), F), albedo), PI_R);
+#endif
     return FN(muls)(FN(add)(FN(mul)(kd, diffuse), spec), ndotl);
 }
 
@@ -238,9 +265,9 @@ static V3 FN(cook_torrance)(V3 albedo, V3 f0, REAL metallic, REAL rough, V3 n, V
 static inline void FN(frame)(V3 n, V3* t, V3* b)
 {
     if (FABS(n.x) > FABS(n.y))
-        *t = FN(divs)(FN(mk)(-n.z, 0, n.x), SQRT(n.x * n.x + n.z * n.z));
+        *t = FN(div_v)(FN(mk)(-n.z, 0, n.x), SQRT(n.x * n.x + n.z * n.z));
     else
-        *t = FN(divs)(FN(mk)(0, -n.z, n.y), SQRT(n.y * n.y + n.z * n.z));
+        *t = FN(div_v)(FN(mk)(0, -n.z, n.y), SQRT(n.y * n.y + n.z * n.z));
     *b = FN(cross)(n, *t);
 }
 
@@ -350,7 +377,7 @@ static V3 FN(per_pixel)(const orc_scene* sc, const orc_view* view, uint32_t x, u
         const int stop = FN(pcg_float)(&seed) > p;
         orc_emit(sk, ORC_EV_ROULETTE, i, (uint32_t)stop);
         if (stop) break;
-        thr = FN(divs)(thr, p);
+        thr = FN(div_v)(thr, p);
         orc_emit(sk, ORC_EV_FRAME, i, (uint32_t)(FABS(h.normal.x) > FABS(h.normal.y)));
 
         if (m->metallic > 0.0f)

@@ -39,7 +39,6 @@ def add(a, b): return (a[0] + b[0], a[1] + b[1], a[2] + b[2])
 def sub(a, b): return (a[0] - b[0], a[1] - b[1], a[2] - b[2])
 def mul(a, b): return (a[0] * b[0], a[1] * b[1], a[2] * b[2])
 def muls(a, s): return (a[0] * s, a[1] * s, a[2] * s)
-def divs(a, s): return (a[0] / s, a[1] / s, a[2] / s)
 
 
 def dot(a, b):
@@ -154,24 +153,30 @@ def cook_torrance(albedo, f0, metal, rough, n, vv, l):
     a2 = a * a
     den = (ndh * ndh) * (a2 - ONE) + ONE
     den = PI * den * den
-    D = a2 / den
     rr = rough + ONE
-    k = (rr * rr) / F(8.0)
-    G = (ndv / (ndv * (ONE - k) + k)) * (ndl / (ndl * (ONE - k) + k))
+    k = (rr * rr) * F(0.125)
+    gv = ndv * (ONE - k) + k
+    gl = ndl * (ONE - k) + k
     one_f = sub(v(1, 1, 1), Fr)
     kd = muls(one_f, ONE - metal)
-    num = muls(Fr, D * G)
     denom = F(4.0) * ndl * ndv + F(0.001)
-    spec = divs(num, denom)
-    diffuse = divs(mul(one_f, albedo), PI)
+    # matched grouping: F * (D * G) / denom = F * (a2 ndv ndl) / (den gv gl denom); / pi as * (1 / pi)
+    x = ((a2 * ndv) * ndl) / (((den * gv) * gl) * denom)
+    spec = muls(Fr, x)
+    diffuse = muls(mul(one_f, albedo), ONE / PI)
     return muls(add(mul(kd, diffuse), spec), ndl)
+
+
+def div_v(a, s):
+    """a / s as the kernels evaluate it: a * (1 / s)."""
+    return muls(a, ONE / s)
 
 
 def frame(n):
     if abs(n[0]) > abs(n[1]):
-        t = divs((-n[2], ZERO, n[0]), np.sqrt(n[0] * n[0] + n[2] * n[2]))
+        t = div_v((-n[2], ZERO, n[0]), np.sqrt(n[0] * n[0] + n[2] * n[2]))
     else:
-        t = divs((ZERO, -n[2], n[1]), np.sqrt(n[1] * n[1] + n[2] * n[2]))
+        t = div_v((ZERO, -n[2], n[1]), np.sqrt(n[1] * n[1] + n[2] * n[2]))
     return t, cross(n, t)
 
 
@@ -244,6 +249,6 @@ def per_pixel(scene, ip, iv, pos, W, H, x, y, frame_index, max_bounces, sky=Fals
         pr = gmax(F(0.1), gmin(ONE, np.sqrt(dot(thr, thr))))
         if seed.float() > pr:
             break
-        thr = divs(thr, pr)
+        thr = div_v(thr, pr)
         d = sample_ggx(nrm, rough, seed) if metal > ZERO else sample_cosine(nrm, seed)
     return color
