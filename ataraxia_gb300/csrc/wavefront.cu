@@ -891,10 +891,26 @@ __global__ void __launch_bounds__(kThreads) k_accumulate(WaveState ws, WaveJob j
     const bool shared = wave_shares_primary(job);
     const uint2* prim = job.prim_cache ? job.prim_cache + job.pixel0 : ws.prim;
     const float4 miss = job.sky ? make_float4(0.6f, 0.7f, 0.9f, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float fspp = __uint2float_rn(job.spp);
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < job.n_pixels; j += stride) {
         const uint32_t p = job.pixel0 + j;
         float4 a = accum[p];
         const bool missed = shared && (int32_t)prim[j].y < 0;
+        // Every sample adds (0, 0, 0) and a frame (a missed primary without
+        // sky light, or no bounces): the spp additions of 0 leave x, y, z as
+        // the first one does (-0 becomes +0), and spp additions of 1 to an
+        // integer count stay exact up to 2^24, so one addition of spp equals
+        // them.
+        if ((missed ? !job.sky : job.max_bounces <= 0) && job.spp > 0u && a.w >= 0.0f &&
+            a.w <= 16777216.0f - fspp && a.w == truncf(a.w)) {
+            a.x = a.x + 0.0f;
+            a.y = a.y + 0.0f;
+            a.z = a.z + 0.0f;
+            a.w = a.w + fspp;
+            accum[p] = a;
+            if (job.pack_frame) image[p] = pack_rgba8(a, fpack);
+            continue;
+        }
         for (uint32_t s = 0; s < job.spp; ++s) {
             float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
             if (missed) c = miss;
