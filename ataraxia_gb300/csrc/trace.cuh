@@ -103,8 +103,11 @@ __device__ __forceinline__ float4 table_sphere(const float4* __restrict__ sph, u
 // division out of the inner loop.  Each sphere shifts h's sign bit in from the
 // right (one funnel shift) and the word is inverted once at the end, so
 // sphere base+k ends at bit 31-k: the highest set bit is the lowest index.
-// CNT is 32 for a full chunk, 31 for a partial one of cnt spheres.
-template <bool SMEM, int CNT>
+// CNT is 32 for a full chunk, 31 for a partial one of cnt spheres.  EXIT:
+// a partial chunk leaves the unrolled loop after its last sphere instead of
+// stepping over the rest (k_fused, whose small tables are one partial chunk;
+// elsewhere the guarded form compiles to the better code for full chunks).
+template <bool SMEM, int CNT, bool EXIT = false>
 __device__ __forceinline__ uint32_t candidate_bits(const float4* __restrict__ sph, uint32_t base, float3 o, float3 d,
                                                    float a, uint32_t cnt)
 {
@@ -118,6 +121,7 @@ __device__ __forceinline__ uint32_t candidate_bits(const float4* __restrict__ sp
         const uint32_t np = CNT == 32 ? 16u : (cnt + 1u) >> 1;
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
+            if (EXIT && CNT != 32 && (uint32_t)k >= np) break;
             if (CNT == 32 || (uint32_t)k < np) {
                 const float4 p = sph[base + 2u * k], q = sph[base + 2u * k + 1u];
                 const float2 vx = __fadd2_rn(ox, make_float2(p.x, p.y));
@@ -137,6 +141,7 @@ __device__ __forceinline__ uint32_t candidate_bits(const float4* __restrict__ sp
     }
 #pragma unroll
     for (int k = 0; k < CNT; ++k) {
+        if (EXIT && CNT != 32 && (uint32_t)k >= cnt) break;
         if (CNT == 32 || (uint32_t)k < cnt) {
             const float4 s = __ldg(&sph[base + k]);
             const float ox = o.x - s.x, oy = o.y - s.y, oz = o.z - s.z;
@@ -152,7 +157,7 @@ __device__ __forceinline__ uint32_t candidate_bits(const float4* __restrict__ sp
 }
 
 // Renderer.cu:256-279: brute-force nearest hit, lowest index on equal t.
-template <bool SMEM>
+template <bool SMEM, bool EXIT = false>
 __device__ __forceinline__ int32_t nearest_brute(const float4* __restrict__ sph, uint32_t n, float3 o, float3 d,
                                                  float& tmin)
 {
@@ -162,7 +167,7 @@ __device__ __forceinline__ int32_t nearest_brute(const float4* __restrict__ sph,
     for (uint32_t base = 0; base < n; base += 32u) {
         const uint32_t cnt = n - base;
         uint32_t mask = cnt >= 32u ? candidate_bits<SMEM, 32>(sph, base, o, d, a, 32u)
-                                   : candidate_bits<SMEM, 31>(sph, base, o, d, a, cnt);
+                                   : candidate_bits<SMEM, 31, EXIT>(sph, base, o, d, a, cnt);
         while (mask) {
             const uint32_t k = (uint32_t)__clz(mask);   // lowest sphere index first (ties keep it)
             mask &= ~(0x80000000u >> k);
@@ -182,7 +187,7 @@ __device__ __forceinline__ int32_t nearest_brute(const float4* __restrict__ sph,
 // hit and tests t > 0 && t*t < dist2; since the nearest accepted t is <= every
 // accepted t and squaring is monotone, that equals "some sphere has t > 0 and
 // t*t < dist2", so the loop can stop at the first such sphere.
-template <bool SMEM>
+template <bool SMEM, bool EXIT = false>
 __device__ __forceinline__ bool occluded_brute(const float4* __restrict__ sph, uint32_t n, float3 o, float3 d,
                                                float dist2)
 {
@@ -190,7 +195,7 @@ __device__ __forceinline__ bool occluded_brute(const float4* __restrict__ sph, u
     for (uint32_t base = 0; base < n; base += 32u) {
         const uint32_t cnt = n - base;
         uint32_t mask = cnt >= 32u ? candidate_bits<SMEM, 32>(sph, base, o, d, a, 32u)
-                                   : candidate_bits<SMEM, 31>(sph, base, o, d, a, cnt);
+                                   : candidate_bits<SMEM, 31, EXIT>(sph, base, o, d, a, cnt);
         while (mask) {
             const uint32_t k = (uint32_t)__clz(mask);
             mask &= ~(0x80000000u >> k);
@@ -481,12 +486,12 @@ __device__ __forceinline__ bool db_reaches(const SceneView& sc, uint32_t own, fl
     return dot3(e, e) <= reach * reach;
 }
 
-template <int IS>
+template <int IS, bool EXIT = false>
 __device__ __forceinline__ int32_t scene_nearest(const SceneView& sc, const float4* sph, float3 o, float3 d,
                                                  float& tmin)
 {
     if (IS == kIsBvh) return bvh_nearest(sc, o, d, tmin);
-    return nearest_brute<IS == kIsSmem>(sph, sc.n_sph, o, d, tmin);
+    return nearest_brute<IS == kIsSmem, EXIT>(sph, sc.n_sph, o, d, tmin);
 }
 
 // Nearest hit of a ray leaving sphere own (~0u: from elsewhere).
@@ -498,12 +503,12 @@ __device__ __forceinline__ int32_t scene_nearest_from(const SceneView& sc, const
     return scene_nearest<IS>(sc, sph, o, d, tmin);
 }
 
-template <int IS>
+template <int IS, bool EXIT = false>
 __device__ __forceinline__ bool scene_occluded(const SceneView& sc, const float4* sph, float3 o, float3 d,
                                                float dist2)
 {
     if (IS == kIsBvh) return bvh_occluded(sc, o, d, dist2);
-    return occluded_brute<IS == kIsSmem>(sph, sc.n_sph, o, d, dist2);
+    return occluded_brute<IS == kIsSmem, EXIT>(sph, sc.n_sph, o, d, dist2);
 }
 
 }  // namespace atx

@@ -965,7 +965,7 @@ __global__ void __launch_bounds__(kThreads, kFusedBlocksPerSm) k_fused(SceneView
                 t0 = __uint_as_float(pr.x);
                 h0 = (int32_t)pr.y;
             } else {
-                h0 = scene_nearest<IS>(sc, sph, o0, d0, t0);
+                h0 = scene_nearest<IS, true>(sc, sph, o0, d0, t0);
                 if (job.prim_cache) job.prim_cache[p] = make_uint2(__float_as_uint(t0), (uint32_t)h0);
             }
         }
@@ -980,7 +980,7 @@ __global__ void __launch_bounds__(kThreads, kFusedBlocksPerSm) k_fused(SceneView
                 float tmin = t0;
                 int32_t hit = h0;
                 if (i > 0) {
-                    hit = scene_nearest<IS>(sc, sph, o, d, tmin);
+                    hit = scene_nearest<IS, true>(sc, sph, o, d, tmin);
                     ++n_ext;
                 } else if (hit >= 0) {
                     ++n_first;
@@ -1013,7 +1013,7 @@ __global__ void __launch_bounds__(kThreads, kFusedBlocksPerSm) k_fused(SceneView
                         lit = (seen & bit) != 0u;
                     } else {
                         const float3 so = add3(pos, muls3(nrm, kOffset));
-                        lit = sc.n_sph == 0u || !scene_occluded<IS>(sc, sph, so, L, dist2);
+                        lit = sc.n_sph == 0u || !scene_occluded<IS, true>(sc, sph, so, L, dist2);
                         ++n_sh;
                         if (i == 0 && cache_vis) {
                             known |= bit;
