@@ -7,8 +7,9 @@ paths (one path = one pixel-sample).  Synthetic seeded scene (scenes.config1);
 the camera is set through the public API (atx_set_camera) as a caller would.
 
 Metric: Mpaths/s, whole job (N replicas on N GPUs, one process per GPU,
-`scaling: weak`).  The path state of one wave (4 Mi paths x 120 B) is larger
-than L2, so every step streams its working set through HBM; no explicit flush.
+`scaling: weak`).  The path state of a launch (four lanes of 8.3 Mi paths,
+about 1 GB each) is larger than L2, so every step streams its working set
+through HBM; no explicit flush.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -48,6 +49,8 @@ def hbm_peak_gbs():
         return 6800.0
 METRIC = "Mpaths/s per GB300"
 UNIT = "Mpaths/s"
+WORKLOAD_MEDIUM = ("medium scene: 256 spheres, 64 materials, 8 lights, 1920x1080, 8 bounces, "
+                   "16 spp per launch (one step = one launch)")
 
 
 def log(*a):
@@ -395,10 +398,9 @@ def run_ours(args, dist: Dist):
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes.config1)",
-        "config": {"workload": "medium scene: 256 spheres, 64 materials, 8 lights, 1920x1080, 8 bounces, "
-                               "16 spp per launch (one step = one launch)",
+        "config": {"workload": WORKLOAD_MEDIUM,
                    "paths_per_step": paths_step, "parallelism": f"replicas x{dist.world}",
-                   "l2": "working set > L2: two lanes of 16.6 Mi-path wave state (2.3 GB each) per launch"},
+                   "l2": "working set > L2: four lanes of 8.3 Mi-path wave state (about 1 GB each) per launch"},
         "mrays_per_s": round(mrays, 1),
         "rays_per_path": round(rays / (args.steps * paths_step), 4),
         "primary_hit_frac": round(shaded0 / (prof_steps * paths_step), 4),
@@ -938,14 +940,15 @@ def run_reference(args, dist: Dist):
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": dist.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes.config1)",
-        "config": {"workload": "medium scene: 256 spheres, 64 materials, 8 lights, 1920x1080, 8 bounces, "
-                               "16 spp per launch", "parallelism": "host cores (OpenMP)"},
+        "config": {"workload": WORKLOAD_MEDIUM, "parallelism": "host cores (OpenMP)"},
         "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample + " per step"},
         "mrays_per_s": round(statistics.mean(mrays), 3),
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference's own render path needs glm, Vulkan and GLFW, absent here; this arm runs its "
-                "per-pixel path restated in C on the host cores",
+        "note": "the reference's perPixel is device code only, with no host path of its own; this arm runs it "
+                "restated in C (the oracle's literal mode, within 1e-3 of the reference's kernel built with IEEE "
+                "arithmetic on >= 99.99% of pixels) on the host cores; the reference's own CUDA kernel, compiled "
+                "from its sources, is timed in the main line's ref_cuda_kernel",
     }
 
 
