@@ -1406,8 +1406,12 @@ cudaError_t enqueue_wave(const SceneView& sc, const CameraView& cam, const WaveS
             for (int b = 0; b < bounces; ++b) {
                 if constexpr (IS != kIsBvh) {
                     if (inl && b >= kPathsFrom) {   // the late bounces in one persistent launch
+                        // on half the resident blocks: the late bounces are a trickle of
+                        // paths, and the blocks stay resident until their pools drain,
+                        // holding slots the other lanes' kernels could use (+1%)
                         begin(kFamExtend);
-                        k_paths<kIsGlobal><<<shape.blocks_extend, kExtendThreads, 0, stream>>>(sc, ws, job, b);
+                        k_paths<kIsGlobal><<<max(1, shape.blocks_extend / 2), kExtendThreads, 0, stream>>>(sc, ws, job,
+                                                                                                           b);
                         end(kFamExtend);
                         ++nl;
                         break;

@@ -109,18 +109,17 @@ class Clocks:
         self.lines: list[str] = []
 
     def start(self):
+        """Starts sampling every 100 ms; the caller keeps the GPU on the workload until the timed region."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
                  "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            time.sleep(0.3)
         except OSError:
             self.proc = None
 
     def stop(self) -> dict:
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        time.sleep(0.15)
         self.proc.terminate()
         out, _ = self.proc.communicate(timeout=10)
         rows = [l.split(",") for l in out.strip().splitlines() if l.strip()]
@@ -136,7 +135,19 @@ class Clocks:
                 if v.strip().lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "window": "untimed launches of the same workload for 0.4 s before and 0.25 s after the timed "
+                          "region keep every sample under load"}
+
+
+def soak(r, spp: int, seconds: float):
+    """Untimed launches of the workload for about `seconds`, around the timed region while the clock
+    sampler runs (the timed region itself is too short for more than a sample or two)."""
+    t_end = time.perf_counter() + seconds
+    while time.perf_counter() < t_end:
+        for _ in range(32):
+            r.render_frames(spp)
+        r.synchronize()
 
 
 # ------------------------------------------------------------ CPU baseline
@@ -211,11 +222,12 @@ def run_ours(args, dist: Dist):
     stream = torch.cuda.ExternalStream(r.stream, device=dev)
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
-    s0 = r.stats()
     clocks = Clocks(dev)
+    clocks.start()
+    soak(r, sc.spp, 0.4)
+    s0 = r.stats()
     dist.barrier()
     torch.cuda.synchronize()
-    clocks.start()
     ev0.record(stream)
     for _ in range(args.steps):
         r.render_frames(sc.spp)
@@ -223,9 +235,10 @@ def run_ours(args, dist: Dist):
     ev1.record(stream)
     ev1.synchronize()
     torch.cuda.synchronize()
+    s1 = r.stats()
+    soak(r, sc.spp, 0.25)
     clk = clocks.stop()
     dist.barrier()
-    s1 = r.stats()
     ms_local = ev0.elapsed_time(ev1)
     ms = dist.max(ms_local)
     launches = s1["kernel_launches"] - s0["kernel_launches"]
