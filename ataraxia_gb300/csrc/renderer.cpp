@@ -843,20 +843,36 @@ atx_status Renderer::tuning(atx_tuning* out)
     return ATX_OK;
 }
 
+// Device time per render of `passes` renders issued back to back, as a caller
+// renders: one interval on stream_ from before the first to after the last
+// (with overlapped renders a render's own events would also hold the
+// previous render's lanes).
 atx_status Renderer::time_renders(uint32_t spp, uint32_t passes, double* ms)
 {
     frame_ = 1;
     ATX_TRY(render(spp));   // the per-camera tables are built on the second render of a camera
     ATX_TRY(render(spp));
-    double total = 0.0;
-    for (uint32_t k = 0; k < passes; ++k) {
-        ATX_TRY(render(spp));
-        ATX_CUDA(cudaEventSynchronize(ev_stop_));
-        float t = 0.0f;
-        ATX_CUDA(cudaEventElapsedTime(&t, ev_start_, ev_stop_));
-        total += t;
+    ATX_TRY(join());
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaError_t e = cudaEventCreate(&ev[0]);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[0], stream_);
+    atx_status s = ATX_OK;
+    if (e == cudaSuccess) {
+        for (uint32_t k = 0; k < passes && s == ATX_OK; ++k) s = render(spp);
+        if (s == ATX_OK) s = join();
+        if (s == ATX_OK) {
+            e = cudaEventRecord(ev[1], stream_);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+            float t = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+            *ms = (double)t / passes;
+        }
     }
-    *ms = total / passes;
+    for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    ATX_TRY(s);
+    ATX_CUDA(e);
     return ATX_OK;
 }
 

@@ -622,7 +622,7 @@ def large_scene_leg(args, dev: int) -> dict:
     r.set_camera(atx.Camera(sc.fov, sc.near, sc.far, sc.camera_position, sc.camera_direction))
     r.set_settings(atx.Settings(accumulation=True, skyLight=False, maxBounces=sc.max_bounces))
     t0 = time.perf_counter()
-    tuned = r.autotune(sc.spp, passes=2, use_cache=False) if not args.bvh_leaf else r.tuning()
+    tuned = r.autotune(sc.spp, passes=3, use_cache=False) if not args.bvh_leaf else r.tuning()
     tune_s = time.perf_counter() - t0
     for _ in range(3):
         r.render_frames(sc.spp)
