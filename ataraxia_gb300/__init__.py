@@ -418,8 +418,8 @@ class Renderer:
         N.check(N.lib().atx_get_tuning(self._h, C.byref(t)))
         return {k: getattr(t, k) for k, _ in N.Tuning._fields_}
 
-    def set_tuning(self, bvh_leaf_size=0, lanes=0, wave_paths=0, threads=0, wave_spp=0, path_kernel=0):
-        t = N.Tuning(bvh_leaf_size, lanes, wave_paths, threads, wave_spp, path_kernel, 0, 0.0)
+    def set_tuning(self, bvh_leaf_size=0, lanes=0, wave_paths=0, threads=0, wave_spp=0, path_kernel=0, cell_res=0):
+        t = N.Tuning(bvh_leaf_size, lanes, wave_paths, threads, wave_spp, path_kernel, 0, cell_res, 0.0)
         N.check(N.lib().atx_set_tuning(self._h, C.byref(t)))
 
     def reset_kernel_times(self):

@@ -76,7 +76,7 @@ class Stats(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("bvh_leaf_size", C.c_uint32), ("lanes", C.c_uint32), ("wave_paths", C.c_uint32),
                 ("threads", C.c_uint32), ("wave_spp", C.c_uint32), ("path_kernel", C.c_uint32),
-                ("from_cache", C.c_uint32), ("ms", C.c_double)]
+                ("from_cache", C.c_uint32), ("cell_res", C.c_uint32), ("ms", C.c_double)]
 
 
 class KernelTimes(C.Structure):

@@ -112,6 +112,7 @@ atx_status Batch::add_scene(const atx_batch_scene& d, uint32_t* id)
     s->image.use_stream_order(&order_);
     s->prim.use_stream_order(&order_);
     s->dirs.use_stream_order(&order_);
+    s->scene.cell_res = cell_res_;
     // on the upload stream: a pass running on the batch stream is not waited for
     ATX_TRY(s->scene.upload(d.spheres, d.n_spheres, d.materials, d.n_materials, d.lights, d.n_lights, &budget_,
                             up_stream_));

@@ -60,6 +60,10 @@ public:
     // Device bytes of the lanes' path state (not charged to the budget).
     uint64_t scratch_bytes() const { return scratch_.used(); }
     cudaStream_t stream() const { return stream_; }
+    // Cells along a face's edge of the light and direction buffers of scenes
+    // added from now on (0: default_cell_res by sphere count; the server's
+    // per-job scenes use kCellResJobs, which are cheaper to build).
+    void set_cell_res(uint32_t res) { cell_res_ = res; }
 
 private:
     struct Slot {
@@ -89,6 +93,7 @@ private:
     void release_scratch();
 
     atx_config cfg_;
+    uint32_t cell_res_ = 0;
     Budget budget_;      // resident scenes
     Budget scratch_;     // lanes' path state
     cudaStream_t stream_ = nullptr;      // passes, read-backs, frees

@@ -31,8 +31,10 @@ constexpr double kK = 1.2207031e-3;   // 5 sqrt(2^-24) per unit of distance, as 
 uint64_t up(uint64_t x) { return (x + 255u) & ~uint64_t(255u); }
 
 // Scratch for the cell cones (k_cell_cones) at the end of both buffers.
-constexpr uint64_t kConeBytes = ((kLbCells * sizeof(float4) + 255u) & ~uint64_t(255u)) +
-                                ((kLbCells * sizeof(float) + 255u) & ~uint64_t(255u));
+uint64_t cone_bytes(uint32_t res)
+{
+    return up(cells_for(res) * sizeof(float4)) + up(cells_for(res) * sizeof(float));
+}
 
 // Unit direction of face f (0..5: +x, -x, +y, -y, +z, -z) at in-face
 // coordinates (u, v): the axes trace.cuh lb_cell divides by the face axis
@@ -55,13 +57,14 @@ __device__ float dotf3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z 
 // lookup's rounding, the rest for the build's arithmetic): axis and the
 // cosine of the half-angle in cone[cell], its sine in cone_sin[cell].  The
 // farthest points of a cell from its centre are its corners.
-__global__ void k_cell_cones(float4* cone, float* cone_sin)
+__global__ void k_cell_cones(uint32_t res, float4* cone, float* cone_sin)
 {
     const uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= kLbCells) return;
-    const uint32_t f = cell / (kLbRes * kLbRes), i = (cell / kLbRes) % kLbRes, j = cell % kLbRes;
-    const float u0 = 2.0f * i / kLbRes - 1.0f, u1 = 2.0f * (i + 1) / kLbRes - 1.0f;
-    const float v0 = 2.0f * j / kLbRes - 1.0f, v1 = 2.0f * (j + 1) / kLbRes - 1.0f;
+    if (cell >= cells_for(res)) return;
+    const uint32_t f = cell / (res * res), i = (cell / res) % res, j = cell % res;
+    const float fr = (float)res;
+    const float u0 = 2.0f * i / fr - 1.0f, u1 = 2.0f * (i + 1) / fr - 1.0f;
+    const float v0 = 2.0f * j / fr - 1.0f, v1 = 2.0f * (j + 1) / fr - 1.0f;
     const float3 ctr = face_dir(f, 0.5f * (u0 + u1), 0.5f * (v0 + v1));
     float cmin = 1.0f;
     for (int k = 0; k < 4; ++k) cmin = fminf(cmin, dotf3(ctr, face_dir(f, (k & 1) ? u1 : u0, (k & 2) ? v1 : v0)));
@@ -98,11 +101,13 @@ __global__ void k_lb_dcap(const float4* __restrict__ sph, const float* __restric
 // taken from it, a 2e-5 slack on the final comparison.
 __global__ void k_lb_build(const float4* __restrict__ sph, const float* __restrict__ rad, uint32_t n,
                            const DevLight* __restrict__ lights, uint32_t nl, const float* __restrict__ dcap,
-                           const float4* __restrict__ cone, const float* __restrict__ cone_sin, uint16_t* line)
+                           uint32_t res, const float4* __restrict__ cone, const float* __restrict__ cone_sin,
+                           uint16_t* line)
 {
+    const uint32_t cells = cells_for(res);
     const uint32_t id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
-    if (id >= nl * kLbCells) return;   // whole warps: blockDim is a multiple of 32
-    const uint32_t l = id / kLbCells, cell = id % kLbCells;
+    if (id >= nl * cells) return;   // whole warps: blockDim is a multiple of 32
+    const uint32_t l = id / cells, cell = id % cells;
     const float4 cc = cone[cell];
     const float3 ctr = make_float3(cc.x, cc.y, cc.z);
     const float ch = cc.w, sh = cone_sin[cell];
@@ -197,7 +202,7 @@ __device__ bool db_listed(float3 ctr, float ch, float sh, float4 o, float rho, f
 // face axis), kept in index order; then one warp per cell at a time tests only
 // those and appends the listed ones in index order.
 __global__ void __launch_bounds__(256) k_db_build(const float4* __restrict__ sph, const float* __restrict__ rad,
-                                                  uint32_t n, const float* __restrict__ reach,
+                                                  uint32_t n, const float* __restrict__ reach, uint32_t res,
                                                   const float4* __restrict__ cone, const float* __restrict__ cone_sin,
                                                   uint16_t* line)
 {
@@ -230,12 +235,12 @@ __global__ void __launch_bounds__(256) k_db_build(const float4* __restrict__ sph
     }
 
     // pass 2: one warp per cell
-    for (uint32_t c = warp; c < kLbRes * kLbRes; c += 8u) {
-        const uint32_t cell = f * kLbRes * kLbRes + c;
+    for (uint32_t c = warp; c < res * res; c += 8u) {
+        const uint32_t cell = f * res * res + c;
         const float4 cc = cone[cell];
         const float3 ctr = make_float3(cc.x, cc.y, cc.z);
         const float ch = cc.w, sh = cone_sin[cell];
-        const uint32_t id = i * kLbCells + cell;
+        const uint32_t id = i * cells_for(res) + cell;
         uint16_t* out = line + (size_t)id * kLbLine + 1;
         uint32_t cnt = 0;
         for (uint32_t base = 0; base < nc && cnt <= kLbMaxList; base += 32u) {
@@ -257,46 +262,50 @@ __global__ void __launch_bounds__(256) k_db_build(const float4* __restrict__ sph
 
 }  // namespace
 
-uint64_t lb_bytes(uint32_t nl)
+uint64_t lb_bytes(uint32_t nl, uint32_t res)
 {
-    const uint64_t cells = (uint64_t)nl * kLbCells;
-    return up(cells * kLbLine * sizeof(uint16_t)) + up(nl * sizeof(float)) + kConeBytes + 256;
+    const uint64_t cells = (uint64_t)nl * cells_for(res);
+    return up(cells * kLbLine * sizeof(uint16_t)) + up(nl * sizeof(float)) + cone_bytes(res) + 256;
 }
 
 cudaError_t lb_build(const float4* sph, const float* radius, uint32_t n, const DevLight* lights, uint32_t nl,
-                     void* buf, uint64_t bytes, LightBufferView* out, cudaStream_t stream)
+                     uint32_t res, void* buf, uint64_t bytes, LightBufferView* out, cudaStream_t stream)
 {
-    if (nl == 0 || nl > kLbMaxLights || n == 0 || n > kLbMaxSpheres || bytes < lb_bytes(nl))
+    if (nl == 0 || nl > kLbMaxLights || n == 0 || n > kLbMaxSpheres || res < kCellResMin || res > kCellResMax ||
+        bytes < lb_bytes(nl, res))
         return cudaErrorInvalidValue;
-    const uint64_t cells = (uint64_t)nl * kLbCells;
+    const uint64_t cells = (uint64_t)nl * cells_for(res);
     unsigned char* p = static_cast<unsigned char*>(buf);
     uint16_t* line = reinterpret_cast<uint16_t*>(p);
     p += up(cells * kLbLine * sizeof(uint16_t));
     float* dcap = reinterpret_cast<float*>(p);
     p += up(nl * sizeof(float));
     float4* cone = reinterpret_cast<float4*>(p);
-    float* cone_sin = reinterpret_cast<float*>(p + up(kLbCells * sizeof(float4)));
-    k_cell_cones<<<(kLbCells + 255) / 256, 256, 0, stream>>>(cone, cone_sin);
+    float* cone_sin = reinterpret_cast<float*>(p + up(cells_for(res) * sizeof(float4)));
+    k_cell_cones<<<(cells_for(res) + 255) / 256, 256, 0, stream>>>(res, cone, cone_sin);
     k_lb_dcap<<<nl, 256, 0, stream>>>(sph, radius, n, lights, dcap);
-    k_lb_build<<<(unsigned)((cells * 32 + 255) / 256), 256, 0, stream>>>(sph, radius, n, lights, nl, dcap, cone,
-                                                                       cone_sin, line);
+    k_lb_build<<<(unsigned)((cells * 32 + 255) / 256), 256, 0, stream>>>(sph, radius, n, lights, nl, dcap, res,
+                                                                       cone, cone_sin, line);
     out->line = line;
     out->dcap = dcap;
     out->n_lights = nl;
+    out->res = res;
     return cudaGetLastError();
 }
 
-uint64_t db_bytes(uint32_t n)
+uint64_t db_bytes(uint32_t n, uint32_t res)
 {
-    const uint64_t cells = (uint64_t)n * kLbCells;
-    return up(cells * kLbLine * sizeof(uint16_t)) + up(n * sizeof(float)) + up(sizeof(float)) + kConeBytes + 256;
+    const uint64_t cells = (uint64_t)n * cells_for(res);
+    return up(cells * kLbLine * sizeof(uint16_t)) + up(n * sizeof(float)) + up(sizeof(float)) + cone_bytes(res) +
+           256;
 }
 
-cudaError_t db_build(const float4* sph, const float* radius, uint32_t n, void* buf, uint64_t bytes,
+cudaError_t db_build(const float4* sph, const float* radius, uint32_t n, uint32_t res, void* buf, uint64_t bytes,
                      DirBufferView* out, cudaStream_t stream)
 {
-    if (n == 0 || n > kDbMaxSpheres || bytes < db_bytes(n)) return cudaErrorInvalidValue;
-    const uint64_t cells = (uint64_t)n * kLbCells;
+    if (n == 0 || n > kDbMaxSpheres || res < kCellResMin || res > kCellResMax || bytes < db_bytes(n, res))
+        return cudaErrorInvalidValue;
+    const uint64_t cells = (uint64_t)n * cells_for(res);
     unsigned char* p = static_cast<unsigned char*>(buf);
     uint16_t* line = reinterpret_cast<uint16_t*>(p);
     p += up(cells * kLbLine * sizeof(uint16_t));
@@ -305,14 +314,15 @@ cudaError_t db_build(const float4* sph, const float* radius, uint32_t n, void* b
     float* ext = reinterpret_cast<float*>(p);
     p += up(sizeof(float));
     float4* cone = reinterpret_cast<float4*>(p);
-    float* cone_sin = reinterpret_cast<float*>(p + up(kLbCells * sizeof(float4)));
-    k_cell_cones<<<(kLbCells + 255) / 256, 256, 0, stream>>>(cone, cone_sin);
+    float* cone_sin = reinterpret_cast<float*>(p + up(cells_for(res) * sizeof(float4)));
+    k_cell_cones<<<(cells_for(res) + 255) / 256, 256, 0, stream>>>(res, cone, cone_sin);
     k_db_extent<<<1, 256, 0, stream>>>(sph, radius, n, ext);
     k_db_reach<<<(n + 255) / 256, 256, 0, stream>>>(radius, n, ext, reach);
-    k_db_build<<<n * 6u, 256, 0, stream>>>(sph, radius, n, reach, cone, cone_sin, line);
+    k_db_build<<<n * 6u, 256, 0, stream>>>(sph, radius, n, reach, res, cone, cone_sin, line);
     out->line = line;
     out->reach = reach;
     out->n = n;
+    out->res = res;
     return cudaGetLastError();
 }
 

@@ -11,22 +11,24 @@
 
 namespace atx {
 
-// Device bytes lb_build needs for nl lights.
-uint64_t lb_bytes(uint32_t nl);
+// Device bytes lb_build needs for nl lights at res cells along a face's edge.
+uint64_t lb_bytes(uint32_t nl, uint32_t res);
 
 // Builds the light buffer of the n spheres sph (cx, cy, cz, r*r) with radii
-// radius[] and the nl lights (1 <= nl <= kLbMaxLights, n <= kLbMaxSpheres)
-// into buf (lb_bytes(nl) bytes of device memory) on stream; *out views buf.
+// radius[] and the nl lights (1 <= nl <= kLbMaxLights, n <= kLbMaxSpheres),
+// res cells along a face's edge (kCellResMin..kCellResMax), into buf
+// (lb_bytes(nl, res) bytes of device memory) on stream; *out views buf.
 cudaError_t lb_build(const float4* sph, const float* radius, uint32_t n, const DevLight* lights, uint32_t nl,
-                     void* buf, uint64_t bytes, LightBufferView* out, cudaStream_t stream);
+                     uint32_t res, void* buf, uint64_t bytes, LightBufferView* out, cudaStream_t stream);
 
-// Device bytes db_build needs for n spheres.
-uint64_t db_bytes(uint32_t n);
+// Device bytes db_build needs for n spheres at res cells along a face's edge.
+uint64_t db_bytes(uint32_t n, uint32_t res);
 
 // Builds the direction buffer of the n spheres sph (cx, cy, cz, r*r) with
-// radii radius[] (1 <= n <= kDbMaxSpheres) into buf (db_bytes(n) bytes of
-// device memory) on stream; *out views buf.
-cudaError_t db_build(const float4* sph, const float* radius, uint32_t n, void* buf, uint64_t bytes,
+// radii radius[] (1 <= n <= kDbMaxSpheres), res cells along a face's edge,
+// into buf (db_bytes(n, res) bytes of device memory) on stream; *out views
+// buf.
+cudaError_t db_build(const float4* sph, const float* radius, uint32_t n, uint32_t res, void* buf, uint64_t bytes,
                      DirBufferView* out, cudaStream_t stream);
 
 }  // namespace atx

@@ -99,24 +99,51 @@ atx_status SceneStore::upload(const atx_sphere* s, uint32_t n, const atx_materia
     } else {
         bvh.reset();
     }
+    ATX_TRY(build_cells(budget, stream));
+    ATX_CUDA(cudaStreamSynchronize(stream));
+    return ATX_OK;
+}
+
+atx_status SceneStore::build_cells(Budget* budget, cudaStream_t stream)
+{
+    const uint32_t n = view.n_sph, nl = view.n_lights;
+    const uint32_t res = cell_res ? cell_res : default_cell_res(n);
     // light buffer for the shadow rays of the brute-force tables
+    view.lb = LightBufferView{};
     if (!view.use_bvh && n >= 1 && n <= kLbMaxSpheres && nl >= 1 && nl <= kLbMaxLights) {
-        ATX_TRY(lbuf.ensure(lb_bytes(nl), budget, "light buffer"));
+        ATX_TRY(lbuf.ensure(lb_bytes(nl, res), budget, "light buffer"));
         LightBufferView lv{};
-        ATX_CUDA(lb_build(view.sph, sph_rad.as<float>(), n, view.lights, nl, lbuf.get(), lbuf.bytes(), &lv, stream));
+        ATX_CUDA(lb_build(view.sph, sph_rad.as<float>(), n, view.lights, nl, res, lbuf.get(), lbuf.bytes(), &lv,
+                          stream));
         view.lb = lv;
     } else {
         lbuf.reset();
     }
     // direction buffer for the extension rays of the brute-force tables
+    view.db = DirBufferView{};
     if (!view.use_bvh && n >= 1 && n <= kDbMaxSpheres) {
-        ATX_TRY(dbuf.ensure(db_bytes(n), budget, "direction buffer"));
+        ATX_TRY(dbuf.ensure(db_bytes(n, res), budget, "direction buffer"));
         DirBufferView dv{};
-        ATX_CUDA(db_build(view.sph, sph_rad.as<float>(), n, dbuf.get(), dbuf.bytes(), &dv, stream));
+        ATX_CUDA(db_build(view.sph, sph_rad.as<float>(), n, res, dbuf.get(), dbuf.bytes(), &dv, stream));
         view.db = dv;
     } else {
         dbuf.reset();
     }
+    return ATX_OK;
+}
+
+uint32_t SceneStore::cells() const
+{
+    return view.db.n ? view.db.res : view.lb.n_lights ? view.lb.res : 0u;
+}
+
+atx_status SceneStore::rebuild_cells(uint32_t res, Budget* budget, cudaStream_t stream)
+{
+    if (res && (res < kCellResMin || res > kCellResMax))
+        return fail(ATX_ERR_INVALID_ARG, "cell resolution %u outside %u..%u", res, kCellResMin, kCellResMax);
+    cell_res = res;
+    if (cells() == 0 || cells() == (res ? res : default_cell_res(view.n_sph))) return ATX_OK;
+    ATX_TRY(build_cells(budget, stream));
     ATX_CUDA(cudaStreamSynchronize(stream));
     return ATX_OK;
 }
@@ -399,6 +426,7 @@ atx_status Renderer::set_scene(const atx_sphere* s, uint32_t n, const atx_materi
     masks_valid_ = false;
     prev_cam_valid_ = false;
     scene_.bvh_leaf = tune_.bvh_leaf_size ? tune_.bvh_leaf_size : cfg_.bvh_leaf_size;
+    scene_.cell_res = tune_.cell_res;
     return scene_.upload(s, n, m, nm, l, nl, &budget_, stream_);
 }
 
@@ -819,6 +847,8 @@ atx_status Renderer::set_tuning(const atx_tuning& t)
         return fail(ATX_ERR_INVALID_ARG, "tuning: threads must be a multiple of 32 up to 256");
     if (t.bvh_leaf_size > 64u) return fail(ATX_ERR_INVALID_ARG, "tuning: leaf size above 64");
     if (t.path_kernel > 2u) return fail(ATX_ERR_INVALID_ARG, "tuning: path_kernel is 0, 1 or 2");
+    if (t.cell_res && (t.cell_res < kCellResMin || t.cell_res > kCellResMax))
+        return fail(ATX_ERR_INVALID_ARG, "tuning: cell_res is 0 or %u..%u", kCellResMin, kCellResMax);
     ATX_TRY(activate());
     ATX_TRY(join());
     ATX_CUDA(cudaStreamSynchronize(stream_));
@@ -829,6 +859,9 @@ atx_status Renderer::set_tuning(const atx_tuning& t)
         masks_valid_ = false;       // the tile candidate lists walk the tree
         prev_cam_valid_ = false;
     }
+    // light and direction buffers at another resolution (the lists change,
+    // the frames do not)
+    if (t.cell_res != tune_.cell_res) ATX_TRY(scene_.rebuild_cells(t.cell_res, &budget_, stream_));
     if (t.threads != tune_.threads || t.path_kernel != tune_.path_kernel) shape_valid_ = false;
     tune_ = t;
     tune_.from_cache = 0;
@@ -840,6 +873,7 @@ atx_status Renderer::tuning(atx_tuning* out)
 {
     *out = tune_;
     out->bvh_leaf_size = scene_.leaf_size();
+    out->cell_res = scene_.cells();
     return ATX_OK;
 }
 
@@ -947,6 +981,12 @@ atx_status Renderer::autotune(uint32_t spp, uint32_t passes, bool use_cache, atx
         t.threads = threads;
         ATX_TRY(trial(t));
     }
+    if (!sv.use_bvh && (sv.db.n || sv.lb.n_lights))   // cells of the light and direction buffers
+        for (uint32_t res : {16u, 24u, 32u}) {
+            atx_tuning t = best;
+            t.cell_res = res;
+            ATX_TRY(trial(t));
+        }
     if (!sv.use_bvh && sv.n_sph <= 256u)   // whole paths in one thread against the wavefront stages
         for (uint32_t pk : {1u, 2u}) {
             atx_tuning t = best;

@@ -18,6 +18,7 @@ struct SceneStore {
     SceneView view{};
     uint32_t bvh_threshold = 0;
     uint32_t bvh_leaf = 0;
+    uint32_t cell_res = 0;   // cells along a face's edge of the light and direction buffers (0: default_cell_res)
     const StreamOrder* order = nullptr;   // stream-ordered allocation (batches); nullptr: cudaMalloc
 
     // Validates, converts and uploads on stream (Renderer.cu:25-57).
@@ -27,6 +28,14 @@ struct SceneStore {
     // the resident sphere table; results are unchanged (the walk is exact).
     atx_status rebuild_bvh(uint32_t leaf, cudaStream_t stream);
     uint32_t leaf_size() const;
+    // Rebuilds the light and direction buffers (when the scene has them) with
+    // res cells along a face's edge (0: default_cell_res); results are
+    // unchanged (every cell's list holds whatever a ray in it can meet).
+    atx_status rebuild_cells(uint32_t res, Budget* budget, cudaStream_t stream);
+    // The buffers' cells along a face's edge (0: the scene has neither).
+    uint32_t cells() const;
+    // Builds the light and direction buffers of the uploaded tables at cell_res.
+    atx_status build_cells(Budget* budget, cudaStream_t stream);
     uint64_t device_bytes() const
     {
         return sph.bytes() + sph_mat.bytes() + sph_rad.bytes() + mat.bytes() + lights.bytes() + bvh.bytes() +

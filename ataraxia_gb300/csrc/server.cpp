@@ -36,7 +36,7 @@ bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1])
 // and its read-backs; result buffers are page-locked, cached by size.
 class BatchExecutor : public Executor {
 public:
-    explicit BatchExecutor(const atx_config& cfg) : b_(cfg), device_(cfg.device) {}
+    explicit BatchExecutor(const atx_config& cfg) : b_(cfg), device_(cfg.device) { b_.set_cell_res(kCellResJobs); }
     ~BatchExecutor() override
     {
         if (cudaSetDevice(device_) != cudaSuccess) return;
@@ -293,8 +293,8 @@ uint64_t Server::job_bytes(const atx_batch_scene& s, uint32_t bvh_threshold)
     if (bvh) b += up256(lbvh_bytes((uint32_t)n));
     // light and direction buffers, as SceneStore::upload builds them
     if (!bvh && n >= 1 && n <= kLbMaxSpheres && s.n_lights >= 1 && s.n_lights <= kLbMaxLights)
-        b += up256(lb_bytes(s.n_lights));
-    if (!bvh && n >= 1 && n <= kDbMaxSpheres) b += up256(db_bytes((uint32_t)n));
+        b += up256(lb_bytes(s.n_lights, kCellResJobs));
+    if (!bvh && n >= 1 && n <= kDbMaxSpheres) b += up256(db_bytes((uint32_t)n, kCellResJobs));
     const uint64_t px = (uint64_t)s.width * s.height;
     b += up256(16 * px) + up256(4 * px) + up256(8 * px) + up256(16 * px);   // accumulator, image, primary hits, directions
     return b;

@@ -376,9 +376,9 @@ __device__ __forceinline__ bool occluded_cone(const float4* __restrict__ sph, ui
 
 // Cell of direction w around a light, as light_buffer.cu lays out the cube:
 // the face of the largest |component| (+x, -x, +y, -y, +z, -z), then the other
-// two components over it (in [-1, 1]) on a kLbRes grid.  -1 for a zero or
+// two components over it (in [-1, 1]) on a res x res grid.  -1 for a zero or
 // non-finite w.
-__device__ __forceinline__ int lb_cell(float3 w)
+__device__ __forceinline__ int lb_cell(float3 w, uint32_t res)
 {
     const float ax = fabsf(w.x), ay = fabsf(w.y), az = fabsf(w.z);
     uint32_t face;
@@ -394,10 +394,10 @@ __device__ __forceinline__ int lb_cell(float3 w)
         m = az, a = w.x, b = w.y;
     }
     if (!(m > 0.0f && m < 3.0e38f) || !(fabsf(a) <= m && fabsf(b) <= m)) return -1;
-    const float h = 0.5f * (float)kLbRes / m;
-    const int i = min((int)((a + m) * h), (int)kLbRes - 1);
-    const int j = min((int)((b + m) * h), (int)kLbRes - 1);
-    return (int)((face * kLbRes + (uint32_t)i) * kLbRes + (uint32_t)j);
+    const float h = 0.5f * (float)res / m;
+    const int i = min((int)((a + m) * h), (int)res - 1);
+    const int j = min((int)((b + m) * h), (int)res - 1);
+    return (int)((face * res + (uint32_t)i) * res + (uint32_t)j);
 }
 
 // The spheres of a cell line (words 1..count after the count in word 0):
@@ -432,9 +432,9 @@ __device__ __forceinline__ bool occluded_lb(const SceneView& sc, const float4* _
     const float4 l0 = __ldg(reinterpret_cast<const float4*>(sc.lights + li));
     const float3 w = mk3(o.x - l0.x, o.y - l0.y, o.z - l0.z);
     const float dc = __ldg(&sc.lb.dcap[li]);
-    const int cell = dot3(w, w) <= dc * dc ? lb_cell(w) : -1;
+    const int cell = dot3(w, w) <= dc * dc ? lb_cell(w, sc.lb.res) : -1;
     if (cell < 0) return occluded_brute<SMEM>(sph, sc.n_sph, o, d, dist2);
-    const uint16_t* line = sc.lb.line + (size_t)(li * kLbCells + (uint32_t)cell) * kLbLine;
+    const uint16_t* line = sc.lb.line + ((size_t)li * cells_for(sc.lb.res) + (uint32_t)cell) * kLbLine;
     const uint4 h = __ldg(reinterpret_cast<const uint4*>(line));
     const uint32_t cnt = h.x & 0xffffu;
     if (cnt == kLbAll) return occluded_brute<SMEM>(sph, sc.n_sph, o, d, dist2);
@@ -455,9 +455,9 @@ template <bool SMEM>
 __device__ __forceinline__ int32_t nearest_db(const SceneView& sc, const float4* __restrict__ sph, uint32_t own,
                                               float3 o, float3 d, float& tmin)
 {
-    const int cell = own < sc.db.n ? lb_cell(d) : -1;
+    const int cell = own < sc.db.n ? lb_cell(d, sc.db.res) : -1;
     if (cell < 0) return nearest_brute<SMEM>(sph, sc.n_sph, o, d, tmin);
-    const uint16_t* line = sc.db.line + (size_t)(own * kLbCells + (uint32_t)cell) * kLbLine;
+    const uint16_t* line = sc.db.line + ((size_t)own * cells_for(sc.db.res) + (uint32_t)cell) * kLbLine;
     const uint4 h = __ldg(reinterpret_cast<const uint4*>(line));
     const uint32_t cnt = h.x & 0xffffu;
     if (cnt == kLbAll) return nearest_brute<SMEM>(sph, sc.n_sph, o, d, tmin);

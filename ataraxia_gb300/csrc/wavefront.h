@@ -51,7 +51,7 @@ struct BvhView {
 
 // Light buffer (Haines and Greenberg's light buffer, 1986) for the
 // brute-force sphere tables: for each point light a cube of directions around
-// it, 6 faces of kLbRes x kLbRes cells, and for each cell the spheres that can
+// it, 6 faces of res x res cells, and for each cell the spheres that can
 // block a shadow ray towards that light whose origin, seen from the light,
 // lies in the cell (built by light_buffer.cu).  A shadow ray then tests the
 // spheres of one cell instead of the whole table.
@@ -59,17 +59,32 @@ struct BvhView {
 // listed (or kLbAll when they did not fit), words 1.. their indices in
 // ascending order, so the count and the first seven indices arrive in one
 // 16-byte load.
-constexpr uint32_t kLbRes = 16;
-constexpr uint32_t kLbCells = 6 * kLbRes * kLbRes;
+// res, the cells along a face's edge, is a property of each buffer: finer
+// cells list fewer spheres (the 256-sphere scene: 2.9 per extension-ray
+// lookup and 8.7 for a warp's longest list at 16; at 32 the longest about 30%
+// shorter) and cost more to build and hold (four times the lines at 32).
+constexpr uint32_t kCellResMin = 8;
+constexpr uint32_t kCellResMax = 32;
+constexpr uint32_t kCellResDefault = 32;   // a renderer's and a batch's resident scenes
+constexpr uint32_t kCellResJobs = 16;      // the server's jobs (tables built per job)
+// Up to this many spheres the lists are about one sphere already at 16, and
+// finer cells only make the tables larger (the 9-sphere scene: -1% at 32).
+constexpr uint32_t kCellResFewSpheres = 64;
+__host__ __device__ constexpr uint32_t default_cell_res(uint32_t n_spheres)
+{
+    return n_spheres <= kCellResFewSpheres ? 16u : kCellResDefault;
+}
+__host__ __device__ constexpr uint32_t cells_for(uint32_t res) { return 6u * res * res; }
 constexpr uint32_t kLbLine = 32;                 // 16-bit words per cell
 constexpr uint32_t kLbMaxList = kLbLine - 1;     // spheres a cell can list
 constexpr uint32_t kLbMaxLights = 64;
 constexpr uint32_t kLbMaxSpheres = 65534;        // indices are 16-bit, 0xffff is kLbAll
 constexpr uint32_t kLbAll = 0xffff;              // the cell's list overflowed: test every sphere
 struct LightBufferView {
-    const uint16_t* line;    // [n_lights * kLbCells * kLbLine] cell lines
+    const uint16_t* line;    // [n_lights * cells_for(res) * kLbLine] cell lines
     const float* dcap;       // [n_lights] the lists hold for shadow-ray origins within dcap of the light
     uint32_t n_lights;       // 0: no light buffer
+    uint32_t res;            // cells along a face's edge
 };
 
 // Direction buffer for the extension rays of the brute-force tables (ray
@@ -79,11 +94,12 @@ struct LightBufferView {
 // sphere in a direction of the cell can hit (built by light_buffer.cu).
 // Every extension ray after the first bounce leaves the sphere its path last
 // hit, so its nearest hit tests the spheres of one cell.
-constexpr uint32_t kDbMaxSpheres = 1024;   // 100 KB of cells per sphere
+constexpr uint32_t kDbMaxSpheres = 1024;   // 393 KB of cells per sphere at res 32
 struct DirBufferView {
-    const uint16_t* line;    // [n * kLbCells * kLbLine] cell lines, as the light buffer's
+    const uint16_t* line;    // [n * cells_for(res) * kLbLine] cell lines, as the light buffer's
     const float* reach;      // [n] the lists hold for ray origins within reach of the sphere's centre
     uint32_t n;              // spheres covered; 0: no direction buffer
+    uint32_t res;            // cells along a face's edge
 };
 
 // Shadow-ray records carry the sphere the ray leaves from and the light it

@@ -296,7 +296,10 @@ def run_ours(args, dist: Dist):
 
     e2e_s = e2e_run(frame_step)
 
-    # the same with the scene uploaded every step (tables, light and direction buffers rebuilt)
+    # the same with the scene uploaded every step (tables, light and direction buffers rebuilt, at the
+    # cheaper 16 cells along a face's edge that suit one render per scene)
+    r.set_tuning(cell_res=16)
+
     def scene_step():
         r.set_scene(sph, mats, lts)
         frame_step()
@@ -313,6 +316,8 @@ def run_ours(args, dist: Dist):
                    "clock stops; scene resident (uploaded once, as the reference's Render loop re-uploads it only "
                    "for a new scene or frame 1)",
            "with_scene_upload": {"value": round(dist.world * args.steps * paths_step / e2e_scene_s / 1e6, 2),
+                                 "what": "atx_set_scene every step as well (light and direction buffers rebuilt, "
+                                         "16 cells along a face's edge)",
                                  "h2d_bytes_per_step": CAMERA_BYTES + h2d_scene,
                                  "ms_per_step": round(e2e_scene_s * 1e3 / args.steps, 3)}}
     _ = host_img
@@ -496,7 +501,8 @@ def batch_compare(args, dev: int, steps: int) -> dict:
     one batched pass (all scenes, one CUDA graph) per step.  The plain arm is timed two ways: the device
     time of its render calls alone (CUDA events around each launch, the scene already set), and as a
     caller sees it (wall clock over the whole loop: per scene resize, scene upload with its acceleration
-    structures, camera, settings, the launch and the RGBA8 read-back).  gpu_idle_frac = the share of the
+    structures, camera, settings, the launch and the RGBA8 read-back; built with the cheaper 16 cells
+    along a face's edge, which suit one render per scene).  gpu_idle_frac = the share of the
     caller's loop in which no render kernel of the plain arm runs.  saturated_ceiling = the mix's paths
     over the device time they take when every scene is rendered alone in launches of at least 64 Mi
     paths: what a launch structure that keeps each path's work can approach."""
@@ -519,6 +525,10 @@ def batch_compare(args, dev: int, steps: int) -> dict:
     plain_ms = 0.0
     caller_s = 0.0
     for rep in range(3):                       # rep 0 warms up (allocations, BVH builds)
+        if rep == 2:
+            # a caller that renders each scene once does best with the cheaper light and direction buffers
+            # (16 cells along a face's edge, the server's choice for its jobs)
+            r.set_tuning(cell_res=16)
         t0 = time.perf_counter()
         for sc in mix:
             r.on_resize(sc.width, sc.height)
@@ -841,12 +851,14 @@ def serve_batched(jobs, duration, args, policy="arrival"):
 
 def serve_fifo(jobs, duration, max_pending):
     """One launch per job in arrival order on the plain renderer, image read back after each; jobs
-    arriving while max_pending jobs wait are rejected, as the server's queue bound does."""
+    arriving while max_pending jobs wait are rejected, as the server's queue bound does.  Light and
+    direction buffers at 16 cells along a face's edge, the server's setting for jobs rendered once."""
     from collections import deque
 
     import ataraxia_gb300 as atx
 
     r = atx.Renderer()
+    r.set_tuning(cell_res=16)
     wall0 = time.perf_counter()
     lat, paths, rejected = [], 0, 0
     queue, nxt = deque(), 0

@@ -249,6 +249,10 @@ typedef struct atx_tuning {
                                   stages, 2: whole paths in one thread (brute-force tables; LBVH scenes keep the
                                   wavefront) */
     uint32_t from_cache;       /* atx_autotune: 1 when the setting came from the process-wide cache */
+    uint32_t cell_res;         /* direction cells along a cube face's edge of the light and direction buffers
+                                  (scenes on the brute-force tables; 8..32, 0 = 16 up to 64 spheres, else 32):
+                                  finer cells list fewer spheres per shadow and extension ray and take longer to
+                                  build */
     double ms;                 /* atx_autotune: device time of one render with the chosen setting */
 } atx_tuning;
 

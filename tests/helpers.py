@@ -66,6 +66,7 @@ def job_bytes_bound(sc):
     px = sc.width * sc.height
     tables = 24 * n + 48 * len(sc.materials) + 32 * nl + 8 * 256
     bvh = 264 * n if n >= 1025 else 0
+    # the server builds its jobs' light and direction buffers at 16 cells along a cube face's edge
     cells = 6 * 16 * 16 * 65          # per light / per sphere: a count and 32 indices per direction cell
     cones = 6 * 16 * 16 * 20 + 4096   # build scratch: the cells' bounding cones
     lb = cells * nl + cones if n < 1025 and 1 <= nl <= 64 else 0

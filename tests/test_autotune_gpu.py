@@ -1,7 +1,8 @@
 """The launch tuner (atx_autotune / atx_set_tuning): every setting it can pick renders the same frames
-bit for bit (the LBVH walk is exact for any leaf size; lanes, path state, block size and wave shape
-only change how the same paths are scheduled), the tuner keeps one of them, and its cache answers a
-second call for the same GPU and workload bucket without timing."""
+bit for bit (the LBVH walk is exact for any leaf size, the light and direction buffers' lists for any
+cell resolution; lanes, path state, block size and wave shape only change how the same paths are
+scheduled), the tuner keeps one of them, and its cache answers a second call for the same GPU and
+workload bucket without timing."""
 import numpy as np
 import pytest
 
@@ -12,8 +13,8 @@ pytestmark = pytest.mark.gpu
 
 SETTINGS = [dict(), dict(bvh_leaf_size=4), dict(bvh_leaf_size=8), dict(bvh_leaf_size=32), dict(lanes=1),
             dict(lanes=2), dict(lanes=4), dict(wave_paths=1 << 20), dict(threads=128), dict(wave_spp=1),
-            dict(path_kernel=1), dict(path_kernel=2),
-            dict(bvh_leaf_size=12, lanes=4, wave_paths=4 << 20, threads=128, wave_spp=4)]
+            dict(path_kernel=1), dict(path_kernel=2), dict(cell_res=8), dict(cell_res=16), dict(cell_res=24),
+            dict(bvh_leaf_size=12, lanes=4, wave_paths=4 << 20, threads=128, wave_spp=4, cell_res=16)]
 
 
 def _scene(kind):
@@ -48,15 +49,20 @@ def test_every_tuning_renders_the_same_frames(po, kind):
             got = r.tuning()
             if kind == "lbvh" and "bvh_leaf_size" in t:
                 assert got["bvh_leaf_size"] == t["bvh_leaf_size"]
+            # the brute-force scene (256 spheres) has light and direction buffers, by default with 32 cells
+            # along a face's edge
+            assert got["cell_res"] == (0 if kind == "lbvh" else t.get("cell_res", 32))
             acc, img = _render(r, sc, spp)
             assert bit_mismatches(acc, ref_acc) == 0, t
             assert np.array_equal(img, ref_img), t
         r.set_tuning()
         # the scene set again keeps a tuned leaf size
-        r.set_tuning(bvh_leaf_size=8)
+        r.set_tuning(bvh_leaf_size=8, cell_res=16)
         r.set_scene(sc.spheres, sc.materials, sc.lights)
         if kind == "lbvh":
             assert r.tuning()["bvh_leaf_size"] == 8
+        else:
+            assert r.tuning()["cell_res"] == 16
         acc, _ = _render(r, sc, spp)
         assert bit_mismatches(acc, ref_acc) == 0
 
@@ -81,3 +87,16 @@ def test_autotune_picks_a_setting_and_caches_it():
         assert t2["from_cache"] == 1
         assert {k: t2[k] for k in ("bvh_leaf_size", "lanes", "wave_paths", "threads", "wave_spp", "path_kernel")} == \
                {k: t1[k] for k in ("bvh_leaf_size", "lanes", "wave_paths", "threads", "wave_spp", "path_kernel")}
+
+
+@pytest.mark.parametrize("res", [4, 7, 33, 64])
+def test_cell_resolution_outside_its_range_is_rejected(res):
+    from ataraxia_gb300 import AtxError
+
+    sc = scenes.config1().with_resolution(64, 36)
+    with Renderer() as r:
+        r.on_resize(sc.width, sc.height)
+        r.set_scene(sc.spheres, sc.materials, sc.lights)
+        with pytest.raises(AtxError):
+            r.set_tuning(cell_res=res)
+        assert r.tuning()["cell_res"] == 32
