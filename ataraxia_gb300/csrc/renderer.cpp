@@ -877,32 +877,43 @@ atx_status Renderer::tuning(atx_tuning* out)
     return ATX_OK;
 }
 
-// Device time per render of `passes` renders issued back to back, as a caller
-// renders: one interval on stream_ from before the first to after the last
-// (with overlapped renders a render's own events would also hold the
-// previous render's lanes).
+// Device time per render of renders issued back to back, as a caller renders:
+// one interval on stream_ from before the first to after the last (with
+// overlapped renders a render's own events would also hold the previous
+// render's lanes).  The interval holds at least `passes` renders and about
+// 20 ms of them: in a shorter one the first render's start and the last one's
+// unoverlapped tail weigh enough to favour settings that overlap less (0.3 ms
+// renders of the 256-sphere scene: two lanes over four in three renders).
 atx_status Renderer::time_renders(uint32_t spp, uint32_t passes, double* ms)
 {
     frame_ = 1;
     ATX_TRY(render(spp));   // the per-camera tables are built on the second render of a camera
     ATX_TRY(render(spp));
-    ATX_TRY(join());
     cudaEvent_t ev[2] = {nullptr, nullptr};
     cudaError_t e = cudaEventCreate(&ev[0]);
     if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[0], stream_);
     atx_status s = ATX_OK;
-    if (e == cudaSuccess) {
-        for (uint32_t k = 0; k < passes && s == ATX_OK; ++k) s = render(spp);
+    auto block = [&](uint32_t k, double* per) {
         if (s == ATX_OK) s = join();
-        if (s == ATX_OK) {
-            e = cudaEventRecord(ev[1], stream_);
-            if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
-            float t = 0.0f;
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
-            *ms = (double)t / passes;
-        }
+        if (s != ATX_OK || e != cudaSuccess) return;
+        e = cudaEventRecord(ev[0], stream_);
+        for (uint32_t i = 0; i < k && s == ATX_OK && e == cudaSuccess; ++i) s = render(spp);
+        if (s == ATX_OK) s = join();
+        if (s != ATX_OK || e != cudaSuccess) return;
+        e = cudaEventRecord(ev[1], stream_);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+        float t = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+        *per = (double)t / k;
+    };
+    double per = 0.0;
+    block(passes, &per);
+    constexpr double kBlockMs = 20.0;
+    if (s == ATX_OK && e == cudaSuccess && per > 0.0 && per * passes < kBlockMs) {
+        const uint32_t k = (uint32_t)std::min(256.0, std::ceil(kBlockMs / per));
+        if (k > passes) block(k, &per);
     }
+    *ms = per;
     for (cudaEvent_t x : ev)
         if (x) cudaEventDestroy(x);
     ATX_TRY(s);
