@@ -405,9 +405,9 @@ def run_ours(args, dist: Dist):
                                     "2 FMUL2 + 4 FFMA2 thread instructions of one launch's kernels)",
                     "peak_source": "baseline/fp32_peak.cu: register-resident FFMA chains on every SM of this GPU, "
                                    "best of five launches"}
-        # the work the survey defines as algorithmic for brute-force scenes: every ray tests every sphere
-        # (20 FLOP per test, FMA as 2) plus 120 per shaded hit; the tile masks, light and direction
-        # buffers skip most of those tests, so this rate can exceed the pipe's peak
+        # the algorithmic work of brute-force scenes: every ray tests every sphere (20 FLOP per test, FMA
+        # as 2) plus 120 per shaded hit; the tile masks, light and direction buffers skip most of those
+        # tests, so this rate can exceed the pipe's peak
         rays_launch = (ext_after0 + sc.pixels * prof_steps + sh_rays) / prof_steps
         shaded_launch = (shaded0 + ext_after0) / prof_steps
         bf = rays_launch * len(sc.spheres) * 20 + shaded_launch * 120
